@@ -1,0 +1,339 @@
+"""CPU ORACLE -- test infrastructure only.
+
+numpy/ctypes front end over the C restatement in zc_oracle.c. Only the tests,
+`__graft_entry__.smoke()` and the bench's CPU-baseline leg import this module;
+the product (`zorch_gb300`) never does. Field values are Montgomery u32 (the
+storage of zk_dtypes' *_mont dtypes), canonical values are converted with
+`to_mont` / `from_mont`.
+
+Parity: Poseidon2/sponge/compression/Merkle are pinned to the reference's
+Plonky3 KoalaBear-16 golden (tests/golden/koalabear16.json); the BabyBear
+Poseidon2 instance is project-defined, so BabyBear roots, challenges and proof
+bytes are "parity unpinned vs reference" (oracle == CUDA only).
+"""
+
+from __future__ import annotations
+
+import ctypes as C
+import json
+from dataclasses import dataclass
+from pathlib import Path
+
+import numpy as np
+
+from . import build as _build
+
+BABYBEAR, KOALABEAR = 0, 1
+P_BABYBEAR = 2013265921
+P_KOALABEAR = 2130706433
+MODULUS = {BABYBEAR: P_BABYBEAR, KOALABEAR: P_KOALABEAR}
+
+_u32p = np.ctypeslib.ndpointer(dtype=np.uint32, flags="C_CONTIGUOUS")
+_i32p = np.ctypeslib.ndpointer(dtype=np.int32, flags="C_CONTIGUOUS")
+
+
+def _load() -> C.CDLL:
+    lib = C.CDLL(str(_build.build()))
+    vp, i64, i32, u32 = C.c_void_p, C.c_int64, C.c_int, C.c_uint32
+    sig = {
+        "orc_set_threads": (None, [i32]),
+        "orc_get_threads": (i32, []),
+        "orc_modulus": (u32, [i32]),
+        "orc_to_mont": (u32, [i32, u32]),
+        "orc_from_mont": (u32, [i32, u32]),
+        "orc_mul": (u32, [i32, u32, u32]),
+        "orc_to_mont_vec": (None, [i32, _u32p, _u32p, i64]),
+        "orc_from_mont_vec": (None, [i32, _u32p, _u32p, i64]),
+        "orc_ef4_mul": (None, [i32, _u32p, _u32p, _u32p]),
+        "orc_root_of_unity": (u32, [i32, i32, u32]),
+        "orc_p2_size": (i32, []),
+        "orc_p2_babybear16": (None, [vp]),
+        "orc_p2_from_canonical": (None, [vp, i32, i32, i32, i32, _u32p, _u32p, _u32p, _u32p, u32]),
+        "orc_p2_export_canonical": (None, [vp, _u32p, _u32p, _u32p, _u32p]),
+        "orc_p2_permute": (None, [vp, _u32p]),
+        "orc_sponge_hash": (None, [vp, _u32p, i64, _u32p]),
+        "orc_compress": (None, [vp, _u32p, _u32p, _u32p]),
+        "orc_merkle_commit": (i32, [vp, _u32p, i64, i32, i32, i64, _u32p]),
+        "orc_merkle_open": (i32, [_u32p, i64, i32, i32, i64, _u32p, _i32p, i32, _u32p, _u32p]),
+        "orc_rs_encode": (i32, [i32, _u32p, i64, i32, i32, u32, u32, _u32p]),
+        "orc_rs_encode_horner": (i32, [i32, _u32p, i32, i32, u32, u32, _u32p]),
+        "orc_eval_domain": (None, [i32, i32, u32, u32, _u32p]),
+        "orc_fri_fold": (i32, [i32, _u32p, i64, i32, _u32p, i32, u32, u32, _u32p]),
+        "orc_duplex_init": (None, [vp]),
+        "orc_duplex_observe": (None, [vp, vp, _u32p, i64]),
+        "orc_duplex_sample": (None, [vp, vp, i32, _u32p]),
+        "orc_fri_commit_phase": (i32, [vp, i32, _u32p, i32, u32, u32, i32, i32, i32, vp,
+                                       _u32p, _u32p, _u32p, _i32p, _u32p, _u32p]),
+    }
+    for name, (res, args) in sig.items():
+        fn = getattr(lib, name)
+        fn.restype = res
+        fn.argtypes = args
+    return lib
+
+
+LIB = _load()
+
+
+def set_threads(n: int) -> None:
+    LIB.orc_set_threads(int(n))
+
+
+def threads() -> int:
+    return int(LIB.orc_get_threads())
+
+
+def u32(a) -> np.ndarray:
+    return np.ascontiguousarray(np.asarray(a, dtype=np.uint32))
+
+
+def to_mont(field: int, x) -> np.ndarray:
+    x = u32(x)
+    out = np.empty_like(x)
+    LIB.orc_to_mont_vec(field, x.reshape(-1), out.reshape(-1), x.size)
+    return out
+
+
+def from_mont(field: int, x) -> np.ndarray:
+    x = u32(x)
+    out = np.empty_like(x)
+    LIB.orc_from_mont_vec(field, x.reshape(-1), out.reshape(-1), x.size)
+    return out
+
+
+def root_of_unity(field: int, log_n: int, generator: int = 0) -> int:
+    return int(LIB.orc_root_of_unity(field, log_n, generator))
+
+
+class Poseidon2:
+    """A width-16 Poseidon2 parameterisation (constants stored Montgomery)."""
+
+    def __init__(self) -> None:
+        self._buf = C.create_string_buffer(int(LIB.orc_p2_size()))
+        self.ptr = C.cast(self._buf, C.c_void_p)
+        self.field = BABYBEAR
+
+    @classmethod
+    def babybear16(cls) -> "Poseidon2":
+        p = cls()
+        LIB.orc_p2_babybear16(p.ptr)
+        p.field = BABYBEAR
+        p.alpha, p.rounds_f_half, p.rounds_p = 7, 4, 13
+        return p
+
+    @classmethod
+    def from_canonical(cls, field, alpha, ext_init, ext_term, int_rc, diag, j_scale=1):
+        p = cls()
+        ext_init, ext_term = u32(ext_init).reshape(-1), u32(ext_term).reshape(-1)
+        int_rc, diag = u32(int_rc), u32(diag)
+        LIB.orc_p2_from_canonical(p.ptr, field, alpha, ext_init.size // 16, int_rc.size,
+                                  ext_init, ext_term, int_rc, diag, j_scale)
+        p.field, p.alpha = field, alpha
+        p.rounds_f_half, p.rounds_p = ext_init.size // 16, int_rc.size
+        return p
+
+    @classmethod
+    def koalabear16_golden(cls) -> "Poseidon2":
+        d = load_koalabear_fixture()
+        return cls.from_canonical(KOALABEAR, d["alpha"], d["external_initial"],
+                                  d["external_terminal"], d["internal_rc"],
+                                  d["internal_diag"], d["internal_j_scale"])
+
+    def export_canonical(self):
+        ei = np.zeros(self.rounds_f_half * 16, np.uint32)
+        et = np.zeros(self.rounds_f_half * 16, np.uint32)
+        ir = np.zeros(self.rounds_p, np.uint32)
+        dg = np.zeros(16, np.uint32)
+        LIB.orc_p2_export_canonical(self.ptr, ei, et, ir, dg)
+        return ei.reshape(-1, 16), et.reshape(-1, 16), ir, dg
+
+    def permute(self, state) -> np.ndarray:
+        s = u32(state).copy()
+        LIB.orc_p2_permute(self.ptr, s)
+        return s
+
+    def hash(self, row) -> np.ndarray:
+        row = u32(row).reshape(-1)
+        out = np.zeros(8, np.uint32)
+        LIB.orc_sponge_hash(self.ptr, row, row.size, out)
+        return out
+
+    def compress(self, left, right) -> np.ndarray:
+        out = np.zeros(8, np.uint32)
+        LIB.orc_compress(self.ptr, u32(left), u32(right), out)
+        return out
+
+
+def load_koalabear_fixture() -> dict:
+    path = Path(__file__).resolve().parent.parent / "tests" / "golden" / "koalabear16.json"
+    return json.loads(path.read_text())
+
+
+# ------------------------------------------------------------------ Merkle --
+def merkle_commit(p2: Poseidon2, base: np.ndarray, num_leaves: int, groups: int, g: int,
+                  gstride: int) -> list[np.ndarray]:
+    """Generalised leaf layout: leaf p = concat_q base[q*gstride + p*g : +g]."""
+    base = u32(base).reshape(-1)
+    layers = np.zeros((2 * num_leaves - 1) * 8, np.uint32)
+    rc = LIB.orc_merkle_commit(p2.ptr, base, num_leaves, groups, g, gstride, layers)
+    if rc:
+        raise ValueError(f"merkle_commit failed ({rc})")
+    out, off, n = [], 0, num_leaves
+    while True:
+        out.append(layers[8 * off: 8 * (off + n)].reshape(n, 8))
+        if n == 1:
+            break
+        off += n
+        n //= 2
+    return out
+
+
+def merkle_commit_rows(p2: Poseidon2, matrix: np.ndarray) -> list[np.ndarray]:
+    """Row-major leaves `(L, w)` (MerkleTree.commit)."""
+    m = u32(matrix)
+    return merkle_commit(p2, m, m.shape[0], 1, m.shape[1], 0)
+
+
+def merkle_commit_columns(p2: Poseidon2, cols: np.ndarray) -> list[np.ndarray]:
+    """Column-major leaves `(w, L)`: leaf r = cols[:, r] (codeword.T rows)."""
+    m = u32(cols)
+    return merkle_commit(p2, m, m.shape[1], m.shape[0], 1, m.shape[1])
+
+
+def merkle_open(base, num_leaves, groups, g, gstride, layers: list[np.ndarray], idx):
+    flat = np.concatenate([l.reshape(-1) for l in layers])
+    idx = np.ascontiguousarray(np.asarray(idx, np.int32))
+    depth = len(layers) - 1
+    rows = np.zeros((idx.size, groups * g), np.uint32)
+    paths = np.zeros((max(depth, 0), idx.size, 8), np.uint32)
+    rc = LIB.orc_merkle_open(u32(base).reshape(-1), num_leaves, groups, g, gstride, flat, idx,
+                             idx.size, rows, paths)
+    if rc:
+        raise IndexError("merkle_open index out of range")
+    return rows, paths
+
+
+# ---------------------------------------------------------------------- RS --
+def rs_encode(field: int, coeffs: np.ndarray, log_blowup: int, shift_mont: int = 0,
+              generator: int = 0) -> np.ndarray:
+    c = u32(coeffs)
+    batch_shape = c.shape[:-1]
+    k = c.shape[-1]
+    log_k = k.bit_length() - 1
+    batch = int(np.prod(batch_shape)) if batch_shape else 1
+    out = np.zeros((batch, k << log_blowup), np.uint32)
+    rc = LIB.orc_rs_encode(field, c.reshape(-1), batch, log_k, log_blowup, shift_mont,
+                           generator, out.reshape(-1))
+    if rc:
+        raise ValueError(f"rs_encode failed ({rc})")
+    return out.reshape(*batch_shape, k << log_blowup)
+
+
+def rs_encode_horner(field, coeffs, log_blowup, shift_mont=0, generator=0) -> np.ndarray:
+    c = u32(coeffs)
+    k = c.size
+    out = np.zeros(k << log_blowup, np.uint32)
+    LIB.orc_rs_encode_horner(field, c, k.bit_length() - 1, log_blowup, shift_mont, generator, out)
+    return out
+
+
+def eval_domain(field: int, log_n: int, shift_mont: int = 0, generator: int = 0) -> np.ndarray:
+    out = np.zeros(1 << log_n, np.uint32)
+    LIB.orc_eval_domain(field, log_n, shift_mont, generator, out)
+    return out
+
+
+def fri_fold(field, cw, ef_in: bool, beta, ef_beta: bool, shift_mont=0, generator=0):
+    cw = u32(cw)
+    n = cw.shape[0]
+    lo = 4 if (ef_in or ef_beta) else 1
+    out = np.zeros((n // 2, lo) if lo == 4 else (n // 2,), np.uint32)
+    b = np.zeros(4, np.uint32)
+    b[: (4 if ef_beta else 1)] = u32(beta).reshape(-1)[: (4 if ef_beta else 1)]
+    rc = LIB.orc_fri_fold(field, cw.reshape(-1), n, int(ef_in), b, int(ef_beta), shift_mont,
+                          generator, out.reshape(-1))
+    if rc:
+        raise ValueError("fri_fold needs a power-of-two length >= 2")
+    return out
+
+
+# -------------------------------------------------------------- transcript --
+class Duplex(C.Structure):
+    _fields_ = [("in_buf", C.c_uint32 * 8), ("out_buf", C.c_uint32 * 8),
+                ("sponge", C.c_uint32 * 16), ("in_pos", C.c_int32), ("out_pos", C.c_int32)]
+
+    def wire(self) -> tuple[np.ndarray, ...]:
+        return (np.array(self.in_buf, np.uint32), np.array(self.out_buf, np.uint32),
+                np.array(self.sponge, np.uint32), np.array([self.in_pos], np.int32).view(np.uint32),
+                np.array([self.out_pos], np.int32).view(np.uint32))
+
+
+class Transcript:
+    def __init__(self, p2: Poseidon2) -> None:
+        self.p2 = p2
+        self.st = Duplex()
+        LIB.orc_duplex_init(C.byref(self.st))
+
+    def observe(self, values) -> "Transcript":
+        v = u32(values).reshape(-1)
+        LIB.orc_duplex_observe(self.p2.ptr, C.byref(self.st), v, v.size)
+        return self
+
+    def sample(self, n: int = 1) -> np.ndarray:
+        out = np.zeros(max(n, 1), np.uint32)
+        LIB.orc_duplex_sample(self.p2.ptr, C.byref(self.st), n, out)
+        return out[:n]
+
+
+# ------------------------------------------------------- FRI commit phase --
+@dataclass
+class CommitPhaseProof:
+    roots: np.ndarray          # (R, 8)
+    betas: np.ndarray          # (R, 4) (limb 0 only for base challenges)
+    final_layer: np.ndarray    # (n_R, limbs)
+    positions: np.ndarray      # (Q,)
+    rows: list[np.ndarray]     # per layer (Q, 2*limbs_i)
+    paths: list[np.ndarray]    # per layer (depth_i, Q, 8)
+
+    def to_bytes(self) -> bytes:
+        parts = [self.roots, self.final_layer]
+        for r, p in zip(self.rows, self.paths):
+            parts += [r, p]
+        return b"".join(np.ascontiguousarray(x, dtype="<u4").tobytes() for x in parts)
+
+
+def layer_limbs(num_rounds: int, beta_limbs: int) -> list[int]:
+    limbs = [1]
+    for _ in range(num_rounds):
+        limbs.append(4 if (limbs[-1] == 4 or beta_limbs == 4) else 1)
+    return limbs
+
+
+def fri_commit_phase(p2: Poseidon2, field: int, codeword, num_rounds: int, num_queries: int,
+                     beta_limbs: int, transcript: Transcript, shift_mont=0, generator=0):
+    cw = u32(codeword).reshape(-1)
+    n0 = cw.size
+    log_n = n0.bit_length() - 1
+    limbs = layer_limbs(num_rounds, beta_limbs)
+    roots = np.zeros((num_rounds, 8), np.uint32)
+    betas = np.zeros((num_rounds, 4), np.uint32)
+    nf = n0 >> num_rounds
+    final = np.zeros((nf, limbs[-1]), np.uint32)
+    pos = np.zeros(num_queries, np.int32)
+    row_sizes = [num_queries * 2 * limbs[r] for r in range(num_rounds)]
+    depths = [log_n - 1 - r for r in range(num_rounds)]
+    path_sizes = [d * num_queries * 8 for d in depths]
+    rows = np.zeros(max(sum(row_sizes), 1), np.uint32)
+    paths = np.zeros(max(sum(path_sizes), 1), np.uint32)
+    rc = LIB.orc_fri_commit_phase(p2.ptr, field, cw, log_n, shift_mont, generator, num_rounds,
+                                  num_queries, beta_limbs, C.byref(transcript.st), roots.reshape(-1),
+                                  betas.reshape(-1), final.reshape(-1), pos, rows, paths)
+    if rc:
+        raise ValueError(f"fri_commit_phase failed ({rc})")
+    rl, pl, ro, po = [], [], 0, 0
+    for r in range(num_rounds):
+        rl.append(rows[ro: ro + row_sizes[r]].reshape(num_queries, 2 * limbs[r]))
+        pl.append(paths[po: po + path_sizes[r]].reshape(depths[r], num_queries, 8))
+        ro += row_sizes[r]
+        po += path_sizes[r]
+    return CommitPhaseProof(roots, betas, final, pos, rl, pl)
