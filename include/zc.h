@@ -1,0 +1,174 @@
+/*
+ * zorch-gb300 C ABI: the drop-in boundary under zorch's commit path.
+ *
+ * Every entry point takes plain device pointers, sizes and a CUDA stream
+ * (passed as void*), launches asynchronously on that stream and returns a
+ * status. Field values are Montgomery u32 (x * 2^32 mod p) -- the storage of
+ * zk_dtypes' *_mont dtypes and the wire form of the reference's Fiat-Shamir FFI
+ * contract (zorch/transcript.py:986-999, 1015-1021). Buffers are owned by the
+ * caller; kernels write outputs only and never alias inputs. No entry point
+ * allocates device memory except zc_poseidon2_create (its parameter block) and
+ * zc_init (once per device); scratch is a caller-provided workspace.
+ *
+ * Each declaration names the reference interface it replaces (paths within
+ * fractalyze/zorch).
+ */
+#ifndef ZORCH_GB300_ZC_H_
+#define ZORCH_GB300_ZC_H_
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum {
+  ZC_OK = 0,
+  ZC_BAD_SHAPE = 1,   /* ValueError in the reference (zorch/coding/reed_solomon.py:178-182) */
+  ZC_NOT_POW2 = 2,    /* ValueError (zorch/coding/reed_solomon.py:92-99, zorch/commit/merkle.py:148-149) */
+  ZC_OOB_INDEX = 3,   /* IndexError (zorch/commit/merkle.py:220-221) */
+  ZC_OOM = 4,         /* workspace too small / allocation failed */
+  ZC_TIMEOUT = 5,     /* a bounded device wait gave up */
+  ZC_CUDA_ERR = 6,    /* CUDA runtime error; zc_last_error() has the text */
+  ZC_BAD_ARG = 7,     /* null pointer, misaligned buffer, bad enum */
+  ZC_UNSUPPORTED = 8  /* NotImplementedError (e.g. an arity or generator not built) */
+} zc_status;
+
+typedef enum { ZC_FIELD_BABYBEAR = 0, ZC_FIELD_KOALABEAR = 1 } zc_field;
+
+/* Leaf layout of a Merkle commit: leaf p (0 <= p < num_leaves) is the
+ * concatenation over q < groups of base[q*group_stride + p*group_len ...
+ * + group_len). Row-major [L, w] leaves: groups=1, group_len=w. Column-major
+ * [w, L] (zorch/commit/merkle.py:72-80 column_major=True, and the codeword.T
+ * rows of zorch/pcs/basefold/prover.py:445-447): groups=w, group_len=1,
+ * group_stride=L. FRI pair leaves of an n-element codeword with `limbs` words
+ * per element (zorch/coding/reed_solomon.py:303-307 + zorch/pcs/fold.py:42-52):
+ * groups=2, group_len=limbs, group_stride=(n/2)*limbs. */
+typedef struct {
+  const uint32_t* base;
+  int64_t num_leaves;
+  int32_t groups;
+  int32_t group_len;
+  int64_t group_stride;
+} zc_leaves;
+
+/* Opaque width-16 Poseidon2 parameterisation living in device memory
+ * (hash-frx Poseidon2Params, used at zorch/testkit/koalabear16.py:239-263). */
+typedef struct zc_poseidon2 zc_poseidon2;
+
+/* Duplex transcript state, the five FFI operands in order
+ * (zorch/transcript.py:1015-1021, 1041-1053): in_buf(8), out_buf(8),
+ * sponge(16), in_pos(1), out_pos(1) -- 34 u32 words. */
+#define ZC_DUPLEX_WORDS 34
+
+const char* zc_status_str(zc_status s);
+const char* zc_last_error(void);
+int zc_version(void);
+
+/* Build per-device constant tables. Called implicitly on first use; call it
+ * explicitly before any CUDA-graph capture. */
+zc_status zc_init(int device);
+
+/* Canonical <-> Montgomery conversion of n field words (inputs in canonical
+ * form are reduced mod p first). zk_dtypes performs this at array
+ * construction (fnp.array(..., dtype=koalabear_mont),
+ * zorch/commit/testing/merkle_test.py:51-63); in-place (in == out) is allowed. */
+zc_status zc_to_mont(zc_field field, const uint32_t* in, uint32_t* out, int64_t n, void* stream);
+zc_status zc_from_mont(zc_field field, const uint32_t* in, uint32_t* out, int64_t n,
+                       void* stream);
+
+/* ---- Poseidon2 parameters -------------------------------------------- */
+/* The built-in BabyBear width-16 instance (x^7, 4+4 full, 13 partial rounds).
+ * The reference ships no BabyBear instance; see gen_poseidon2_babybear16.py. */
+zc_status zc_poseidon2_builtin(zc_field field, const zc_poseidon2** out);
+/* Any width-16 instance from canonical host arrays: ext_init/ext_term are
+ * rounds_f_half x 16, int_rc is rounds_p, diag is 16; j_scale is the
+ * internal_j_scale (1 = identity). Replaces Poseidon2(Poseidon2Params(...)). */
+zc_status zc_poseidon2_create(zc_field field, int alpha, int rounds_f_half, int rounds_p,
+                              const uint32_t* ext_init, const uint32_t* ext_term,
+                              const uint32_t* int_rc, const uint32_t* diag,
+                              uint32_t j_scale, zc_poseidon2** out);
+zc_status zc_poseidon2_destroy(zc_poseidon2* p);
+/* Permute `count` independent 16-word states in place (hash-frx Permutation.permute). */
+zc_status zc_poseidon2_permute(const zc_poseidon2* p, uint32_t* states, int64_t count,
+                               void* stream);
+
+/* ---- Reed-Solomon coset LDE ------------------------------------------ */
+/* Replaces ReedSolomon.encode (zorch/coding/reed_solomon.py:177-188):
+ * out[b, j] = sum_i coeffs[b, i] * (shift * w^j)^i for j < 2^(log_k+log_blowup),
+ * natural order in and out, w = generator^((p-1)/n). shift_mont = 0 means no
+ * coset (coset_shift=None). generator 0 = the field's canonical generator
+ * (31 for BabyBear, 3 for KoalaBear); other generators are ZC_UNSUPPORTED.
+ * coeffs: [batch, 2^log_k]; out: [batch, 2^(log_k+log_blowup)]. */
+size_t zc_rs_encode_workspace_bytes(int64_t batch, int log_k, int log_blowup);
+zc_status zc_rs_encode(zc_field field, const uint32_t* coeffs, int64_t batch, int log_k,
+                       int log_blowup, uint32_t shift_mont, uint32_t generator,
+                       uint32_t* out, void* workspace, size_t workspace_bytes,
+                       void* stream);
+
+/* ---- Merkle trees (arity 2) ------------------------------------------- */
+/* Replaces MerkleTree.commit = hash_leaves + fold_digests
+ * (zorch/commit/merkle.py:118-202) over PaddingFreeSponge<16,8,8> leaves and
+ * TruncatedPermutation<2,8,16> nodes. layers: (2L-1)*8 words, level l (leaf
+ * digests l=0 ... root l=log2 L) at node offset 2L - (2L >> l). L must be a
+ * power of two. */
+zc_status zc_merkle_commit(const zc_poseidon2* p, zc_leaves leaves, uint32_t* layers,
+                           void* stream);
+/* Replaces open_rows / MerkleTree.open (zorch/pcs/fold.py:142-149,
+ * zorch/commit/merkle.py:204-235): rows [q, w], paths [depth][q][8] leaf first.
+ * Out-of-range indices are clamped on the device and reported as ZC_OOB_INDEX
+ * through *oob_flag (device word, may be NULL) -- the host checks before use. */
+zc_status zc_merkle_open(zc_leaves leaves, const uint32_t* layers, const int32_t* idx,
+                         int32_t q, uint32_t* rows, uint32_t* paths, uint32_t* oob_flag,
+                         void* stream);
+
+/* ---- FRI fold ---------------------------------------------------------- */
+/* Replaces ReedSolomon.fold -> fri_fold -> fri_fold_values
+ * (zorch/coding/reed_solomon.py:273-278, 543-548, 589-604) on a natural-order
+ * layer of n elements (ef_in: 4 limbs each, else 1), beta on the device
+ * (ef_beta: 4 limbs, else 1), shift_mont the layer's coset shift
+ * coset_shift^(2^level) (:331-339). out: n/2 elements, 4 limbs if either
+ * input is EF4. */
+zc_status zc_fri_fold(zc_field field, const uint32_t* cw, int64_t n, int ef_in,
+                      const uint32_t* beta, int ef_beta, uint32_t shift_mont,
+                      uint32_t generator, uint32_t* out, void* stream);
+/* The fold fused with the next round's pair-leaf commit
+ * (PreFoldPairCommitRound, zorch/pcs/fold.py:90-115): writes the folded layer
+ * `out` and the complete digest layers of its pair-leaf tree
+ * (n/4 leaves) into next_layers. n >= 4. */
+zc_status zc_fri_fold_commit(const zc_poseidon2* p, const uint32_t* cw, int64_t n, int ef_in,
+                             const uint32_t* beta, int ef_beta, uint32_t shift_mont,
+                             uint32_t generator, uint32_t* out, uint32_t* next_layers,
+                             void* stream);
+
+/* ---- Fiat-Shamir duplex (rate 8, width 16) ----------------------------- */
+/* One observe-then-sample hop in the reference's host-FS FFI contract
+ * (set_host_fs_ffi_target, zorch/transcript.py:1005-1035, _host_hop_ffi
+ * :1056-1112): reads the five state operands and m values, writes the five
+ * advanced operands and n challenge words. Inputs may alias outputs. The
+ * device form runs on one GPU thread; the host form on the calling CPU thread
+ * (all pointers host memory, stream ignored). */
+zc_status zc_duplex_hop(const zc_poseidon2* p, const uint32_t* in_buf, const uint32_t* out_buf,
+                        const uint32_t* sponge, const uint32_t* in_pos,
+                        const uint32_t* out_pos, const uint32_t* values, int64_t m,
+                        int32_t n, uint32_t* in_buf_o, uint32_t* out_buf_o,
+                        uint32_t* sponge_o, uint32_t* in_pos_o, uint32_t* out_pos_o,
+                        uint32_t* challenges, void* stream);
+zc_status zc_duplex_hop_host(const zc_poseidon2* p, const uint32_t* in_buf,
+                             const uint32_t* out_buf, const uint32_t* sponge,
+                             const uint32_t* in_pos, const uint32_t* out_pos,
+                             const uint32_t* values, int64_t m, int32_t n,
+                             uint32_t* in_buf_o, uint32_t* out_buf_o, uint32_t* sponge_o,
+                             uint32_t* in_pos_o, uint32_t* out_pos_o, uint32_t* challenges);
+/* Device-resident transcript step on a packed 34-word state: observe m values
+ * then squeeze n words into `out`; if positions != NULL also write
+ * positions[i] = out[i] mod block_len (sample_positions, zorch/pcs/fold.py:173-182). */
+zc_status zc_duplex_step(const zc_poseidon2* p, uint32_t* state, const uint32_t* values,
+                         int64_t m, int32_t n, uint32_t* out, int32_t* positions,
+                         int64_t block_len, void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* ZORCH_GB300_ZC_H_ */

@@ -1,0 +1,75 @@
+"""Build the CUDA library libzc.so in-tree for sm_103a (GB300).
+
+Three translation units compiled in parallel with nvcc, then linked into
+zorch_gb300/_build/libzc.so. No cmake, no torch extension machinery: the
+library exposes a plain C ABI (include/zc.h) that Python reaches via ctypes.
+"""
+
+from __future__ import annotations
+
+import os
+import subprocess
+import sys
+from concurrent.futures import ThreadPoolExecutor
+from pathlib import Path
+
+PKG = Path(__file__).resolve().parent
+ROOT = PKG.parent
+CSRC = PKG / "csrc"
+OUT_DIR = PKG / "_build"
+LIB = OUT_DIR / "libzc.so"
+SOURCES = ["zc_core.cu", "zc_ntt.cu", "zc_merkle.cu"]
+ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+
+
+def _nvcc() -> str:
+    cuda = os.environ.get("CUDA_HOME", "/usr/local/cuda")
+    cand = Path(cuda) / "bin" / "nvcc"
+    return str(cand) if cand.exists() else "nvcc"
+
+
+def toolchain_available() -> bool:
+    import shutil
+
+    return Path(_nvcc()).exists() or shutil.which("nvcc") is not None
+
+
+def _deps() -> list[Path]:
+    return [CSRC / s for s in SOURCES] + list(CSRC.glob("*.cuh")) + list(CSRC.glob("*.h")) + [
+        ROOT / "include" / "zc.h", Path(__file__)]
+
+
+def build(force: bool = False, verbose: bool = False, extra: list[str] | None = None) -> Path:
+    if LIB.exists() and not force and not extra:
+        newest = max(d.stat().st_mtime for d in _deps())
+        if LIB.stat().st_mtime >= newest:
+            return LIB
+    OUT_DIR.mkdir(parents=True, exist_ok=True)
+    flags = ["-O3", "-lineinfo", "-std=c++17", "--expt-relaxed-constexpr", "-Xcompiler", "-fPIC",
+             "-I", str(ROOT / "include"), *ARCH, *(extra or [])]
+    if verbose:
+        flags += ["-Xptxas", "-v"]
+
+    def compile_one(src: str) -> Path:
+        obj = OUT_DIR / (Path(src).stem + ".o")
+        cmd = [_nvcc(), *flags, "-c", str(CSRC / src), "-o", str(obj)]
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError(f"nvcc failed for {src}:\n{r.stderr}")
+        if verbose and r.stderr:
+            sys.stderr.write(r.stderr)
+        return obj
+
+    with ThreadPoolExecutor(max_workers=len(SOURCES)) as ex:
+        objs = list(ex.map(compile_one, SOURCES))
+    tmp = LIB.with_suffix(f".{os.getpid()}.tmp")
+    cmd = [_nvcc(), *ARCH, "-shared", "-o", str(tmp), *map(str, objs), "-lcudart"]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError(f"link failed:\n{r.stderr}")
+    os.replace(tmp, LIB)
+    return LIB
+
+
+if __name__ == "__main__":
+    print(build(force=True, verbose="-v" in sys.argv))

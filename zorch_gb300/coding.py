@@ -1,0 +1,157 @@
+"""Reed-Solomon code over BabyBear / KoalaBear on the GPU (drop-in for
+zorch/coding/reed_solomon.py:71-426).
+
+`encode` is the coset low-degree extension (zc_rs_encode), `fold` the natural
+order conjugate-pair FRI fold (zc_fri_fold). Tensors are torch.int32 CUDA
+tensors of Montgomery words; the coset shift and generator are canonical ints
+(e.g. coset_shift=31, generator=31 for BabyBear).
+"""
+
+from __future__ import annotations
+
+import torch
+
+from . import _lib
+from .field import BABYBEAR, Field, field_of, ptr, stream_handle
+
+
+def _is_pow2(x: int) -> bool:
+    return x > 0 and (x & (x - 1)) == 0
+
+
+def _log2(x: int) -> int:
+    return x.bit_length() - 1
+
+
+def rs_encode(field: Field, message: torch.Tensor, log_blowup: int, shift_mont: int = 0,
+              generator: int = 0, out: torch.Tensor | None = None) -> torch.Tensor:
+    """zc_rs_encode over the last axis of `message` (any leading batch shape)."""
+    k = message.shape[-1]
+    if not _is_pow2(k):
+        raise ValueError(f"message_len must be a power of two, got {k}")
+    batch = message.numel() // k
+    n = k << log_blowup
+    if out is None:
+        out = torch.empty(*message.shape[:-1], n, dtype=torch.int32, device=message.device)
+    L = _lib.lib()
+    ws_bytes = L.zc_rs_encode_workspace_bytes(batch, _log2(k), log_blowup)
+    ws = torch.empty(max(ws_bytes // 4, 1), dtype=torch.int32, device=message.device)
+    _lib.check(L.zc_rs_encode(field.id, ptr(message.contiguous()), batch, _log2(k), log_blowup,
+                              shift_mont, generator, ptr(out), ptr(ws), ws_bytes,
+                              stream_handle()), "rs_encode")
+    return out
+
+
+def eval_domain(field, n: int, *, shift: int | None = None, generator: int | None = None,
+                device="cuda") -> torch.Tensor:
+    """[shift * w^j] in NTT order (zorch/coding/reed_solomon.py:49-68), read off
+    the encoder applied to e_1 exactly as the reference does."""
+    f = field_of(field)
+    if not _is_pow2(n):
+        raise ValueError(f"eval_domain size must be a power of two, got {n}")
+    sh = f.mont(shift) if shift is not None else 0
+    if n == 1:
+        return torch.full((1,), sh or f.one_mont, dtype=torch.int32, device=device)
+    e1 = torch.zeros(n, dtype=torch.int32, device=device)
+    e1[1] = f.one_mont
+    return rs_encode(f, e1, 0, sh, generator or 0)
+
+
+class ReedSolomon:
+    """Reed-Solomon code; implements the reference's FoldableCode seam
+    (zorch/coding/foldable_code.py:27-70) for the binary natural-order fold."""
+
+    def __init__(self, message_len: int, blowup: int, field=BABYBEAR, *,
+                 coset_shift: int | None = None, fold_factor: int = 2,
+                 generator: int | None = None) -> None:
+        if not _is_pow2(message_len):
+            raise ValueError(f"message_len must be a power of two, got {message_len}")
+        if not _is_pow2(blowup):
+            raise ValueError(f"blowup must be a power of two, got {blowup}")
+        if not _is_pow2(fold_factor) or fold_factor < 2:
+            raise ValueError(f"fold_factor must be a power of two >= 2, got {fold_factor}")
+        if fold_factor != 2:
+            raise NotImplementedError("only the binary (arity-2) fold is built")
+        self.field = field_of(field)
+        if generator not in (None, 0, self.field.generator):
+            raise NotImplementedError("only the field's canonical generator is built")
+        self.message_len = message_len
+        self.blowup = blowup
+        self.block_len = message_len * blowup
+        self.coset_shift = coset_shift
+        self.generator = generator
+        self.fold_factor = fold_factor
+        self._shift_mont = self.field.mont(coset_shift) if coset_shift is not None else 0
+
+    def _key(self):
+        return (self.message_len, self.block_len, self.field.id, self.coset_shift,
+                self.fold_factor, self.generator)
+
+    def __eq__(self, other) -> bool:
+        return isinstance(other, ReedSolomon) and self._key() == other._key()
+
+    def __hash__(self) -> int:
+        return hash(self._key())
+
+    @property
+    def log_blowup(self) -> int:
+        return _log2(self.blowup)
+
+    def encode(self, message: torch.Tensor, out: torch.Tensor | None = None) -> torch.Tensor:
+        if message.shape[-1] != self.message_len:
+            raise ValueError(f"message last axis must be {self.message_len}, "
+                             f"got {message.shape[-1]}")
+        return rs_encode(self.field, message, self.log_blowup, self._shift_mont,
+                         self.generator or 0, out)
+
+    def domain(self) -> torch.Tensor:
+        return eval_domain(self.field, self.block_len, shift=self.coset_shift,
+                           generator=self.generator)
+
+    def level_shift_mont(self, level: int) -> int:
+        """coset_shift^(2^level) in Montgomery form (zorch/coding/reed_solomon.py:331-339)."""
+        if self.coset_shift is None:
+            return 0
+        return self.field.mont(pow(self.coset_shift, 1 << level, self.field.p))
+
+    def level_of(self, n: int) -> int:
+        return _log2(self.block_len // n)
+
+    def fold(self, codeword: torch.Tensor, beta: torch.Tensor,
+             out: torch.Tensor | None = None) -> torch.Tensor:
+        """Natural-order (x, -x) fold; base layers are [n], EF4 layers [n, 4];
+        beta is a device tensor of 1 (base) or 4 (EF4) words."""
+        n = codeword.shape[0]
+        if n < 2:
+            raise ValueError(f"fri_fold requires a codeword of length >= 2, got {n}")
+        ef_in = codeword.dim() == 2
+        ef_beta = beta.numel() == 4
+        lo = 4 if (ef_in or ef_beta) else 1
+        if out is None:
+            shape = (n // 2, 4) if lo == 4 else (n // 2,)
+            out = torch.empty(shape, dtype=torch.int32, device=codeword.device)
+        level = self.level_of(n)
+        _lib.check(_lib.lib().zc_fri_fold(self.field.id, ptr(codeword), n, int(ef_in),
+                                          ptr(beta.contiguous()), int(ef_beta),
+                                          self.level_shift_mont(level), self.generator or 0,
+                                          ptr(out), stream_handle()), "fri_fold")
+        return out
+
+    def pair_leaves(self, codeword: torch.Tensor) -> torch.Tensor:
+        """Leaf p = (cw[p], cw[p + n/2]) in base limbs (materialised copy)."""
+        half = codeword.shape[0] // 2
+        return torch.stack([codeword[:half], codeword[half:]], dim=1).reshape(half, -1)
+
+    def pair_indices(self, positions: torch.Tensor, level: int):
+        return positions, positions + (self.block_len >> (level + 1))
+
+    def layer_positions(self, positions: torch.Tensor, num_rounds: int) -> list[torch.Tensor]:
+        """a_i = q_i mod (n / 2^{i+1}) (zorch/coding/reed_solomon.py:320-329)."""
+        out, q = [], positions
+        for i in range(num_rounds):
+            q = torch.remainder(q, self.block_len >> (i + 1))
+            out.append(q)
+        return out
+
+    def check_final(self, final: torch.Tensor, claim: torch.Tensor) -> bool:
+        return bool((final == claim).all())

@@ -1,0 +1,202 @@
+"""Poseidon2 sponge/compression Merkle trees on the GPU (drop-in for
+zorch/commit/merkle.py:46-331, arity 2).
+
+`Poseidon2` wraps a width-16 parameterisation (hash-frx Poseidon2Params): the
+built-in BabyBear-16 instance or any instance given by canonical constants.
+`MerkleTree.commit` hashes every leaf with PaddingFreeSponge<16,8,8> and folds
+pairs with TruncatedPermutation<2,8,16>, keeping every digest layer in one flat
+device buffer (leaf digests first, root last).
+"""
+
+from __future__ import annotations
+
+import ctypes as C
+from dataclasses import dataclass
+
+import numpy as np
+import torch
+
+from . import _lib
+from .field import BABYBEAR, KOALABEAR, field_of, ptr, stream_handle
+
+
+class Poseidon2:
+    """A width-16 Poseidon2 permutation living on the device."""
+
+    def __init__(self, handle: int, field, owned: bool) -> None:
+        self._h = handle
+        self.field = field_of(field)
+        self._owned = owned
+
+    @classmethod
+    def builtin(cls, field=BABYBEAR) -> "Poseidon2":
+        h = C.c_void_p()
+        _lib.check(_lib.lib().zc_poseidon2_builtin(field_of(field).id, C.byref(h)),
+                   "poseidon2_builtin")
+        return cls(h.value, field, False)
+
+    @classmethod
+    def from_params(cls, field, alpha: int, ext_init, ext_term, int_rc, diag,
+                    j_scale: int = 1) -> "Poseidon2":
+        """Canonical constants: ext_init/ext_term (R_F/2, 16), int_rc (R_P,), diag (16,)."""
+        f = field_of(field)
+        ei = np.ascontiguousarray(np.asarray(ext_init, np.uint32).reshape(-1))
+        et = np.ascontiguousarray(np.asarray(ext_term, np.uint32).reshape(-1))
+        ir = np.ascontiguousarray(np.asarray(int_rc, np.uint32))
+        dg = np.ascontiguousarray(np.asarray(diag, np.uint32))
+        if ei.size % 16 or ei.size != et.size or dg.size != 16:
+            raise ValueError("Poseidon2 width-16 constants have the wrong shape")
+        h = C.c_void_p()
+        _lib.check(_lib.lib().zc_poseidon2_create(
+            f.id, alpha, ei.size // 16, ir.size, ei.ctypes.data, et.ctypes.data,
+            ir.ctypes.data if ir.size else None, dg.ctypes.data, j_scale, C.byref(h)),
+            "poseidon2_create")
+        return cls(h.value, f, True)
+
+    @property
+    def handle(self) -> int:
+        return self._h
+
+    def permute(self, states: torch.Tensor) -> torch.Tensor:
+        """Permute [count, 16] states (a copy is returned)."""
+        s = states.contiguous().clone()
+        _lib.check(_lib.lib().zc_poseidon2_permute(self._h, ptr(s), s.numel() // 16,
+                                                   stream_handle()), "poseidon2_permute")
+        return s
+
+    def __del__(self) -> None:
+        if getattr(self, "_owned", False) and self._h:
+            try:
+                _lib.lib().zc_poseidon2_destroy(self._h)
+            except Exception:
+                pass
+            self._h = 0
+
+
+def level_offset(num_leaves: int, level: int) -> int:
+    return 2 * num_leaves - ((2 * num_leaves) >> level)
+
+
+class DigestLayers:
+    """All digest layers of one tree in a flat [(2L-1), 8] device buffer."""
+
+    def __init__(self, flat: torch.Tensor, num_leaves: int) -> None:
+        self.flat = flat
+        self.num_leaves = num_leaves
+
+    @property
+    def depth(self) -> int:
+        return self.num_leaves.bit_length() - 1
+
+    def __len__(self) -> int:
+        return self.depth + 1
+
+    def __getitem__(self, level: int) -> torch.Tensor:
+        if level < 0:
+            level += len(self)
+        off = level_offset(self.num_leaves, level)
+        return self.flat[off: off + (self.num_leaves >> level)]
+
+    def __iter__(self):
+        return (self[i] for i in range(len(self)))
+
+    @property
+    def root(self) -> torch.Tensor:
+        return self.flat[-1]
+
+
+@dataclass(frozen=True)
+class Opening:
+    """Batched openings: rows [Q, w] and path [depth, Q, 8] (leaf first)."""
+
+    row: torch.Tensor
+    path: torch.Tensor
+
+
+def leaves_layout(base: torch.Tensor, num_leaves: int, groups: int, group_len: int,
+                  group_stride: int) -> _lib.Leaves:
+    return _lib.Leaves(ptr(base), num_leaves, groups, group_len, group_stride)
+
+
+class MerkleTree:
+    """Arity-2 Merkle commitment over a single matrix (zorch/commit/merkle.py:59-331).
+
+    `column_major=False` reads a leaf as a row of `[num_leaves, leaf_width]`;
+    True as a column of `[leaf_width, num_leaves]` (zorch/commit/merkle.py:72-80)."""
+
+    arity = 2
+    digest_elems = 8
+
+    def __init__(self, perm: Poseidon2 | None = None, *, column_major: bool = False) -> None:
+        self.perm = perm if perm is not None else Poseidon2.builtin(BABYBEAR)
+        self.column_major = column_major
+
+    def __eq__(self, other) -> bool:
+        return (isinstance(other, MerkleTree) and self.perm.handle == other.perm.handle
+                and self.column_major == other.column_major)
+
+    def __hash__(self) -> int:
+        return hash((self.perm.handle, self.column_major))
+
+    def _layout(self, matrix: torch.Tensor) -> _lib.Leaves:
+        if matrix.dim() != 2:
+            raise ValueError(f"matrix must be 2-D, got ndim={matrix.dim()}")
+        m = matrix.contiguous()
+        if self.column_major:
+            w, L = m.shape
+            return leaves_layout(m, L, w, 1, L)
+        L, w = m.shape
+        return leaves_layout(m, L, 1, w, 0)
+
+    def commit_layout(self, lv: _lib.Leaves, device="cuda",
+                      out: torch.Tensor | None = None) -> tuple[torch.Tensor, DigestLayers]:
+        L = lv.num_leaves
+        if L == 0:
+            raise ValueError("matrix must contain at least one leaf")
+        if L & (L - 1):
+            raise ValueError(f"leaf count ({L}) must be a power of two")
+        flat = out if out is not None else torch.empty((2 * L - 1, 8), dtype=torch.int32,
+                                                       device=device)
+        _lib.check(_lib.lib().zc_merkle_commit(self.perm.handle, lv, ptr(flat), stream_handle()),
+                   "merkle_commit")
+        layers = DigestLayers(flat, L)
+        return layers.root, layers
+
+    def commit(self, matrix: torch.Tensor) -> tuple[torch.Tensor, DigestLayers]:
+        """(raw_root (8,), digest_layers) (zorch/commit/merkle.py:118-134)."""
+        return self.commit_layout(self._layout(matrix), matrix.device)
+
+    def open_layout(self, lv: _lib.Leaves, layers: DigestLayers, indices: torch.Tensor,
+                    width: int) -> Opening:
+        idx = indices.to(torch.int32).contiguous()
+        q = idx.numel()
+        rows = torch.empty((q, width), dtype=torch.int32, device=idx.device)
+        paths = torch.empty((layers.depth, q, 8), dtype=torch.int32, device=idx.device)
+        flag = torch.zeros(1, dtype=torch.int32, device=idx.device)
+        _lib.check(_lib.lib().zc_merkle_open(lv, ptr(layers.flat), ptr(idx), q, ptr(rows),
+                                             ptr(paths), ptr(flag), stream_handle()),
+                   "merkle_open")
+        if int(flag.item()):
+            raise IndexError(f"leaf index out of range [0, {lv.num_leaves})")
+        return Opening(rows, paths)
+
+    def open_rows(self, matrix: torch.Tensor, layers: DigestLayers,
+                  indices: torch.Tensor) -> Opening:
+        """Open `matrix` (always leaf-major [L, w] like the reference) at every
+        index (zorch/pcs/fold.py:142-149)."""
+        m = matrix.contiguous()
+        lv = leaves_layout(m, m.shape[0], 1, m.shape[1], 0)
+        return self.open_layout(lv, layers, indices, m.shape[1])
+
+    def open(self, matrix: torch.Tensor, layers: DigestLayers, index: int) -> Opening:
+        if not 0 <= int(index) < matrix.shape[0]:
+            raise IndexError(f"leaf index {index} out of range [0, {matrix.shape[0]})")
+        op = self.open_rows(matrix, layers, torch.tensor([int(index)], device=matrix.device))
+        return Opening(op.row[0], op.path[:, 0])
+
+
+def koalabear16_params(fixture: dict) -> Poseidon2:
+    """A Poseidon2 from a KoalaBear-16 parameter dict (canonical constants)."""
+    return Poseidon2.from_params(KOALABEAR, fixture["alpha"], fixture["external_initial"],
+                                 fixture["external_terminal"], fixture["internal_rc"],
+                                 fixture["internal_diag"], fixture.get("internal_j_scale", 1))

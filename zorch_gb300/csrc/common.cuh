@@ -1,0 +1,50 @@
+// Shared host/device helpers: status codes, launch checks, level offsets.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "../../include/zc.h"
+
+namespace zc {
+
+#define ZC_TRY(expr)                       \
+  do {                                     \
+    zc_status _s = (expr);                 \
+    if (_s != ZC_OK) return _s;            \
+  } while (0)
+
+#define ZC_CUDA(expr)                                  \
+  do {                                                 \
+    cudaError_t _e = (expr);                           \
+    if (_e != cudaSuccess) return zc::cuda_fail(_e);   \
+  } while (0)
+
+zc_status cuda_fail(cudaError_t e);
+zc_status launch_check();
+
+inline bool is_pow2(int64_t x) { return x > 0 && (x & (x - 1)) == 0; }
+inline int ilog2(int64_t x) {
+  int l = 0;
+  while (((int64_t)1 << l) < x) l++;
+  return l;
+}
+
+// Digest-layer layout of an arity-2 tree over L leaves: level l (leaf digests
+// = level 0, root = level log2 L) starts at node offset 2L - (2L >> l).
+__host__ __device__ __forceinline__ int64_t level_offset(int64_t L, int l) {
+  return 2 * L - ((2 * L) >> l);
+}
+
+__device__ __forceinline__ void store_digest(uint32_t* dst, const uint32_t* d) {
+  uint4* p = reinterpret_cast<uint4*>(dst);
+  p[0] = make_uint4(d[0], d[1], d[2], d[3]);
+  p[1] = make_uint4(d[4], d[5], d[6], d[7]);
+}
+__device__ __forceinline__ void load_digest(const uint32_t* src, uint32_t* d) {
+  const uint4* p = reinterpret_cast<const uint4*>(src);
+  uint4 a = p[0], b = p[1];
+  d[0] = a.x; d[1] = a.y; d[2] = a.z; d[3] = a.w;
+  d[4] = b.x; d[5] = b.y; d[6] = b.z; d[7] = b.w;
+}
+
+}  // namespace zc

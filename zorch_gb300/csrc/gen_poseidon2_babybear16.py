@@ -173,6 +173,9 @@ def main() -> None:
     internal = [row[0] for row in rc[half : half + R_P]]
     ext_term = rc[half + R_P :]
 
+    def mont(vals):
+        return [(v << 32) % P for v in vals]
+
     def arr(vals):
         return ", ".join(f"{v}u" for v in vals)
 
@@ -194,6 +197,11 @@ def main() -> None:
         "};",
         f"static const uint32_t ZC_BB16_INT_RC[{R_P}] = {{{arr(internal)}}};",
         f"static const uint32_t ZC_BB16_DIAG[16] = {{{arr(diag)}}};",
+        "// Montgomery forms (x * 2^32 mod p), what the kernels load.",
+        "#define ZC_BB16_EXT_INIT_MONT_INIT {" + arr(mont(v for r in ext_init for v in r)) + "}",
+        "#define ZC_BB16_EXT_TERM_MONT_INIT {" + arr(mont(v for r in ext_term for v in r)) + "}",
+        "#define ZC_BB16_INT_RC_MONT_INIT {" + arr(mont(internal)) + "}",
+        "#define ZC_BB16_DIAG_MONT_INIT {" + arr(mont(diag)) + "}",
         "",
     ]
     out = Path(__file__).with_name("poseidon2_babybear16.h")

@@ -1,0 +1,155 @@
+// Width-16 Poseidon2 permutation, sponge and 2-to-1 compression on one thread's
+// registers. Semantics follow hash-frx / Plonky3 as pinned by the reference's
+// KoalaBear-16 golden root (zorch/commit/testing/merkle_test.py:51-63):
+// initial external layer, R_F/2 full rounds, R_P partial rounds, R_F/2 full
+// rounds; external layer = M4 = circ(2,3,1,1) per 4-lane block plus the
+// lane-class sums; internal layer s_i <- j*sum(s) + diag_i * s_i.
+//
+// Two constant providers:
+//  - Bb16Builtin: the built-in BabyBear-16 instance (x^7, 4+4+13), constants in
+//    __constant__ memory, compile-time shape;
+//  - RtParams:    any width-16 instance passed at run time (the reference's
+//    Poseidon2Params), staged into shared memory by the kernel.
+#pragma once
+#include "field.cuh"
+#include "poseidon2_babybear16.h"
+
+namespace zc {
+
+// Run-time Poseidon2 parameters (all Montgomery). Mirrors hash-frx's
+// Poseidon2Params fields as used at zorch/testkit/koalabear16.py:253-263.
+struct P2Params {
+  uint32_t field_id;
+  uint32_t alpha;
+  uint32_t rounds_f_half;
+  uint32_t rounds_p;
+  uint32_t ext_init[8][16];
+  uint32_t ext_term[8][16];
+  uint32_t int_rc[64];
+  uint32_t diag[16];
+  uint32_t j_scale;
+  uint32_t j_is_one;
+};
+
+static __constant__ uint32_t c_bb16_ext_init[64] = ZC_BB16_EXT_INIT_MONT_INIT;
+static __constant__ uint32_t c_bb16_ext_term[64] = ZC_BB16_EXT_TERM_MONT_INIT;
+static __constant__ uint32_t c_bb16_int_rc[ZC_BB16_ROUNDS_P] = ZC_BB16_INT_RC_MONT_INIT;
+static __constant__ uint32_t c_bb16_diag[16] = ZC_BB16_DIAG_MONT_INIT;
+
+struct Bb16Builtin {
+  using F = BabyBear;
+  static constexpr int RF_HALF = ZC_BB16_ROUNDS_F_HALF;
+  __device__ __forceinline__ int rf_half() const { return RF_HALF; }
+  __device__ __forceinline__ int rp() const { return ZC_BB16_ROUNDS_P; }
+  __device__ __forceinline__ uint32_t ei(int r, int i) const { return c_bb16_ext_init[r * 16 + i]; }
+  __device__ __forceinline__ uint32_t et(int r, int i) const { return c_bb16_ext_term[r * 16 + i]; }
+  __device__ __forceinline__ uint32_t ir(int r) const { return c_bb16_int_rc[r]; }
+  __device__ __forceinline__ uint32_t dg(int i) const { return c_bb16_diag[i]; }
+  __device__ __forceinline__ uint32_t sbox(uint32_t x) const {
+    uint32_t x2 = mmul<F>(x, x);
+    uint32_t x3 = mmul<F>(x2, x);
+    uint32_t x4 = mmul<F>(x2, x2);
+    return mmul<F>(x3, x4);
+  }
+  __device__ __forceinline__ uint32_t jsum(uint32_t s) const { return s; }
+};
+
+template <class F_>
+struct RtParams {
+  using F = F_;
+  const P2Params* p;  // shared memory on the device, plain memory on the host
+  ZC_HD int rf_half() const { return (int)p->rounds_f_half; }
+  ZC_HD int rp() const { return (int)p->rounds_p; }
+  ZC_HD uint32_t ei(int r, int i) const { return p->ext_init[r][i]; }
+  ZC_HD uint32_t et(int r, int i) const { return p->ext_term[r][i]; }
+  ZC_HD uint32_t ir(int r) const { return p->int_rc[r]; }
+  ZC_HD uint32_t dg(int i) const { return p->diag[i]; }
+  ZC_HD uint32_t sbox(uint32_t x) const {
+    uint32_t x2 = mmul<F>(x, x);
+    switch (p->alpha) {
+      case 3: return mmul<F>(x2, x);
+      case 5: return mmul<F>(mmul<F>(x2, x2), x);
+      case 7: return mmul<F>(mmul<F>(x2, x), mmul<F>(x2, x2));
+      default: return mpow<F>(x, p->alpha);
+    }
+  }
+  ZC_HD uint32_t jsum(uint32_t s) const { return p->j_is_one ? s : mmul<F>(s, p->j_scale); }
+};
+
+// External (M4 block-circulant) linear layer.
+template <class F>
+ZC_HD void p2_ext_linear(uint32_t* s) {
+#pragma unroll
+  for (int c = 0; c < 16; c += 4) {
+    uint32_t x0 = s[c], x1 = s[c + 1], x2 = s[c + 2], x3 = s[c + 3];
+    uint32_t t01 = madd<F>(x0, x1), t23 = madd<F>(x2, x3);
+    uint32_t t0123 = madd<F>(t01, t23);
+    uint32_t t01123 = madd<F>(t0123, x1), t01233 = madd<F>(t0123, x3);
+    s[c + 3] = madd<F>(t01233, madd<F>(x0, x0));
+    s[c + 1] = madd<F>(t01123, madd<F>(x2, x2));
+    s[c + 0] = madd<F>(t01123, t01);
+    s[c + 2] = madd<F>(t01233, t23);
+  }
+  uint32_t sums[4];
+#pragma unroll
+  for (int k = 0; k < 4; k++)
+    sums[k] = madd<F>(madd<F>(s[k], s[4 + k]), madd<F>(s[8 + k], s[12 + k]));
+#pragma unroll
+  for (int i = 0; i < 16; i++) s[i] = madd<F>(s[i], sums[i & 3]);
+}
+
+#pragma nv_exec_check_disable
+template <class K>
+ZC_HD void p2_permute(uint32_t* s, const K& k) {
+  using F = typename K::F;
+  p2_ext_linear<F>(s);
+#pragma unroll 1
+  for (int r = 0; r < k.rf_half(); r++) {
+#pragma unroll
+    for (int i = 0; i < 16; i++) s[i] = k.sbox(madd<F>(s[i], k.ei(r, i)));
+    p2_ext_linear<F>(s);
+  }
+#pragma unroll 1
+  for (int r = 0; r < k.rp(); r++) {
+    s[0] = k.sbox(madd<F>(s[0], k.ir(r)));
+    uint32_t a0 = madd<F>(madd<F>(s[0], s[1]), madd<F>(s[2], s[3]));
+    uint32_t a1 = madd<F>(madd<F>(s[4], s[5]), madd<F>(s[6], s[7]));
+    uint32_t a2 = madd<F>(madd<F>(s[8], s[9]), madd<F>(s[10], s[11]));
+    uint32_t a3 = madd<F>(madd<F>(s[12], s[13]), madd<F>(s[14], s[15]));
+    uint32_t sum = k.jsum(madd<F>(madd<F>(a0, a1), madd<F>(a2, a3)));
+#pragma unroll
+    for (int i = 0; i < 16; i++) s[i] = madd<F>(sum, mmul<F>(k.dg(i), s[i]));
+  }
+#pragma unroll 1
+  for (int r = 0; r < k.rf_half(); r++) {
+#pragma unroll
+    for (int i = 0; i < 16; i++) s[i] = k.sbox(madd<F>(s[i], k.et(r, i)));
+    p2_ext_linear<F>(s);
+  }
+}
+
+// TruncatedPermutation<2, 8, 16>: permute(l || r)[0:8].
+#pragma nv_exec_check_disable
+template <class K>
+ZC_HD void p2_compress(const uint32_t* l, const uint32_t* r, uint32_t* out,
+                                            const K& k) {
+  uint32_t s[16];
+#pragma unroll
+  for (int i = 0; i < 8; i++) {
+    s[i] = l[i];
+    s[8 + i] = r[i];
+  }
+  p2_permute(s, k);
+#pragma unroll
+  for (int i = 0; i < 8; i++) out[i] = s[i];
+}
+
+// Stage run-time params into shared memory (whole block participates).
+__device__ __forceinline__ void stage_params(P2Params* dst, const P2Params* src) {
+  const uint32_t* s = reinterpret_cast<const uint32_t*>(src);
+  uint32_t* d = reinterpret_cast<uint32_t*>(dst);
+  for (int i = threadIdx.x; i < (int)(sizeof(P2Params) / 4); i += blockDim.x) d[i] = s[i];
+  __syncthreads();
+}
+
+}  // namespace zc

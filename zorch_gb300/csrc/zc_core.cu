@@ -1,0 +1,395 @@
+// Status/error plumbing, per-device init, Poseidon2 handles, the batched
+// permutation and the Fiat-Shamir duplex (device and host forms).
+#include <stdio.h>
+#include <string.h>
+
+#include <mutex>
+
+#include "internal.cuh"
+
+namespace zc {
+
+static thread_local char g_err[512] = "";
+
+void set_error(const char* msg) {
+  strncpy(g_err, msg, sizeof(g_err) - 1);
+  g_err[sizeof(g_err) - 1] = 0;
+}
+
+zc_status cuda_fail(cudaError_t e) {
+  snprintf(g_err, sizeof(g_err), "CUDA error %d: %s", (int)e, cudaGetErrorString(e));
+  return ZC_CUDA_ERR;
+}
+
+zc_status launch_check() {
+  cudaError_t e = cudaGetLastError();
+  return e == cudaSuccess ? ZC_OK : cuda_fail(e);
+}
+
+zc_status init_root_tables();  // zc_ntt.cu
+
+static std::mutex g_init_mu;
+static bool g_init_done[64];
+
+zc_status ensure_init() {
+  int dev = 0;
+  ZC_CUDA(cudaGetDevice(&dev));
+  if (dev < 0 || dev >= 64) return ZC_BAD_ARG;
+  std::lock_guard<std::mutex> lock(g_init_mu);
+  if (g_init_done[dev]) return ZC_OK;
+  ZC_TRY(init_root_tables());
+  ZC_CUDA(cudaDeviceSynchronize());  // tables visible to every stream afterwards
+  g_init_done[dev] = true;
+  return ZC_OK;
+}
+
+// ------------------------------------------------------------ duplex ------
+// The DuplexTranscript state machine (zorch/transcript.py:239-481) on one
+// thread. Packed state: in_buf[8] out_buf[8] sponge[16] in_pos out_pos.
+struct Duplex {
+  uint32_t in_buf[8];
+  uint32_t out_buf[8];
+  uint32_t sponge[16];
+  int32_t in_pos;
+  int32_t out_pos;
+};
+
+// _observe_body (zorch/transcript.py:637-748): the stream in_buf[0:in_pos] ++
+// values is absorbed a full rate block at a time (overwrite sponge[0:8],
+// permute); the tail stays pending; a fresh output iff no tail remains.
+template <class K>
+ZC_HD void duplex_observe(Duplex& t, const uint32_t* v, int64_t m, const K& k) {
+  if (m <= 0) return;
+  int pos = t.in_pos & 7;  // a corrupt caller state cannot index past the buffer
+  for (int64_t i = 0; i < m; i++) {
+    t.in_buf[pos++] = v[i];
+    if (pos == 8) {
+      for (int j = 0; j < 8; j++) t.sponge[j] = t.in_buf[j];
+      p2_permute(t.sponge, k);
+      pos = 0;
+    }
+  }
+  for (int j = pos; j < 8; j++) t.in_buf[j] = 0;
+  t.in_pos = pos;
+  if (pos == 0) {
+    for (int j = 0; j < 8; j++) t.out_buf[j] = t.sponge[j];
+    t.out_pos = 8;
+  } else {
+    for (int j = 0; j < 8; j++) t.out_buf[j] = 0;
+    t.out_pos = 0;
+  }
+}
+
+// _sample_one (zorch/transcript.py:370-387) n times; _duplexing (:299-313)
+// merges the pending prefix over sponge[0:in_pos] (:154-163) and permutes.
+template <class K>
+ZC_HD void duplex_sample(Duplex& t, int n, uint32_t* out, const K& k) {
+  t.in_pos &= 7;
+  if (t.out_pos < 0 || t.out_pos > 8) t.out_pos = 0;
+  for (int i = 0; i < n; i++) {
+    if (t.in_pos > 0 || t.out_pos == 0) {
+      for (int j = 0; j < t.in_pos; j++) t.sponge[j] = t.in_buf[j];
+      p2_permute(t.sponge, k);
+      for (int j = 0; j < 8; j++) {
+        t.in_buf[j] = 0;
+        t.out_buf[j] = t.sponge[j];
+      }
+      t.in_pos = 0;
+      t.out_pos = 8;
+    }
+    t.out_pos -= 1;
+    out[i] = t.out_buf[t.out_pos];
+  }
+}
+
+template <class K>
+__global__ void k_duplex_step(const P2Params* rt, uint32_t* state, const uint32_t* values,
+                              int64_t m, int n, uint32_t* out, int32_t* positions,
+                              int64_t block_len) {
+  __shared__ P2Params s_rt;
+  K k = KIn<K>::make(rt, &s_rt);
+  if (threadIdx.x != 0) return;
+  Duplex t;
+  memcpy(&t, state, sizeof(Duplex));
+  duplex_observe(t, values, m, k);
+  for (int i = 0; i < n; i++) {
+    uint32_t w;
+    duplex_sample(t, 1, &w, k);
+    if (out) out[i] = w;
+    if (positions) positions[i] = (int32_t)(w % (uint32_t)block_len);
+  }
+  memcpy(state, &t, sizeof(Duplex));
+}
+
+template <class K>
+__global__ void k_duplex_hop(const P2Params* rt, const uint32_t* in_buf, const uint32_t* out_buf,
+                             const uint32_t* sponge, const uint32_t* in_pos,
+                             const uint32_t* out_pos, const uint32_t* values, int64_t m, int n,
+                             uint32_t* in_buf_o, uint32_t* out_buf_o, uint32_t* sponge_o,
+                             uint32_t* in_pos_o, uint32_t* out_pos_o, uint32_t* chal) {
+  __shared__ P2Params s_rt;
+  K k = KIn<K>::make(rt, &s_rt);
+  if (threadIdx.x != 0) return;
+  Duplex t;
+  for (int j = 0; j < 8; j++) {
+    t.in_buf[j] = in_buf[j];
+    t.out_buf[j] = out_buf[j];
+  }
+  for (int j = 0; j < 16; j++) t.sponge[j] = sponge[j];
+  t.in_pos = (int32_t)in_pos[0];
+  t.out_pos = (int32_t)out_pos[0];
+  duplex_observe(t, values, m, k);
+  for (int i = 0; i < n; i++) duplex_sample(t, 1, chal + i, k);
+  for (int j = 0; j < 8; j++) {
+    in_buf_o[j] = t.in_buf[j];
+    out_buf_o[j] = t.out_buf[j];
+  }
+  for (int j = 0; j < 16; j++) sponge_o[j] = t.sponge[j];
+  in_pos_o[0] = (uint32_t)t.in_pos;
+  out_pos_o[0] = (uint32_t)t.out_pos;
+}
+
+template <class F>
+__global__ void k_convert(const uint32_t* in, uint32_t* out, int64_t n, int to) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x)
+    out[i] = to ? to_mont<F>(in[i]) : from_mont<F>(in[i]);
+}
+
+template <class K>
+__global__ void k_permute(const P2Params* rt, uint32_t* states, int64_t count) {
+  __shared__ P2Params s_rt;
+  K k = KIn<K>::make(rt, &s_rt);
+  int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= count) return;
+  uint32_t s[16];
+  for (int j = 0; j < 16; j++) s[j] = states[i * 16 + j];
+  p2_permute(s, k);
+  for (int j = 0; j < 16; j++) states[i * 16 + j] = s[j];
+}
+
+}  // namespace zc
+
+using namespace zc;
+
+extern "C" {
+
+const char* zc_status_str(zc_status s) {
+  switch (s) {
+    case ZC_OK: return "ok";
+    case ZC_BAD_SHAPE: return "bad shape";
+    case ZC_NOT_POW2: return "size is not a power of two";
+    case ZC_OOB_INDEX: return "index out of range";
+    case ZC_OOM: return "workspace too small or out of memory";
+    case ZC_TIMEOUT: return "device wait timed out";
+    case ZC_CUDA_ERR: return "CUDA error";
+    case ZC_BAD_ARG: return "bad argument";
+    case ZC_UNSUPPORTED: return "unsupported configuration";
+  }
+  return "unknown status";
+}
+
+const char* zc_last_error(void) { return g_err; }
+int zc_version(void) { return 1; }
+
+zc_status zc_init(int device) {
+  if (device >= 0) ZC_CUDA(cudaSetDevice(device));
+  ZC_TRY(ensure_init());
+  ZC_CUDA(cudaDeviceSynchronize());
+  return ZC_OK;
+}
+
+static zc_status upload_params(zc_poseidon2* h) {
+  ZC_CUDA(cudaMalloc((void**)&h->dev, sizeof(P2Params)));
+  ZC_CUDA(cudaMemcpy(h->dev, &h->host, sizeof(P2Params), cudaMemcpyHostToDevice));
+  return ZC_OK;
+}
+
+zc_status zc_poseidon2_builtin(zc_field field, const zc_poseidon2** out) {
+  if (!out) return ZC_BAD_ARG;
+  if (field != ZC_FIELD_BABYBEAR) {
+    set_error("no built-in Poseidon2 instance for this field; create one with zc_poseidon2_create");
+    return ZC_UNSUPPORTED;
+  }
+  static std::mutex mu;
+  static zc_poseidon2* inst[64] = {};
+  int dev = 0;
+  ZC_CUDA(cudaGetDevice(&dev));
+  std::lock_guard<std::mutex> lock(mu);
+  if (!inst[dev]) {
+    zc_poseidon2* h = new zc_poseidon2();
+    memset(&h->host, 0, sizeof(h->host));
+    h->field = ZC_FIELD_BABYBEAR;
+    h->builtin = 1;
+    const uint32_t ei[64] = ZC_BB16_EXT_INIT_MONT_INIT, et[64] = ZC_BB16_EXT_TERM_MONT_INIT;
+    const uint32_t ir[ZC_BB16_ROUNDS_P] = ZC_BB16_INT_RC_MONT_INIT, dg[16] = ZC_BB16_DIAG_MONT_INIT;
+    h->host.field_id = 0;
+    h->host.alpha = ZC_BB16_ALPHA;
+    h->host.rounds_f_half = ZC_BB16_ROUNDS_F_HALF;
+    h->host.rounds_p = ZC_BB16_ROUNDS_P;
+    memcpy(h->host.ext_init, ei, sizeof(ei));
+    memcpy(h->host.ext_term, et, sizeof(et));
+    memcpy(h->host.int_rc, ir, sizeof(ir));
+    memcpy(h->host.diag, dg, sizeof(dg));
+    h->host.j_scale = BabyBear::ONE;
+    h->host.j_is_one = 1;
+    zc_status s = upload_params(h);
+    if (s != ZC_OK) {
+      delete h;
+      return s;
+    }
+    inst[dev] = h;
+  }
+  *out = inst[dev];
+  return ZC_OK;
+}
+
+zc_status zc_poseidon2_create(zc_field field, int alpha, int rounds_f_half, int rounds_p,
+                              const uint32_t* ext_init, const uint32_t* ext_term,
+                              const uint32_t* int_rc, const uint32_t* diag, uint32_t j_scale,
+                              zc_poseidon2** out) {
+  if (!out || !ext_init || !ext_term || !int_rc || !diag) return ZC_BAD_ARG;
+  if (field != ZC_FIELD_BABYBEAR && field != ZC_FIELD_KOALABEAR) return ZC_BAD_ARG;
+  if (rounds_f_half < 0 || rounds_f_half > 8 || rounds_p < 0 || rounds_p > 64 || alpha < 2) {
+    set_error("Poseidon2 shape out of range (rounds_f_half <= 8, rounds_p <= 64)");
+    return ZC_UNSUPPORTED;
+  }
+  zc_poseidon2* h = new zc_poseidon2();
+  memset(&h->host, 0, sizeof(h->host));
+  h->field = field;
+  h->builtin = 0;
+  auto conv = [&](uint32_t x) {
+    return field == ZC_FIELD_BABYBEAR ? to_mont<BabyBear>(x) : to_mont<KoalaBear>(x);
+  };
+  h->host.field_id = (uint32_t)field;
+  h->host.alpha = (uint32_t)alpha;
+  h->host.rounds_f_half = (uint32_t)rounds_f_half;
+  h->host.rounds_p = (uint32_t)rounds_p;
+  for (int r = 0; r < rounds_f_half; r++)
+    for (int i = 0; i < 16; i++) {
+      h->host.ext_init[r][i] = conv(ext_init[r * 16 + i]);
+      h->host.ext_term[r][i] = conv(ext_term[r * 16 + i]);
+    }
+  for (int r = 0; r < rounds_p; r++) h->host.int_rc[r] = conv(int_rc[r]);
+  for (int i = 0; i < 16; i++) h->host.diag[i] = conv(diag[i]);
+  h->host.j_scale = conv(j_scale);
+  h->host.j_is_one = (j_scale == 1);
+  zc_status s = upload_params(h);
+  if (s != ZC_OK) {
+    delete h;
+    return s;
+  }
+  *out = h;
+  return ZC_OK;
+}
+
+zc_status zc_poseidon2_destroy(zc_poseidon2* p) {
+  if (!p || p->builtin) return ZC_BAD_ARG;
+  if (p->dev) cudaFree(p->dev);
+  delete p;
+  return ZC_OK;
+}
+
+zc_status zc_poseidon2_permute(const zc_poseidon2* p, uint32_t* states, int64_t count,
+                               void* stream) {
+  if (!states || count < 0) return ZC_BAD_ARG;
+  if (count == 0) return ZC_OK;
+  cudaStream_t st = (cudaStream_t)stream;
+  return with_perm(p, [&](auto k, const P2Params* rt) {
+    using K = decltype(k);
+    int64_t blocks = (count + 127) / 128;
+    k_permute<K><<<(unsigned)blocks, 128, 0, st>>>(rt, states, count);
+    return launch_check();
+  });
+}
+
+static zc_status convert(zc_field field, const uint32_t* in, uint32_t* out, int64_t n, int to,
+                         void* stream) {
+  if (!in || !out || n < 0) return ZC_BAD_ARG;
+  if (n == 0) return ZC_OK;
+  cudaStream_t st = (cudaStream_t)stream;
+  return with_field(field, [&](auto f) {
+    using F = decltype(f);
+    int64_t blocks = (n + 255) / 256;
+    if (blocks > 152 * 16) blocks = 152 * 16;
+    k_convert<F><<<(unsigned)blocks, 256, 0, st>>>(in, out, n, to);
+    return launch_check();
+  });
+}
+
+zc_status zc_to_mont(zc_field field, const uint32_t* in, uint32_t* out, int64_t n, void* stream) {
+  return convert(field, in, out, n, 1, stream);
+}
+
+zc_status zc_from_mont(zc_field field, const uint32_t* in, uint32_t* out, int64_t n,
+                       void* stream) {
+  return convert(field, in, out, n, 0, stream);
+}
+
+zc_status zc_duplex_step(const zc_poseidon2* p, uint32_t* state, const uint32_t* values,
+                         int64_t m, int32_t n, uint32_t* out, int32_t* positions,
+                         int64_t block_len, void* stream) {
+  if (!state || m < 0 || n < 0 || (m > 0 && !values)) return ZC_BAD_ARG;
+  if (positions && (block_len <= 0 || block_len > 0xffffffffLL)) return ZC_BAD_ARG;
+  cudaStream_t st = (cudaStream_t)stream;
+  return with_perm(p, [&](auto k, const P2Params* rt) {
+    using K = decltype(k);
+    k_duplex_step<K><<<1, 32, 0, st>>>(rt, state, values, m, n, out, positions, block_len);
+    return launch_check();
+  });
+}
+
+zc_status zc_duplex_hop(const zc_poseidon2* p, const uint32_t* in_buf, const uint32_t* out_buf,
+                        const uint32_t* sponge, const uint32_t* in_pos, const uint32_t* out_pos,
+                        const uint32_t* values, int64_t m, int32_t n, uint32_t* in_buf_o,
+                        uint32_t* out_buf_o, uint32_t* sponge_o, uint32_t* in_pos_o,
+                        uint32_t* out_pos_o, uint32_t* challenges, void* stream) {
+  if (!in_buf || !out_buf || !sponge || !in_pos || !out_pos || !in_buf_o || !out_buf_o ||
+      !sponge_o || !in_pos_o || !out_pos_o || m < 0 || n < 0 || (m > 0 && !values) ||
+      (n > 0 && !challenges))
+    return ZC_BAD_ARG;
+  cudaStream_t st = (cudaStream_t)stream;
+  return with_perm(p, [&](auto k, const P2Params* rt) {
+    using K = decltype(k);
+    k_duplex_hop<K><<<1, 32, 0, st>>>(rt, in_buf, out_buf, sponge, in_pos, out_pos, values, m,
+                                      n, in_buf_o, out_buf_o, sponge_o, in_pos_o, out_pos_o,
+                                      challenges);
+    return launch_check();
+  });
+}
+
+zc_status zc_duplex_hop_host(const zc_poseidon2* p, const uint32_t* in_buf,
+                             const uint32_t* out_buf, const uint32_t* sponge,
+                             const uint32_t* in_pos, const uint32_t* out_pos,
+                             const uint32_t* values, int64_t m, int32_t n, uint32_t* in_buf_o,
+                             uint32_t* out_buf_o, uint32_t* sponge_o, uint32_t* in_pos_o,
+                             uint32_t* out_pos_o, uint32_t* challenges) {
+  if (!p || !in_buf || !out_buf || !sponge || !in_pos || !out_pos || !in_buf_o || !out_buf_o ||
+      !sponge_o || !in_pos_o || !out_pos_o || m < 0 || n < 0 || (m > 0 && !values) ||
+      (n > 0 && !challenges))
+    return ZC_BAD_ARG;
+  Duplex t;
+  memcpy(t.in_buf, in_buf, 32);
+  memcpy(t.out_buf, out_buf, 32);
+  memcpy(t.sponge, sponge, 64);
+  t.in_pos = (int32_t)in_pos[0];
+  t.out_pos = (int32_t)out_pos[0];
+  if (t.in_pos < 0 || t.in_pos >= 8 || t.out_pos < 0 || t.out_pos > 8) return ZC_BAD_ARG;
+  if (p->field == ZC_FIELD_BABYBEAR) {
+    RtParams<BabyBear> k{&p->host};
+    duplex_observe(t, values, m, k);
+    duplex_sample(t, n, challenges, k);
+  } else {
+    RtParams<KoalaBear> k{&p->host};
+    duplex_observe(t, values, m, k);
+    duplex_sample(t, n, challenges, k);
+  }
+  memcpy(in_buf_o, t.in_buf, 32);
+  memcpy(out_buf_o, t.out_buf, 32);
+  memcpy(sponge_o, t.sponge, 64);
+  in_pos_o[0] = (uint32_t)t.in_pos;
+  out_pos_o[0] = (uint32_t)t.out_pos;
+  return ZC_OK;
+}
+
+}  // extern "C"

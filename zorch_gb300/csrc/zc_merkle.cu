@@ -1,0 +1,359 @@
+// Merkle commit (fused per-subtree leaf hash + compression), openings, and
+// the FRI fold -- plain, and fused with the hashing of the next layer.
+//
+// One CTA owns a subtree of T = blockDim.x leaves: each thread hashes one leaf
+// (or compresses one child pair), writes the digest to its level in HBM and
+// keeps it in shared memory; the CTA then compresses in shared memory up to its
+// subtree root, writing every level (the tree keeps all layers for openings,
+// zorch/commit/merkle.py:187-202) without reading any level back from HBM.
+// Levels above the subtree roots run as further launches of the same kernel
+// fed by the stored level (NodeLeaf), log2(256)+1 levels per launch.
+#include "internal.cuh"
+
+namespace zc {
+
+constexpr int kMaxT = 256;
+
+// Leaf p = concat over q < G of base[q*gs + p*g .. +g] (zc_leaves).
+struct LayoutLeaf {
+  const uint32_t* base;
+  int G, g;
+  int64_t gs;
+  template <class K>
+  __device__ __forceinline__ void digest(int64_t p, uint32_t* d, const K& k) const {
+    // PaddingFreeSponge<16, 8, 8> (overwrite mode, no padding)
+    uint32_t s[16];
+#pragma unroll
+    for (int j = 0; j < 16; j++) s[j] = 0;
+    const int w = G * g;
+    const uint32_t* src = base + p * (int64_t)g;
+    int q = 0, r = 0;
+    for (int e = 0; e < w; e += 8) {
+#pragma unroll
+      for (int j = 0; j < 8; j++) {
+        if (e + j < w) {
+          s[j] = __ldg(src + (int64_t)q * gs + r);
+          if (++r == g) {
+            r = 0;
+            q++;
+          }
+        }
+      }
+      p2_permute(s, k);
+    }
+#pragma unroll
+    for (int j = 0; j < 8; j++) d[j] = s[j];
+  }
+};
+
+// Node p of level l0 from children 2p, 2p+1 of the stored level l0-1.
+struct NodeLeaf {
+  const uint32_t* in;
+  template <class K>
+  __device__ __forceinline__ void digest(int64_t p, uint32_t* d, const K& k) const {
+    uint32_t a[8], b[8];
+    load_digest(in + 16 * p, a);
+    load_digest(in + 16 * p + 8, b);
+    p2_compress(a, b, d, k);
+  }
+};
+
+// fri_fold_values on one element j of a natural-order layer of n elements:
+// g = (f[j] + f[j+n/2])/2 + beta * (f[j] - f[j+n/2]) * xinv, xinv = 1/(2 x_j)
+// (zorch/coding/reed_solomon.py:543-548).
+template <class F, int LI, int LB>
+struct FoldMath {
+  static constexpr int LO = (LI == 4 || LB == 4) ? 4 : 1;
+  __device__ __forceinline__ static void fold(const uint32_t* f, int64_t half, int64_t j,
+                                              uint32_t xinv, const uint32_t* beta,
+                                              uint32_t* out) {
+    uint32_t a[4] = {0, 0, 0, 0}, b[4] = {0, 0, 0, 0};
+#pragma unroll
+    for (int e = 0; e < LI; e++) {
+      a[e] = __ldg(f + j * LI + e);
+      b[e] = __ldg(f + (j + half) * LI + e);
+    }
+    uint32_t sum[4], d[4];
+#pragma unroll
+    for (int e = 0; e < LI; e++) {
+      sum[e] = mmul<F>(madd<F>(a[e], b[e]), F::INV2);
+      d[e] = mmul<F>(msub<F>(a[e], b[e]), xinv);
+    }
+    if (LO == 1) {
+      out[0] = madd<F>(sum[0], mmul<F>(beta[0], d[0]));
+    } else if (LB == 1) {  // EF4 layer, base challenge
+#pragma unroll
+      for (int e = 0; e < 4; e++) out[e] = madd<F>(sum[e], mmul<F>(beta[0], d[e]));
+    } else if (LI == 1) {  // base layer, EF4 challenge: beta * d is a scalar multiple
+#pragma unroll
+      for (int e = 0; e < 4; e++) {
+        uint32_t t = mmul<F>(beta[e], d[0]);
+        out[e] = e == 0 ? madd<F>(sum[0], t) : t;
+      }
+    } else {
+      ef4 B{{beta[0], beta[1], beta[2], beta[3]}}, D{{d[0], d[1], d[2], d[3]}};
+      ef4 r = ef_mul<F>(B, D);
+#pragma unroll
+      for (int e = 0; e < 4; e++) out[e] = madd<F>(sum[e], r.c[e]);
+    }
+  }
+};
+
+// Leaf p of the next layer's pair tree: (g[p], g[p + n/4]), computed from the
+// current layer f (n elements) and written to g on the way.
+template <class F, int LI, int LB>
+struct FoldLeaf {
+  using M = FoldMath<F, LI, LB>;
+  static constexpr int LO = M::LO;
+  const uint32_t* f;
+  uint32_t* g;
+  const uint32_t* beta;
+  int64_t n;
+  uint32_t inv2s;  // 1 / (2 shift)
+  uint32_t winv;   // w_n^-1
+  uint32_t w4inv;  // w_n^(-n/4)
+  template <class K>
+  __device__ __forceinline__ void digest(int64_t p, uint32_t* d, const K& k) const {
+    const int64_t quarter = n >> 2, half = n >> 1;
+    uint32_t bt[4];
+#pragma unroll
+    for (int e = 0; e < LB; e++) bt[e] = __ldg(beta + e);
+    uint32_t x0 = mmul<F>(inv2s, mpow<F>(winv, (uint64_t)p));
+    uint32_t x1 = mmul<F>(x0, w4inv);
+    uint32_t o0[4], o1[4];
+    M::fold(f, half, p, x0, bt, o0);
+    M::fold(f, half, p + quarter, x1, bt, o1);
+    uint32_t s[16];
+#pragma unroll
+    for (int j = 0; j < 16; j++) s[j] = 0;
+#pragma unroll
+    for (int e = 0; e < LO; e++) {
+      g[p * LO + e] = o0[e];
+      g[(p + quarter) * LO + e] = o1[e];
+      s[e] = o0[e];
+      s[LO + e] = o1[e];
+    }
+    p2_permute(s, k);  // 2*LO <= 8 elements: one absorb block
+#pragma unroll
+    for (int j = 0; j < 8; j++) d[j] = s[j];
+  }
+};
+
+template <class K, class Leaf>
+__global__ void __launch_bounds__(kMaxT) k_subtree(Leaf leaf, uint32_t* layers, int64_t L,
+                                                   int l0, const P2Params* rt) {
+  __shared__ P2Params s_rt;
+  __shared__ uint32_t sm[8 * kMaxT];  // [word][node]: conflict-free digest slots
+  K k = KIn<K>::make(rt, &s_rt);
+  const int T = blockDim.x, t = threadIdx.x;
+  const int64_t p = (int64_t)blockIdx.x * T + t;
+  uint32_t d[8];
+  leaf.digest(p, d, k);
+  store_digest(layers + 8 * (level_offset(L, l0) + p), d);
+#pragma unroll
+  for (int i = 0; i < 8; i++) sm[i * kMaxT + t] = d[i];
+  int lvl = l0, width = T;
+  while (width > 1) {
+    __syncthreads();
+    width >>= 1;
+    lvl++;
+    uint32_t a[8], b[8];
+    if (t < width) {
+#pragma unroll
+      for (int i = 0; i < 8; i++) {
+        a[i] = sm[i * kMaxT + 2 * t];
+        b[i] = sm[i * kMaxT + 2 * t + 1];
+      }
+    }
+    __syncthreads();
+    if (t < width) {
+      p2_compress(a, b, d, k);
+      store_digest(layers + 8 * (level_offset(L, lvl) + (int64_t)blockIdx.x * width + t), d);
+#pragma unroll
+      for (int i = 0; i < 8; i++) sm[i * kMaxT + t] = d[i];
+    }
+  }
+}
+
+// Launches the levels above `l_done` (all levels <= l_done already stored).
+template <class K>
+zc_status finish_tree(uint32_t* layers, int64_t L, int l_done, const P2Params* rt,
+                      cudaStream_t st) {
+  const int depth = ilog2(L);
+  int l = l_done;
+  while (l < depth) {
+    const int64_t parents = (L >> l) >> 1;
+    const int T = parents < kMaxT ? (int)parents : kMaxT;
+    NodeLeaf nl{layers + 8 * level_offset(L, l)};
+    k_subtree<K, NodeLeaf><<<(unsigned)(parents / T), T, 0, st>>>(nl, layers, L, l + 1, rt);
+    ZC_TRY(launch_check());
+    l += 1 + ilog2(T);
+  }
+  return ZC_OK;
+}
+
+template <class K, class Leaf>
+zc_status commit_tree(const Leaf& leaf, uint32_t* layers, int64_t L, const P2Params* rt,
+                      cudaStream_t st) {
+  const int T0 = L < kMaxT ? (int)L : kMaxT;
+  k_subtree<K, Leaf><<<(unsigned)(L / T0), T0, 0, st>>>(leaf, layers, L, 0, rt);
+  ZC_TRY(launch_check());
+  return finish_tree<K>(layers, L, ilog2(T0), rt, st);
+}
+
+__global__ void k_open(zc_leaves lv, const uint32_t* layers, const int32_t* idx, int q, int depth,
+                       uint32_t* rows, uint32_t* paths, uint32_t* oob) {
+  const int qi = blockIdx.x;
+  int64_t i = idx[qi];
+  if (i < 0 || i >= lv.num_leaves) {
+    if (threadIdx.x == 0 && oob) atomicOr(oob, 1u);
+    i = i < 0 ? 0 : lv.num_leaves - 1;
+  }
+  const int w = lv.groups * lv.group_len;
+  for (int e = threadIdx.x; e < w; e += blockDim.x) {
+    const int gq = e / lv.group_len, r = e - gq * lv.group_len;
+    rows[(int64_t)qi * w + e] = lv.base[gq * lv.group_stride + i * lv.group_len + r];
+  }
+  const int64_t L = lv.num_leaves;
+  for (int x = threadIdx.x; x < depth * 8; x += blockDim.x) {
+    const int l = x >> 3, word = x & 7;
+    const int64_t node = (i >> l) ^ 1;
+    paths[((int64_t)l * q + qi) * 8 + word] = layers[8 * (level_offset(L, l) + node) + word];
+  }
+}
+
+template <class F, int LI, int LB>
+__global__ void k_fold(const uint32_t* f, int64_t n, const uint32_t* beta, uint32_t inv2s,
+                       uint32_t winv, uint32_t* g) {
+  using M = FoldMath<F, LI, LB>;
+  const int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const int64_t half = n >> 1;
+  if (j >= half) return;
+  uint32_t bt[4];
+#pragma unroll
+  for (int e = 0; e < LB; e++) bt[e] = __ldg(beta + e);
+  uint32_t out[4];
+  M::fold(f, half, j, mmul<F>(inv2s, mpow<F>(winv, (uint64_t)j)), bt, out);
+#pragma unroll
+  for (int e = 0; e < M::LO; e++) g[j * M::LO + e] = out[e];
+}
+
+template <class F>
+struct FoldScalars {
+  uint32_t inv2s, winv, w4inv;
+};
+
+template <class F>
+zc_status fold_scalars(int64_t n, uint32_t shift_mont, uint32_t generator, FoldScalars<F>* o) {
+  if (generator != 0 && generator != F::GEN) {
+    set_error("only the field's canonical generator is built");
+    return ZC_UNSUPPORTED;
+  }
+  const int log_n = ilog2(n);
+  const uint32_t w = root_of_unity<F>(log_n, generator);
+  o->winv = minv<F>(w);
+  const uint32_t sh = shift_mont ? shift_mont : F::ONE;
+  o->inv2s = mmul<F>(F::INV2, minv<F>(sh));
+  o->w4inv = n >= 4 ? mpow<F>(o->winv, (uint64_t)(n >> 2)) : F::ONE;
+  return ZC_OK;
+}
+
+template <class F, int LI, int LB>
+zc_status fold_launch(const uint32_t* cw, int64_t n, const uint32_t* beta, uint32_t shift_mont,
+                      uint32_t generator, uint32_t* out, cudaStream_t st) {
+  FoldScalars<F> fs;
+  ZC_TRY(fold_scalars<F>(n, shift_mont, generator, &fs));
+  const int64_t half = n >> 1;
+  const int B = 256;
+  k_fold<F, LI, LB><<<(unsigned)((half + B - 1) / B), B, 0, st>>>(cw, n, beta, fs.inv2s, fs.winv,
+                                                                  out);
+  return launch_check();
+}
+
+template <class K, int LI, int LB>
+zc_status fold_commit_launch(const uint32_t* cw, int64_t n, const uint32_t* beta,
+                             uint32_t shift_mont, uint32_t generator, uint32_t* out,
+                             uint32_t* layers, const P2Params* rt, cudaStream_t st) {
+  using F = typename K::F;
+  FoldScalars<F> fs;
+  ZC_TRY(fold_scalars<F>(n, shift_mont, generator, &fs));
+  FoldLeaf<F, LI, LB> leaf{cw, out, beta, n, fs.inv2s, fs.winv, fs.w4inv};
+  return commit_tree<K>(leaf, layers, n >> 2, rt, st);
+}
+
+}  // namespace zc
+
+using namespace zc;
+
+extern "C" {
+
+zc_status zc_merkle_commit(const zc_poseidon2* p, zc_leaves lv, uint32_t* layers, void* stream) {
+  if (!layers || (!lv.base && lv.groups * lv.group_len > 0) || lv.groups < 0 ||
+      lv.group_len < 0)
+    return ZC_BAD_ARG;
+  if (!is_pow2(lv.num_leaves)) {
+    set_error("leaf count must be a power of two");
+    return ZC_NOT_POW2;
+  }
+  if ((uintptr_t)layers % 16) return ZC_BAD_ARG;
+  if ((int64_t)lv.groups * lv.group_len > (1 << 20)) return ZC_BAD_SHAPE;
+  cudaStream_t st = (cudaStream_t)stream;
+  LayoutLeaf leaf{lv.base, lv.groups, lv.group_len, lv.group_stride};
+  return with_perm(p, [&](auto k, const P2Params* rt) {
+    using K = decltype(k);
+    return commit_tree<K>(leaf, layers, lv.num_leaves, rt, st);
+  });
+}
+
+zc_status zc_merkle_open(zc_leaves lv, const uint32_t* layers, const int32_t* idx, int32_t q,
+                         uint32_t* rows, uint32_t* paths, uint32_t* oob_flag, void* stream) {
+  if (q < 0 || !layers || !idx || (q > 0 && (!rows || !paths))) return ZC_BAD_ARG;
+  if (!is_pow2(lv.num_leaves)) return ZC_NOT_POW2;
+  if (q == 0) return ZC_OK;
+  const int depth = ilog2(lv.num_leaves);
+  k_open<<<q, 128, 0, (cudaStream_t)stream>>>(lv, layers, idx, q, depth, rows, paths, oob_flag);
+  return launch_check();
+}
+
+zc_status zc_fri_fold(zc_field field, const uint32_t* cw, int64_t n, int ef_in,
+                      const uint32_t* beta, int ef_beta, uint32_t shift_mont, uint32_t generator,
+                      uint32_t* out, void* stream) {
+  if (!cw || !beta || !out) return ZC_BAD_ARG;
+  if (!is_pow2(n) || n < 2) {
+    set_error("fri_fold requires a power-of-two codeword of length >= 2");
+    return ZC_NOT_POW2;
+  }
+  cudaStream_t st = (cudaStream_t)stream;
+  return with_field(field, [&](auto f) {
+    using F = decltype(f);
+    if (ef_in && ef_beta) return fold_launch<F, 4, 4>(cw, n, beta, shift_mont, generator, out, st);
+    if (ef_in) return fold_launch<F, 4, 1>(cw, n, beta, shift_mont, generator, out, st);
+    if (ef_beta) return fold_launch<F, 1, 4>(cw, n, beta, shift_mont, generator, out, st);
+    return fold_launch<F, 1, 1>(cw, n, beta, shift_mont, generator, out, st);
+  });
+}
+
+zc_status zc_fri_fold_commit(const zc_poseidon2* p, const uint32_t* cw, int64_t n, int ef_in,
+                             const uint32_t* beta, int ef_beta, uint32_t shift_mont,
+                             uint32_t generator, uint32_t* out, uint32_t* next_layers,
+                             void* stream) {
+  if (!cw || !beta || !out || !next_layers) return ZC_BAD_ARG;
+  if (!is_pow2(n) || n < 4) {
+    set_error("fri_fold_commit requires a power-of-two codeword of length >= 4");
+    return ZC_NOT_POW2;
+  }
+  if ((uintptr_t)next_layers % 16) return ZC_BAD_ARG;
+  cudaStream_t st = (cudaStream_t)stream;
+  return with_perm(p, [&](auto k, const P2Params* rt) {
+    using K = decltype(k);
+    if (ef_in && ef_beta)
+      return fold_commit_launch<K, 4, 4>(cw, n, beta, shift_mont, generator, out, next_layers, rt, st);
+    if (ef_in)
+      return fold_commit_launch<K, 4, 1>(cw, n, beta, shift_mont, generator, out, next_layers, rt, st);
+    if (ef_beta)
+      return fold_commit_launch<K, 1, 4>(cw, n, beta, shift_mont, generator, out, next_layers, rt, st);
+    return fold_commit_launch<K, 1, 1>(cw, n, beta, shift_mont, generator, out, next_layers, rt, st);
+  });
+}
+
+}  // extern "C"

@@ -1,0 +1,361 @@
+// Reed-Solomon coset low-degree extension (ReedSolomon.encode,
+// zorch/coding/reed_solomon.py:177-188): out[j] = sum_i m_i (h w_n^j)^i,
+// natural order in and out, n = k * b.
+//
+// Decomposition: with j = b*t + s (s < b, t < k),
+//   out[b*t + s] = NTT_k(m_i * g_s^i)[t],   g_s = h * w_n^s,
+// i.e. b coset NTTs of size k over the unpadded message (the zero padding of
+// the reference is never materialised). Each size-k NTT runs in shared memory:
+//  - k <= 4096 and b*k <= 16384: one pass, one CTA per column holding all b
+//    cosets, so the b*k outputs are written as one contiguous block;
+//  - otherwise the four-step (Bailey) split k = k1 * k2: pass 1 runs k2-point
+//    NTTs down strided columns (a tile of consecutive i1 per CTA, one coset
+//    per CTA), multiplies by w_k^(i1*t2) and writes a [b][k2][k1] intermediate
+//    to the caller's workspace; pass 2 runs the k1-point NTTs along its rows
+//    for all b cosets of a t2 tile and writes contiguous b*TT runs of out.
+// In shared memory the transform is an iterative radix-2 DIT whose input is
+// stored bit-reversed as it is loaded (the bit reversal folded into the load),
+// processed 4 stages per register pass (16 elements per thread).
+#include "internal.cuh"
+
+namespace zc {
+
+// w^i tables for the primitive 2^TA-th root w = gen^((p-1)/2^TA) (TA = the
+// field's two-adicity): lo[i] = w^i (i < 2^14), hi[i] = w^(i*2^14). Static
+// device memory -- no allocation; filled once per device by zc_init.
+constexpr int kRootLoBits = 14;
+__device__ uint32_t g_roots_bb[(1 << kRootLoBits) + (1 << (BabyBear::TWO_ADICITY - kRootLoBits))];
+__device__ uint32_t g_roots_kb[(1 << kRootLoBits) + (1 << (KoalaBear::TWO_ADICITY - kRootLoBits))];
+
+template <class F>
+__device__ __forceinline__ uint32_t* roots_tab();
+template <>
+__device__ __forceinline__ uint32_t* roots_tab<BabyBear>() { return g_roots_bb; }
+template <>
+__device__ __forceinline__ uint32_t* roots_tab<KoalaBear>() { return g_roots_kb; }
+
+template <class F>
+__global__ void k_init_roots() {
+  constexpr int lo = 1 << kRootLoBits, hi = 1 << (F::TWO_ADICITY - kRootLoBits);
+  const uint32_t w = root_of_unity<F>(F::TWO_ADICITY, 0);
+  uint32_t* t = roots_tab<F>();
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < lo + hi; i += gridDim.x * blockDim.x) {
+    const uint64_t e = i < lo ? (uint64_t)i : (uint64_t)(i - lo) << kRootLoBits;
+    t[i] = mpow<F>(w, e);
+  }
+}
+
+zc_status init_root_tables() {
+  k_init_roots<BabyBear><<<64, 256>>>();
+  ZC_TRY(launch_check());
+  k_init_roots<KoalaBear><<<64, 256>>>();
+  ZC_TRY(launch_check());
+  return ZC_OK;
+}
+
+// w_{2^log_n}^e for e < 2^log_n.
+template <class F>
+__device__ __forceinline__ uint32_t omega_pow(int log_n, uint32_t e) {
+  const uint32_t E = e << (F::TWO_ADICITY - log_n);
+  const uint32_t* t = roots_tab<F>();
+  return mmul<F>(t[E & ((1u << kRootLoBits) - 1)], t[(1u << kRootLoBits) + (E >> kRootLoBits)]);
+}
+
+__device__ __forceinline__ int pad(int i) { return i + (i >> 5); }
+__device__ __forceinline__ int brev(int i, int bits) {
+  return bits ? (int)(__brev((unsigned)i) >> (32 - bits)) : 0;
+}
+__host__ __device__ __forceinline__ int padded(int m) { return m + (m >> 5); }
+
+// tab[i] = base^i for i < count (count a power of two), by doubling.
+template <class F>
+__device__ void pow_table(uint32_t* tab, int count, uint32_t base) {
+  if (threadIdx.x == 0) {
+    tab[0] = F::ONE;
+    if (count > 1) tab[1] = base;
+  }
+  __syncthreads();
+  for (int len = 2; len < count; len <<= 1) {
+    const uint32_t step = mmul<F>(tab[len >> 1], tab[len >> 1]);
+    for (int i = threadIdx.x; i < len; i += blockDim.x) tab[len + i] = mmul<F>(tab[i], step);
+    __syncthreads();
+  }
+}
+
+// Stages s0 .. s0+R-1 of the DIT over `rows` rows of m = 2^logm (padded row
+// stride rs), twiddles tw[e] = w_m^e.
+template <class F, int R>
+__device__ __forceinline__ void dit_pass(uint32_t* a, int rows, int logm, int rs,
+                                         const uint32_t* tw, int s0) {
+  constexpr int G = 1 << R;
+  const int glog = logm - R;
+  const int total = rows << glog;
+  for (int gi = threadIdx.x; gi < total; gi += blockDim.x) {
+    const int row = gi >> glog, q = gi & ((1 << glog) - 1);
+    const int off = q & ((1 << s0) - 1), blk = q >> s0;
+    const int base = (blk << (s0 + R)) | off;
+    uint32_t* ar = a + row * rs;
+    uint32_t v[G];
+#pragma unroll
+    for (int j = 0; j < G; j++) v[j] = ar[pad(base + (j << s0))];
+#pragma unroll
+    for (int r = 0; r < R; r++) {
+      const int s = s0 + r;
+#pragma unroll
+      for (int j = 0; j < G; j++) {
+        if (!(j & (1 << r))) {
+          const int j2 = j | (1 << r);
+          const int pos = off + ((j & ((1 << r) - 1)) << s0);
+          const uint32_t w = tw[pos << (logm - 1 - s)];
+          const uint32_t t = mmul<F>(v[j2], w);
+          v[j2] = msub<F>(v[j], t);
+          v[j] = madd<F>(v[j], t);
+        }
+      }
+    }
+#pragma unroll
+    for (int j = 0; j < G; j++) ar[pad(base + (j << s0))] = v[j];
+  }
+}
+
+// Natural-order NTT of each row (input stored bit-reversed).
+template <class F>
+__device__ void smem_ntt(uint32_t* a, int rows, int logm, int rs, const uint32_t* tw) {
+  for (int s0 = 0; s0 < logm; s0 += 4) {
+    const int R = logm - s0 < 4 ? logm - s0 : 4;
+    switch (R) {
+      case 4: dit_pass<F, 4>(a, rows, logm, rs, tw, s0); break;
+      case 3: dit_pass<F, 3>(a, rows, logm, rs, tw, s0); break;
+      case 2: dit_pass<F, 2>(a, rows, logm, rs, tw, s0); break;
+      default: dit_pass<F, 1>(a, rows, logm, rs, tw, s0); break;
+    }
+    __syncthreads();
+  }
+}
+
+constexpr int kThreads = 512;
+
+template <class F>
+__global__ void __launch_bounds__(kThreads) k_lde_small(const uint32_t* x, uint32_t* out,
+                                                        int log_k, int log_b, uint32_t h) {
+  extern __shared__ uint32_t sm[];
+  const int k = 1 << log_k, b = 1 << log_b, log_n = log_k + log_b;
+  const int rs = padded(k);
+  uint32_t* work = sm;
+  uint32_t* tw = work + b * rs;
+  uint32_t* hp = tw + (k > 1 ? k / 2 : 1);
+  const int64_t c = blockIdx.x;
+  const uint32_t* xc = x + (c << log_k);
+  pow_table<F>(tw, k > 1 ? k / 2 : 1, log_k ? omega_pow<F>(log_k, 1) : F::ONE);
+  pow_table<F>(hp, k, h);
+  for (int idx = threadIdx.x; idx < (b << log_k); idx += blockDim.x) {
+    const int s = idx >> log_k, i = idx & (k - 1);
+    uint32_t v = mmul<F>(__ldg(xc + i), hp[i]);
+    if (s) v = mmul<F>(v, omega_pow<F>(log_n, (uint32_t)(s * i)));
+    work[s * rs + pad(brev(i, log_k))] = v;
+  }
+  __syncthreads();
+  smem_ntt<F>(work, b, log_k, rs, tw);
+  uint32_t* oc = out + (c << log_n);
+  for (int idx = threadIdx.x; idx < (b << log_k); idx += blockDim.x) {
+    const int t = idx >> log_b, s = idx & (b - 1);
+    oc[idx] = work[s * rs + pad(t)];
+  }
+}
+
+// Pass 1: grid (coset s, i1 tile, column). z layout per column: [b][k2][k1].
+template <class F>
+__global__ void __launch_bounds__(kThreads) k_lde_pass1(const uint32_t* x, uint32_t* z, int log_k1,
+                                                        int log_k2, int log_b, int log_ti,
+                                                        uint32_t h) {
+  extern __shared__ uint32_t sm[];
+  const int k1 = 1 << log_k1, k2 = 1 << log_k2, TI = 1 << log_ti;
+  const int log_k = log_k1 + log_k2, log_n = log_k + log_b;
+  const int rs = padded(k2);
+  uint32_t* work = sm;
+  uint32_t* tw = work + TI * rs;
+  uint32_t* R = tw + (k2 > 1 ? k2 / 2 : 1);
+  uint32_t* gi = R + k2;
+  const int s = blockIdx.x;
+  const int i1_0 = blockIdx.y * TI;
+  const int64_t c = blockIdx.z;
+  const uint32_t gs = mmul<F>(h, s ? omega_pow<F>(log_n, (uint32_t)s) : F::ONE);
+  const uint32_t G = mpow<F>(gs, (uint64_t)k1);
+  pow_table<F>(tw, k2 > 1 ? k2 / 2 : 1, log_k2 ? omega_pow<F>(log_k2, 1) : F::ONE);
+  pow_table<F>(R, k2, G);
+  for (int i = threadIdx.x; i < TI; i += blockDim.x) gi[i] = mpow<F>(gs, (uint64_t)(i1_0 + i));
+  __syncthreads();
+  const uint32_t* xc = x + (c << log_k);
+  for (int idx = threadIdx.x; idx < (TI << log_k2); idx += blockDim.x) {
+    const int d = idx & (TI - 1), i2 = idx >> log_ti;
+    uint32_t v = __ldg(xc + i1_0 + d + ((int64_t)i2 << log_k1));
+    v = mmul<F>(mmul<F>(v, gi[d]), R[i2]);
+    work[d * rs + pad(brev(i2, log_k2))] = v;
+  }
+  __syncthreads();
+  smem_ntt<F>(work, TI, log_k2, rs, tw);
+  uint32_t* zc_ = z + ((c << log_b) + s) * ((int64_t)1 << log_k);
+  for (int idx = threadIdx.x; idx < (TI << log_k2); idx += blockDim.x) {
+    const int d = idx & (TI - 1), t2 = idx >> log_ti;
+    uint32_t v = work[d * rs + pad(t2)];
+    v = mmul<F>(v, omega_pow<F>(log_k, (uint32_t)((i1_0 + d) * t2)));
+    zc_[((int64_t)t2 << log_k1) + i1_0 + d] = v;
+  }
+}
+
+// Pass 2: grid (t2 tile, column); all b cosets of TT rows per CTA.
+template <class F>
+__global__ void __launch_bounds__(kThreads) k_lde_pass2(const uint32_t* z, uint32_t* out,
+                                                        int log_k1, int log_k2, int log_b,
+                                                        int log_tt) {
+  extern __shared__ uint32_t sm[];
+  const int k1 = 1 << log_k1, TT = 1 << log_tt, b = 1 << log_b;
+  const int log_k = log_k1 + log_k2, log_n = log_k + log_b;
+  const int rows = b * TT;
+  const int rs = padded(k1);
+  uint32_t* work = sm;
+  uint32_t* tw = work + rows * rs;
+  const int t2_0 = blockIdx.x * TT;
+  const int64_t c = blockIdx.y;
+  pow_table<F>(tw, k1 > 1 ? k1 / 2 : 1, log_k1 ? omega_pow<F>(log_k1, 1) : F::ONE);
+  const uint32_t* zc_ = z + (c << log_n);
+  for (int idx = threadIdx.x; idx < (rows << log_k1); idx += blockDim.x) {
+    const int i1 = idx & (k1 - 1), row = idx >> log_k1;
+    const int s = row >> log_tt, dt = row & (TT - 1);
+    const uint32_t v =
+        zc_[((int64_t)s << log_k) + ((int64_t)(t2_0 + dt) << log_k1) + i1];
+    work[row * rs + pad(brev(i1, log_k1))] = v;
+  }
+  __syncthreads();
+  smem_ntt<F>(work, rows, log_k1, rs, tw);
+  uint32_t* oc = out + (c << log_n);
+  for (int idx = threadIdx.x; idx < (rows << log_k1); idx += blockDim.x) {
+    const int s = idx & (b - 1), dt = (idx >> log_b) & (TT - 1), t1 = idx >> (log_b + log_tt);
+    const uint32_t v = work[((s << log_tt) + dt) * rs + pad(t1)];
+    oc[((int64_t)(t2_0 + dt + ((int64_t)t1 << log_k2)) << log_b) + s] = v;
+  }
+}
+
+struct LdePlan {
+  bool small;
+  int log_k1, log_k2, log_ti, log_tt;
+  size_t smem_small, smem1, smem2;
+};
+
+constexpr int kSmallMaxLogK = 12;
+constexpr int kSmallMaxLogN = 14;
+constexpr int kTileLog = 14;  // elements per shared-memory tile (2^14 = 64 KB)
+
+inline LdePlan plan_lde(int log_k, int log_b) {
+  LdePlan p{};
+  const int k = 1 << log_k, b = 1 << log_b;
+  p.small = log_k <= kSmallMaxLogK && log_k + log_b <= kSmallMaxLogN;
+  p.smem_small = 4 * ((size_t)b * padded(k) + (k > 1 ? k / 2 : 1) + k);
+  p.log_k2 = log_k / 2;
+  p.log_k1 = log_k - p.log_k2;
+  int ti = kTileLog - p.log_k2;
+  if (p.log_k2 >= 12 && ti < 3) ti = 3;
+  if (ti > p.log_k1) ti = p.log_k1;
+  if (ti < 0) ti = 0;
+  p.log_ti = ti;
+  int tt = kTileLog - p.log_k1 - log_b;
+  if (tt > p.log_k2) tt = p.log_k2;
+  if (tt < 0) tt = 0;
+  p.log_tt = tt;
+  const int k1 = 1 << p.log_k1, k2 = 1 << p.log_k2;
+  p.smem1 = 4 * ((size_t)(1 << p.log_ti) * padded(k2) + (k2 > 1 ? k2 / 2 : 1) + k2 +
+                 (1 << p.log_ti));
+  p.smem2 = 4 * ((size_t)(b << p.log_tt) * padded(k1) + (k1 > 1 ? k1 / 2 : 1));
+  return p;
+}
+
+template <class F>
+zc_status lde_launch(const uint32_t* x, int64_t batch, int log_k, int log_b, uint32_t h,
+                     uint32_t* out, void* ws, size_t ws_bytes, cudaStream_t st) {
+  const LdePlan p = plan_lde(log_k, log_b);
+  const int log_n = log_k + log_b;
+  const size_t smem_cap = 227 * 1024;
+  if ((p.small && p.smem_small > smem_cap) ||
+      (!p.small && (p.smem1 > smem_cap || p.smem2 > smem_cap))) {
+    set_error("LDE tile does not fit in shared memory (blowup too large for this size)");
+    return ZC_UNSUPPORTED;
+  }
+  if (p.small) {
+    ZC_CUDA(cudaFuncSetAttribute(k_lde_small<F>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)p.smem_small));
+    for (int64_t c0 = 0; c0 < batch; c0 += 0x7fffffff) {
+      const int64_t cols = batch - c0 < 0x7fffffff ? batch - c0 : 0x7fffffff;
+      k_lde_small<F><<<(unsigned)cols, kThreads, p.smem_small, st>>>(
+          x + (c0 << log_k), out + (c0 << log_n), log_k, log_b, h);
+      ZC_TRY(launch_check());
+    }
+    return ZC_OK;
+  }
+  const size_t col_bytes = (size_t)4 << log_n;
+  if (!ws || ws_bytes < col_bytes) {
+    set_error("rs_encode workspace smaller than one column's LDE (4 * 2^(log_k+log_b) bytes)");
+    return ZC_OOM;
+  }
+  if ((uintptr_t)ws % 16) return ZC_BAD_ARG;
+  int64_t chunk = (int64_t)(ws_bytes / col_bytes);
+  if (chunk > 65535) chunk = 65535;
+  if (chunk > batch) chunk = batch;
+  ZC_CUDA(cudaFuncSetAttribute(k_lde_pass1<F>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                               (int)p.smem1));
+  ZC_CUDA(cudaFuncSetAttribute(k_lde_pass2<F>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                               (int)p.smem2));
+  uint32_t* z = (uint32_t*)ws;
+  for (int64_t c0 = 0; c0 < batch; c0 += chunk) {
+    const int64_t cols = batch - c0 < chunk ? batch - c0 : chunk;
+    dim3 g1(1u << log_b, 1u << (p.log_k1 - p.log_ti), (unsigned)cols);
+    k_lde_pass1<F><<<g1, kThreads, p.smem1, st>>>(x + (c0 << log_k), z, p.log_k1, p.log_k2,
+                                                  log_b, p.log_ti, h);
+    ZC_TRY(launch_check());
+    dim3 g2(1u << (p.log_k2 - p.log_tt), (unsigned)cols);
+    k_lde_pass2<F><<<g2, kThreads, p.smem2, st>>>(z, out + (c0 << log_n), p.log_k1, p.log_k2,
+                                                  log_b, p.log_tt);
+    ZC_TRY(launch_check());
+  }
+  return ZC_OK;
+}
+
+}  // namespace zc
+
+using namespace zc;
+
+extern "C" {
+
+size_t zc_rs_encode_workspace_bytes(int64_t batch, int log_k, int log_blowup) {
+  if (batch <= 0 || log_k < 0 || log_blowup < 0) return 0;
+  const LdePlan p = plan_lde(log_k, log_blowup);
+  if (p.small) return 0;
+  const size_t col = (size_t)4 << (log_k + log_blowup);
+  size_t cols = (size_t)batch;
+  const size_t cap = (size_t)1 << 30;  // 1 GiB of intermediate per chunk by default
+  if (cols * col > cap) cols = cap / col ? cap / col : 1;
+  return cols * col;
+}
+
+zc_status zc_rs_encode(zc_field field, const uint32_t* coeffs, int64_t batch, int log_k,
+                       int log_blowup, uint32_t shift_mont, uint32_t generator, uint32_t* out,
+                       void* workspace, size_t workspace_bytes, void* stream) {
+  if (!coeffs || !out || batch < 0 || log_k < 0 || log_blowup < 0) return ZC_BAD_ARG;
+  if (batch == 0) return ZC_OK;
+  return with_field(field, [&](auto f) -> zc_status {
+    using F = decltype(f);
+    if (log_k + log_blowup > F::TWO_ADICITY || log_k > 24) {
+      set_error("LDE size exceeds the supported two-adic range");
+      return ZC_BAD_SHAPE;
+    }
+    if (generator != 0 && generator != F::GEN) {
+      set_error("only the field's canonical generator is built");
+      return ZC_UNSUPPORTED;
+    }
+    ZC_TRY(ensure_init());
+    const uint32_t h = shift_mont ? shift_mont : F::ONE;
+    return lde_launch<F>(coeffs, batch, log_k, log_blowup, h, out, workspace, workspace_bytes,
+                         (cudaStream_t)stream);
+  });
+}
+
+}  // extern "C"

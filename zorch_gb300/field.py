@@ -1,0 +1,130 @@
+"""Field descriptors and canonical <-> Montgomery conversion.
+
+Device data is Montgomery u32 (x * 2^32 mod p) held in torch.int32 tensors as
+raw bit patterns -- the storage of zk_dtypes' `babybear_mont` /
+`koalabear_mont` and the reference's Fiat-Shamir wire form
+(zorch/transcript.py:986-999).
+"""
+
+from __future__ import annotations
+
+from dataclasses import dataclass
+
+import numpy as np
+import torch
+
+from . import _lib
+
+
+@dataclass(frozen=True)
+class Field:
+    id: int
+    name: str
+    p: int
+    generator: int
+    two_adicity: int
+    ef4_w: int  # EF4 = F[x]/(x^4 - w)
+
+    @property
+    def one_mont(self) -> int:
+        return (1 << 32) % self.p
+
+    def mont(self, x: int) -> int:
+        return ((x % self.p) << 32) % self.p
+
+    def canon(self, x: int) -> int:
+        return x * pow(1 << 32, self.p - 2, self.p) % self.p
+
+    def mul_mont(self, a: int, b: int) -> int:
+        return a * b * pow(1 << 32, self.p - 2, self.p) % self.p
+
+    def pow_mont(self, a: int, e: int) -> int:
+        return self.mont(pow(self.canon(a), e, self.p))
+
+    def inv_mont(self, a: int) -> int:
+        return self.mont(pow(self.canon(a), self.p - 2, self.p))
+
+    def root_of_unity(self, log_n: int, generator: int | None = None) -> int:
+        g = generator or self.generator
+        return pow(g, (self.p - 1) >> log_n, self.p)
+
+
+BABYBEAR = Field(_lib.BABYBEAR, "babybear", 2013265921, 31, 27, 11)
+KOALABEAR = Field(_lib.KOALABEAR, "koalabear", 2130706433, 3, 24, 3)
+FIELDS = {BABYBEAR.id: BABYBEAR, KOALABEAR.id: KOALABEAR}
+
+
+def field_of(f: "Field | int | str") -> Field:
+    if isinstance(f, Field):
+        return f
+    if isinstance(f, str):
+        return {"babybear": BABYBEAR, "koalabear": KOALABEAR}[f.lower()]
+    return FIELDS[int(f)]
+
+
+# ---------------------------------------------------------------- host ----
+def to_mont_np(field, x) -> np.ndarray:
+    f = field_of(field)
+    x = np.asarray(x, dtype=np.uint64) % np.uint64(f.p)
+    return ((x << np.uint64(32)) % np.uint64(f.p)).astype(np.uint32)
+
+
+def from_mont_np(field, x) -> np.ndarray:
+    f = field_of(field)
+    rinv = np.uint64(pow(1 << 32, f.p - 2, f.p))
+    x = np.asarray(x, dtype=np.uint64)
+    # x < p < 2^31 and rinv < 2^31, so the product fits in 62 bits
+    return ((x * rinv) % np.uint64(f.p)).astype(np.uint32)
+
+
+# -------------------------------------------------------------- device ----
+def stream_handle(stream: torch.cuda.Stream | None = None) -> int:
+    s = stream if stream is not None else torch.cuda.current_stream()
+    return int(s.cuda_stream)
+
+
+def ptr(t: torch.Tensor | None) -> int | None:
+    """Device pointer of a contiguous 32-bit CUDA tensor (None passes through)."""
+    if t is None:
+        return None
+    if not t.is_cuda:
+        raise ValueError("expected a CUDA tensor")
+    if t.element_size() != 4:
+        raise ValueError(f"expected a 32-bit tensor, got {t.dtype}")
+    if not t.is_contiguous():
+        raise ValueError("expected a contiguous tensor")
+    return t.data_ptr()
+
+
+def to_device(x: np.ndarray, device="cuda") -> torch.Tensor:
+    """Host u32 array -> int32 device tensor of the same bits."""
+    a = np.ascontiguousarray(np.asarray(x, dtype=np.uint32)).view(np.int32)
+    return torch.from_numpy(a).to(device)
+
+
+def to_host(t: torch.Tensor) -> np.ndarray:
+    """int32 device tensor -> u32 host array of the same bits."""
+    return t.detach().contiguous().cpu().numpy().view(np.uint32)
+
+
+def to_mont(field, t: torch.Tensor, out: torch.Tensor | None = None) -> torch.Tensor:
+    """Canonical -> Montgomery on the device (zc_to_mont)."""
+    f = field_of(field)
+    out = torch.empty_like(t) if out is None else out
+    _lib.check(_lib.lib().zc_to_mont(f.id, ptr(t), ptr(out), t.numel(), stream_handle()),
+               "to_mont")
+    return out
+
+
+def from_mont(field, t: torch.Tensor, out: torch.Tensor | None = None) -> torch.Tensor:
+    f = field_of(field)
+    out = torch.empty_like(t) if out is None else out
+    _lib.check(_lib.lib().zc_from_mont(f.id, ptr(t), ptr(out), t.numel(), stream_handle()),
+               "from_mont")
+    return out
+
+
+def random_canonical(field, shape, seed: int) -> np.ndarray:
+    """Seeded uniform draw in [0, p) (PCG64 via numpy.random.default_rng)."""
+    f = field_of(field)
+    return np.random.default_rng(seed).integers(0, f.p, size=shape, dtype=np.uint64).astype(np.uint32)
