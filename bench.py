@@ -1,0 +1,383 @@
+#!/usr/bin/env python
+"""Benchmark of the polynomial-commitment hot path on GB300.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl zorch|reference]
+                    [--workload trace|served]
+
+Prints ONE JSON line (rank 0). Workloads (seeded synthetic BabyBear data,
+uniform in [0, p), canonical form converted to Montgomery inside each step):
+
+- trace:  a 2^20 x 64 matrix, every column coset-LDE'd at blowup 4 (shift 31,
+          generator 31) to 2^22 x 64, row leaves hashed (Poseidon2-16 sponge,
+          64 elements per leaf), binary compression to one root, then 128
+          seeded query openings (row + authentication path).
+- served: the continuous-batching commit stream (see zorch_gb300/serve.py).
+
+value = input field elements committed per second with inputs resident in
+HBM; e2e = the same through the public API from pinned host buffers with the
+host<->device copies inside the timed region. --impl reference times the
+reference algorithm's CPU restatement (the oracle; the reference itself is
+Python over FRX wheels absent from this image) on the host cores.
+Multi-GPU: replicas only (each rank runs the same workload; no collective).
+"""
+
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+P = 2013265921
+METRIC = "field elements committed/s (batched/served vs plain GPU path)"
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["zorch", "reference"], default="zorch")
+    ap.add_argument("--workload", choices=["trace", "served"], default="trace")
+    ap.add_argument("--log-rows", type=int, default=20)
+    ap.add_argument("--cols", type=int, default=64)
+    ap.add_argument("--log-blowup", type=int, default=2)
+    ap.add_argument("--queries", type=int, default=128)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    return ap.parse_args()
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+# ------------------------------------------------------------- clocks -----
+class Clocks:
+    """nvidia-smi sampling during the timed region (reads only)."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device_index: int) -> None:
+        self.dev = device_index
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        fd, self.path = tempfile.mkstemp(prefix="clocks_", suffix=".csv")
+        os.close(fd)
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.dev), f"--query-gpu={self.FIELDS}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except (FileNotFoundError, OSError):
+            self.proc = None
+        return self
+
+    def stop(self) -> dict:
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        rows = []
+        for line in open(self.path):
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) >= 9:
+                rows.append(parts)
+        os.unlink(self.path)
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"], "samples": 0}
+
+        def num(x):
+            try:
+                return float(x)
+            except ValueError:
+                return None
+
+        sm = [num(r[1]) for r in rows if num(r[1]) is not None]
+        mx = [num(r[2]) for r in rows if num(r[2]) is not None]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in rows for i in range(4) if r[5 + i].lower() == "active"})
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": max(mx) if mx else None, "reasons": reasons,
+                "samples": len(rows),
+                "power_w_max": max((num(r[3]) or 0) for r in rows)}
+
+
+# ------------------------------------------------------- CPU baseline -----
+def cpu_trace_sample(log_rows, cols, log_blowup, queries, threads=0, reps=1):
+    """The oracle (C restatement, OpenMP) on a bounded slice of the trace
+    workload: encode + row-leaf Merkle commit + openings."""
+    from oracle import oracle as orc
+
+    if threads:
+        orc.set_threads(threads)
+    rng = np.random.default_rng(7)
+    x = rng.integers(0, P, size=(cols, 1 << log_rows), dtype=np.uint64).astype(np.uint32)
+    p2 = orc.Poseidon2.babybear16()
+    shift = orc.to_mont(0, np.array([31], np.uint32))[0]
+    idx = rng.integers(0, 1 << (log_rows + log_blowup), size=queries).astype(np.int32)
+    best = None
+    for _ in range(reps):
+        t0 = time.perf_counter()
+        xm = orc.to_mont(0, x)
+        cw = orc.rs_encode(0, xm, log_blowup, int(shift))
+        layers = orc.merkle_commit_columns(p2, cw)
+        orc.merkle_open(cw, cw.shape[1], cols, 1, cw.shape[1], layers, idx)
+        dt = time.perf_counter() - t0
+        best = dt if best is None else min(best, dt)
+    return (cols << log_rows) / best, best, orc.threads()
+
+
+# ---------------------------------------------------------- workloads -----
+def trace_workload(args, device):
+    import torch
+
+    from zorch_gb300.coding import ReedSolomon
+    from zorch_gb300.commit import MerkleTree, Poseidon2
+    from zorch_gb300.field import BABYBEAR, to_mont
+    from zorch_gb300.pcs import BasefoldProver
+
+    rows, cols = 1 << args.log_rows, args.cols
+    perm = Poseidon2.builtin(BABYBEAR)
+    code = ReedSolomon(rows, 1 << args.log_blowup, BABYBEAR, coset_shift=31, generator=31)
+    prover = BasefoldProver(code, MerkleTree(perm, column_major=True), args.queries)
+    rng = np.random.default_rng(20240601)
+    host = rng.integers(0, P, size=(cols, rows), dtype=np.uint64).astype(np.uint32).view(np.int32)
+    pinned = torch.from_numpy(host).pin_memory()
+    canon = pinned.to(device)
+    xm = torch.empty_like(canon)
+    n = rows << args.log_blowup
+    idx = torch.from_numpy(rng.integers(0, n, size=args.queries).astype(np.int32)).to(device)
+    stream = torch.cuda.current_stream()
+    ev = {}
+
+    def step(e2e=False, timing=None):
+        src = canon
+        if e2e:
+            src = pinned.to(device, non_blocking=True)
+        if timing is not None:
+            timing[0].record(stream)
+        to_mont(BABYBEAR, src, xm)
+        cw = code.encode(xm)
+        if timing is not None:
+            timing[1].record(stream)
+        K, nn = cw.shape
+        from zorch_gb300.commit import leaves_layout
+
+        root, layers = prover.tree.commit_layout(leaves_layout(cw, nn, K, 1, nn), device)
+        if timing is not None:
+            timing[2].record(stream)
+        op = prover.tree.open_layout(leaves_layout(cw, nn, K, 1, nn), layers, idx, K)
+        if e2e:
+            out = torch.cat([root.reshape(-1), op.row.reshape(-1), op.path.reshape(-1)])
+            host_out = out.cpu()
+            return host_out.numel() * 4
+        return 0
+
+    info = {
+        "elements": cols * rows,
+        "h2d_bytes": cols * rows * 4,
+        "d2h_bytes": 4 * (8 + args.queries * cols + (args.log_rows + args.log_blowup) * args.queries * 8),
+        "config": {"workload": f"trace commit {rows}x{cols}, blowup {1 << args.log_blowup}, "
+                               f"row leaves, {args.queries} query openings",
+                   "rows": rows, "cols": cols, "blowup": 1 << args.log_blowup,
+                   "queries": args.queries, "field": "babybear", "hash": "poseidon2-16 (built-in)",
+                   "l2": "inputs larger than L2 (256 MiB in, 1 GiB LDE)"},
+        "leaves": n, "perms_leaf": n * ((cols + 7) // 8), "perms_node": n - 1,
+        "ntt_bytes": 4 * cols * rows + 4 * cols * n,
+    }
+    return step, info
+
+
+def main():
+    args = parse()
+    rank, world, local = dist_env()
+    if args.impl == "reference":
+        return reference_arm(args, rank, world)
+
+    import torch
+
+    torch.cuda.set_device(local)
+    device = torch.device("cuda", local)
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl", device_id=device)
+    from zorch_gb300 import _lib
+
+    _lib.check(_lib.lib().zc_init(local), "init")
+    step, info = trace_workload(args, device)
+    stream = torch.cuda.current_stream()
+
+    for _ in range(max(args.warmup, 3)):
+        step()
+    torch.cuda.synchronize()
+
+    def barrier():
+        if world > 1:
+            import torch.distributed as dist
+
+            dist.barrier()
+
+    # ---- device-resident timed region
+    marks = [[torch.cuda.Event(enable_timing=True) for _ in range(3)] for _ in range(args.steps)]
+    clocks = Clocks(local).start()
+    launches0 = _lib.lib().zc_launch_count()
+    barrier()
+    torch.cuda.synchronize()
+    t_start = torch.cuda.Event(enable_timing=True)
+    t_end = torch.cuda.Event(enable_timing=True)
+    t_start.record(stream)
+    for k in range(args.steps):
+        step(timing=marks[k])
+    t_end.record(stream)
+    torch.cuda.synchronize()
+    barrier()
+    clk = clocks.stop()
+    launches = _lib.lib().zc_launch_count() - launches0
+    ms = t_start.elapsed_time(t_end)
+    ms_max = ms
+    if world > 1:
+        import torch.distributed as dist
+
+        tt = torch.tensor([ms], device=device)
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        ms_max = float(tt.item())
+    ntt_ms = sum(m[0].elapsed_time(m[1]) for m in marks) / args.steps
+    hash_ms = sum(m[1].elapsed_time(m[2]) for m in marks) / args.steps
+
+    # ---- end-to-end through the public API from pinned host memory
+    for _ in range(2):
+        step(e2e=True)
+    torch.cuda.synchronize()
+    barrier()
+    e0 = time.perf_counter()
+    for _ in range(args.steps):
+        step(e2e=True)
+    torch.cuda.synchronize()
+    e2e_s = time.perf_counter() - e0
+    if world > 1:
+        import torch.distributed as dist
+
+        tt = torch.tensor([e2e_s], device=device)
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        e2e_s = float(tt.item())
+
+    elems_total = info["elements"] * args.steps * world
+    value = elems_total / (ms_max / 1e3)
+    e2e_value = elems_total / e2e_s
+
+    peaks = {}
+    try:
+        peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+    except (OSError, ValueError):
+        pass
+    hbm_peak = float(peaks.get("hbm_gbs", 6800.0))
+    sm_mhz = float(peaks.get("sm_max_mhz", 2070.0))
+    # Hash kernel (dominant): integer instructions executed per Poseidon2
+    # permutation of the built-in BabyBear-16 instance, from the ncu capture
+    # summarised in profiles/ (thread-level SASS instructions).
+    inst_per_perm = float(os.environ.get("ZC_INST_PER_PERM", "7200"))
+    perms = info["perms_leaf"] + info["perms_node"]
+    int_peak = 152 * 128 * sm_mhz * 1e6 / 1e9  # Ginst/s: 152 SMs x 128 lanes x clock
+    achieved = perms * inst_per_perm / (hash_ms / 1e3) / 1e9
+    out = {
+        "metric": METRIC,
+        "value": value,
+        "unit": "elem/s",
+        "n_gpus": world,
+        "steps": args.steps,
+        "warmup": max(args.warmup, 3),
+        "ms_per_step": ms_max / args.steps,
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "u32 (BabyBear, Montgomery)",
+        "data": "synthetic: seeded uniform [0, p) canonical BabyBear elements",
+        "config": info["config"] | {"parallelism": f"replicas x{world}"},
+        "e2e": {"value": e2e_value, "unit": "elem/s", "h2d_bytes_per_step": info["h2d_bytes"],
+                "d2h_bytes_per_step": info["d2h_bytes"]},
+        "roofline": {"bound": "int32", "kernel": "merkle leaf/subtree Poseidon2 (k_subtree)",
+                     "achieved": achieved, "peak": int_peak, "unit": "Ginst/s",
+                     "frac": achieved / int_peak, "traffic": None,
+                     "peak_source": "152 SMs x 128 INT32 lanes x sm_max_mhz (MEASURED_PEAKS.json)",
+                     "ms": hash_ms, "perms": perms},
+        "roofline_ntt": {"bound": "hbm", "kernel": "coset LDE (k_lde_pass1+pass2)",
+                         "achieved": info["ntt_bytes"] / (ntt_ms / 1e3) / 1e9, "peak": hbm_peak,
+                         "unit": "GB/s", "frac": info["ntt_bytes"] / (ntt_ms / 1e3) / 1e9 / hbm_peak,
+                         "ms": ntt_ms, "peak_source": "MEASURED_PEAKS.json hbm_gbs (of measured)"},
+        "clocks": clk,
+        "gpu_launches": int(launches),
+    }
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        v, secs, thr = cpu_trace_sample(16, args.cols, args.log_blowup, args.queries, reps=1)
+        out["cpu_baseline"] = {"value": v, "unit": "elem/s", "cores": thr, "kind": "port",
+                               "sample": f"oracle C restatement, 2^16 x {args.cols} slice of the "
+                                         f"trace workload ({secs:.2f} s)"}
+    if rank == 0:
+        print(json.dumps(out), flush=True)
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.destroy_process_group()
+
+
+def reference_arm(args, rank, world):
+    """The reference algorithm's CPU path (oracle restatement, all host
+    threads) on bounded samples of the same workload; rank 0 only."""
+    if rank != 0:
+        return
+    log_rows = 16
+    for _ in range(max(args.warmup, 1)):
+        cpu_trace_sample(12, args.cols, args.log_blowup, args.queries)
+    vals, secs = [], 0.0
+    for _ in range(args.steps):
+        v, s, thr = cpu_trace_sample(log_rows, args.cols, args.log_blowup, args.queries)
+        vals.append(v)
+        secs += s
+    value = len(vals) * (args.cols << log_rows) / secs
+    out = {
+        "impl": "reference",
+        "metric": METRIC,
+        "value": value,
+        "unit": "elem/s",
+        "n_gpus": world,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": secs / len(vals) * 1e3,
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "u32 (BabyBear, Montgomery)",
+        "data": "synthetic: seeded uniform [0, p) canonical BabyBear elements",
+        "config": {"workload": f"trace commit 2^{log_rows}x{args.cols} slice, blowup "
+                               f"{1 << args.log_blowup}, row leaves, {args.queries} openings"},
+        "cpu_baseline": {"value": value, "unit": "elem/s", "cores": thr, "kind": "port",
+                         "sample": f"2^{log_rows} x {args.cols} per step; the reference is Python "
+                                   "over FRX/hash-frx wheels absent here, so its C restatement "
+                                   "(oracle/) runs instead"},
+        "e2e": {"value": value, "unit": "elem/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(out), flush=True)
+
+
+if __name__ == "__main__":
+    main()

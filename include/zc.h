@@ -65,6 +65,8 @@ typedef struct zc_poseidon2 zc_poseidon2;
 const char* zc_status_str(zc_status s);
 const char* zc_last_error(void);
 int zc_version(void);
+/* Kernels this library has launched in the process so far (all devices). */
+unsigned long long zc_launch_count(void);
 
 /* Build per-device constant tables. Called implicitly on first use; call it
  * explicitly before any CUDA-graph capture. */

@@ -44,6 +44,7 @@ def _declare(lib: C.CDLL) -> None:
         "zc_status_str": (C.c_char_p, [st]),
         "zc_last_error": (C.c_char_p, []),
         "zc_version": (C.c_int, []),
+        "zc_launch_count": (C.c_ulonglong, []),
         "zc_init": (st, [C.c_int]),
         "zc_to_mont": (st, [st, vp, vp, i64, vp]),
         "zc_from_mont": (st, [st, vp, vp, i64, vp]),

@@ -3,6 +3,7 @@
 #include <stdio.h>
 #include <string.h>
 
+#include <atomic>
 #include <mutex>
 
 #include "internal.cuh"
@@ -21,7 +22,10 @@ zc_status cuda_fail(cudaError_t e) {
   return ZC_CUDA_ERR;
 }
 
+static std::atomic<unsigned long long> g_launches{0};
+
 zc_status launch_check() {
+  g_launches.fetch_add(1, std::memory_order_relaxed);
   cudaError_t e = cudaGetLastError();
   return e == cudaSuccess ? ZC_OK : cuda_fail(e);
 }
@@ -190,6 +194,7 @@ const char* zc_status_str(zc_status s) {
 }
 
 const char* zc_last_error(void) { return g_err; }
+unsigned long long zc_launch_count(void) { return g_launches.load(); }
 int zc_version(void) { return 1; }
 
 zc_status zc_init(int device) {
