@@ -1,13 +1,13 @@
-// Merkle commit (fused per-subtree leaf hash + compression), openings, and
-// the FRI fold -- plain, and fused with the hashing of the next layer.
+// Merkle commit, openings, and the FRI fold -- plain, and fused with the
+// hashing of the next layer.
 //
-// One CTA owns a subtree of T = blockDim.x leaves: each thread hashes one leaf
-// (or compresses one child pair), writes the digest to its level in HBM and
-// keeps it in shared memory; the CTA then compresses in shared memory up to its
-// subtree root, writing every level (the tree keeps all layers for openings,
-// zorch/commit/merkle.py:187-202) without reading any level back from HBM.
-// Levels above the subtree roots run as further launches of the same kernel
-// fed by the stored level (NodeLeaf), log2(256)+1 levels per launch.
+// Large trees: one thread per leaf (k_leaf, no barriers, full occupancy) writes
+// the leaf digests; each level with more than 2^15 nodes is one launch of one
+// thread per parent. The small top of a tree, and whole small trees, run as
+// fused CTA subtrees (k_subtree): T = blockDim.x threads hash T leaves (or
+// compress T child pairs), keep the digests in shared memory and compress up to
+// the subtree root, writing every level (the tree keeps all layers for
+// openings, zorch/commit/merkle.py:187-202) without reading a level back.
 #include "internal.cuh"
 
 namespace zc {
@@ -175,6 +175,25 @@ __global__ void __launch_bounds__(kMaxT) k_subtree(Leaf leaf, uint32_t* layers, 
   }
 }
 
+// One thread per leaf (or per parent for NodeLeaf): no shared memory, no
+// barriers, so every warp stays busy for the whole launch.
+template <class K, class Leaf>
+__global__ void __launch_bounds__(kMaxT) k_leaf(Leaf leaf, uint32_t* out, int64_t count,
+                                                const P2Params* rt) {
+  __shared__ P2Params s_rt;
+  K k = KIn<K>::make(rt, &s_rt);
+  const int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= count) return;
+  uint32_t d[8];
+  leaf.digest(p, d, k);
+  store_digest(out + 8 * p, d);
+}
+
+// Levels with more than this many nodes run one thread per node (k_leaf with
+// NodeLeaf, fully occupied); the small top of the tree runs as fused CTA
+// subtrees (k_subtree with NodeLeaf), log2(T)+1 levels per launch.
+constexpr int64_t kLevelWiseMin = 1 << 15;
+
 // Launches the levels above `l_done` (all levels <= l_done already stored).
 template <class K>
 zc_status finish_tree(uint32_t* layers, int64_t L, int l_done, const P2Params* rt,
@@ -183,8 +202,15 @@ zc_status finish_tree(uint32_t* layers, int64_t L, int l_done, const P2Params* r
   int l = l_done;
   while (l < depth) {
     const int64_t parents = (L >> l) >> 1;
-    const int T = parents < kMaxT ? (int)parents : kMaxT;
     NodeLeaf nl{layers + 8 * level_offset(L, l)};
+    if (parents > kLevelWiseMin) {
+      k_leaf<K, NodeLeaf><<<(unsigned)((parents + kMaxT - 1) / kMaxT), kMaxT, 0, st>>>(
+          nl, layers + 8 * level_offset(L, l + 1), parents, rt);
+      ZC_TRY(launch_check());
+      l += 1;
+      continue;
+    }
+    const int T = parents < kMaxT ? (int)parents : kMaxT;
     k_subtree<K, NodeLeaf><<<(unsigned)(parents / T), T, 0, st>>>(nl, layers, L, l + 1, rt);
     ZC_TRY(launch_check());
     l += 1 + ilog2(T);
@@ -195,6 +221,11 @@ zc_status finish_tree(uint32_t* layers, int64_t L, int l_done, const P2Params* r
 template <class K, class Leaf>
 zc_status commit_tree(const Leaf& leaf, uint32_t* layers, int64_t L, const P2Params* rt,
                       cudaStream_t st) {
+  if (L > kLevelWiseMin) {
+    k_leaf<K, Leaf><<<(unsigned)((L + kMaxT - 1) / kMaxT), kMaxT, 0, st>>>(leaf, layers, L, rt);
+    ZC_TRY(launch_check());
+    return finish_tree<K>(layers, L, 0, rt, st);
+  }
   const int T0 = L < kMaxT ? (int)L : kMaxT;
   k_subtree<K, Leaf><<<(unsigned)(L / T0), T0, 0, st>>>(leaf, layers, L, 0, rt);
   ZC_TRY(launch_check());
