@@ -63,6 +63,18 @@ def dist_env():
     return rank, world, local
 
 
+def max_over_ranks(x: float, device=None) -> float:
+    """The slowest rank's time (replicas: every rank times the same work)."""
+    import torch
+    import torch.distributed as dist
+
+    if not dist.is_available() or not dist.is_initialized() or dist.get_world_size() == 1:
+        return x
+    t = torch.tensor([x], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
 # ------------------------------------------------------------- clocks -----
 class Clocks:
     """nvidia-smi sampling during the timed region (reads only)."""
@@ -254,13 +266,7 @@ def main():
     clk = clocks.stop()
     launches = _lib.lib().zc_launch_count() - launches0
     ms = t_start.elapsed_time(t_end)
-    ms_max = ms
-    if world > 1:
-        import torch.distributed as dist
-
-        tt = torch.tensor([ms], device=device)
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        ms_max = float(tt.item())
+    ms_max = max_over_ranks(ms, device)
     ntt_ms = sum(m[0].elapsed_time(m[1]) for m in marks) / args.steps
     hash_ms = sum(m[1].elapsed_time(m[2]) for m in marks) / args.steps
 
@@ -273,13 +279,7 @@ def main():
     for _ in range(args.steps):
         step(e2e=True)
     torch.cuda.synchronize()
-    e2e_s = time.perf_counter() - e0
-    if world > 1:
-        import torch.distributed as dist
-
-        tt = torch.tensor([e2e_s], device=device)
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        e2e_s = float(tt.item())
+    e2e_s = max_over_ranks(time.perf_counter() - e0, device)
 
     elems_total = info["elements"] * args.steps * world
     value = elems_total / (ms_max / 1e3)

@@ -109,6 +109,27 @@ zc_status zc_rs_encode(zc_field field, const uint32_t* coeffs, int64_t batch, in
                        uint32_t* out, void* workspace, size_t workspace_bytes,
                        void* stream);
 
+/* Batched LDE: many jobs (matrices of different heights, widths, blowups) in
+ * two persistent launches over a (job, tile) work list -- the batched form of
+ * the one-call-per-matrix encode of zorch/pcs/basefold/prover.py:437-447.
+ * tile_log selects the shared-memory tile (2^tile_log words; 0 = default),
+ * the knob the autotuner sets per (log_n, width) bucket. The workspace holds
+ * the four-step intermediates (jobs are split into waves that fit) and must be
+ * 256-byte aligned. */
+typedef struct {
+  const uint32_t* coeffs; /* [batch, 2^log_k] */
+  uint32_t* out;          /* [batch, 2^(log_k+log_blowup)] */
+  int64_t batch;
+  int32_t log_k;
+  int32_t log_blowup;
+  uint32_t shift_mont;    /* 0: no coset */
+  int32_t tile_log;       /* 0: default */
+} zc_lde_job;
+size_t zc_rs_encode_batch_workspace_bytes(const zc_lde_job* jobs, int32_t njobs);
+zc_status zc_rs_encode_batch(zc_field field, const zc_lde_job* jobs, int32_t njobs,
+                             uint32_t generator, void* workspace, size_t workspace_bytes,
+                             void* stream);
+
 /* ---- Merkle trees (arity 2) ------------------------------------------- */
 /* Replaces MerkleTree.commit = hash_leaves + fold_digests
  * (zorch/commit/merkle.py:118-202) over PaddingFreeSponge<16,8,8> leaves and
@@ -124,6 +145,17 @@ zc_status zc_merkle_commit(const zc_poseidon2* p, zc_leaves leaves, uint32_t* la
 zc_status zc_merkle_open(zc_leaves leaves, const uint32_t* layers, const int32_t* idx,
                          int32_t q, uint32_t* rows, uint32_t* paths, uint32_t* oob_flag,
                          void* stream);
+
+/* Batched commit of many trees (the per-matrix MerkleTree.commit calls of a
+ * batch, zorch/commit/merkle.py:118-202) in 1 + (max depth - 8) + 1 launches.
+ * workspace: >= 256 bytes, 256-byte aligned (per-launch work counters). */
+typedef struct {
+  zc_leaves leaves;
+  uint32_t* layers; /* (2L-1)*8 words */
+} zc_merkle_job;
+zc_status zc_merkle_commit_batch(const zc_poseidon2* p, const zc_merkle_job* jobs,
+                                 int32_t njobs, void* workspace, size_t workspace_bytes,
+                                 void* stream);
 
 /* ---- FRI fold ---------------------------------------------------------- */
 /* Replaces ReedSolomon.fold -> fri_fold -> fri_fold_values
@@ -143,6 +175,17 @@ zc_status zc_fri_fold_commit(const zc_poseidon2* p, const uint32_t* cw, int64_t 
                              const uint32_t* beta, int ef_beta, uint32_t shift_mont,
                              uint32_t generator, uint32_t* out, uint32_t* next_layers,
                              void* stream);
+
+/* out[j] = sum_c alpha^c * cw[c][j] over w base columns of n words (EF4
+ * alpha, device): batches a committed matrix's columns into one EF4 codeword
+ * for its fold rounds, the role of batch_staggered in the Basefold batch open
+ * (zorch/pcs/basefold/batching.py:38-78), here with powers of one challenge.
+ * out: [n, 4], 16-byte aligned; w <= 4096. */
+zc_status zc_rlc_columns(zc_field field, const uint32_t* cw, int64_t n, int32_t w,
+                         const uint32_t* alpha, uint32_t* out, void* stream);
+/* Synthetic benchmark data (no reference counterpart): out[i] =
+ * SplitMix64(seed * 0x100000001B3 + i) mod p, canonical form. */
+zc_status zc_fill_uniform(zc_field field, uint32_t* out, int64_t n, uint64_t seed, void* stream);
 
 /* ---- Fiat-Shamir duplex (rate 8, width 16) ----------------------------- */
 /* One observe-then-sample hop in the reference's host-FS FFI contract

@@ -62,7 +62,8 @@ def _load() -> C.CDLL:
         "orc_duplex_init": (None, [vp]),
         "orc_duplex_observe": (None, [vp, vp, _u32p, i64]),
         "orc_duplex_sample": (None, [vp, vp, i32, _u32p]),
-        "orc_fri_commit_phase": (i32, [vp, i32, _u32p, i32, u32, u32, i32, i32, i32, vp,
+        "orc_rlc_columns": (None, [i32, _u32p, i64, i32, _u32p, _u32p]),
+        "orc_fri_commit_phase": (i32, [vp, i32, _u32p, i32, i32, u32, u32, i32, i32, i32, vp,
                                        _u32p, _u32p, _u32p, _i32p, _u32p, _u32p]),
     }
     for name, (res, args) in sig.items():
@@ -302,8 +303,16 @@ class CommitPhaseProof:
         return b"".join(np.ascontiguousarray(x, dtype="<u4").tobytes() for x in parts)
 
 
-def layer_limbs(num_rounds: int, beta_limbs: int) -> list[int]:
-    limbs = [1]
+def rlc_columns(field: int, cw, alpha) -> np.ndarray:
+    cw = u32(cw)
+    w, n = cw.shape
+    out = np.zeros((n, 4), np.uint32)
+    LIB.orc_rlc_columns(field, cw.reshape(-1), n, w, u32(alpha), out.reshape(-1))
+    return out
+
+
+def layer_limbs(num_rounds: int, beta_limbs: int, ef_in: bool = False) -> list[int]:
+    limbs = [4 if ef_in else 1]
     for _ in range(num_rounds):
         limbs.append(4 if (limbs[-1] == 4 or beta_limbs == 4) else 1)
     return limbs
@@ -311,10 +320,12 @@ def layer_limbs(num_rounds: int, beta_limbs: int) -> list[int]:
 
 def fri_commit_phase(p2: Poseidon2, field: int, codeword, num_rounds: int, num_queries: int,
                      beta_limbs: int, transcript: Transcript, shift_mont=0, generator=0):
-    cw = u32(codeword).reshape(-1)
-    n0 = cw.size
+    cw = u32(codeword)
+    ef_in = cw.ndim == 2
+    n0 = cw.shape[0]
+    cw = cw.reshape(-1)
     log_n = n0.bit_length() - 1
-    limbs = layer_limbs(num_rounds, beta_limbs)
+    limbs = layer_limbs(num_rounds, beta_limbs, ef_in)
     roots = np.zeros((num_rounds, 8), np.uint32)
     betas = np.zeros((num_rounds, 4), np.uint32)
     nf = n0 >> num_rounds
@@ -325,7 +336,8 @@ def fri_commit_phase(p2: Poseidon2, field: int, codeword, num_rounds: int, num_q
     path_sizes = [d * num_queries * 8 for d in depths]
     rows = np.zeros(max(sum(row_sizes), 1), np.uint32)
     paths = np.zeros(max(sum(path_sizes), 1), np.uint32)
-    rc = LIB.orc_fri_commit_phase(p2.ptr, field, cw, log_n, shift_mont, generator, num_rounds,
+    rc = LIB.orc_fri_commit_phase(p2.ptr, field, cw, log_n, int(ef_in), shift_mont, generator,
+                                  num_rounds,
                                   num_queries, beta_limbs, C.byref(transcript.st), roots.reshape(-1),
                                   betas.reshape(-1), final.reshape(-1), pos, rows, paths)
     if rc:

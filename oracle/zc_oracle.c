@@ -492,6 +492,29 @@ int orc_fri_fold(int field, const uint32_t* cw, int64_t n, int ef_in, const uint
   return 0;
 }
 
+/* out[j] = sum_c alpha^c * cw[c][j]: the columns of a committed matrix
+ * combined into one EF4 codeword with powers of one EF4 challenge. */
+void orc_rlc_columns(int field, const uint32_t* cw, int64_t n, int w, const uint32_t* alpha,
+                     uint32_t* out) {
+  const fld* F = FLD(field);
+  uint32_t* pw = (uint32_t*)malloc(sizeof(uint32_t) * 4 * (size_t)(w > 0 ? w : 1));
+  uint32_t acc[4] = {F->one, 0, 0, 0};
+  for (int c = 0; c < w; c++) {
+    memcpy(pw + 4 * c, acc, 16);
+    uint32_t nx[4];
+    ef4_mul(F, acc, alpha, nx);
+    memcpy(acc, nx, 16);
+  }
+#pragma omp parallel for num_threads(orc_get_threads()) schedule(static)
+  for (int64_t j = 0; j < n; j++) {
+    uint32_t r[4] = {0, 0, 0, 0};
+    for (int c = 0; c < w; c++)
+      for (int e = 0; e < 4; e++) r[e] = fadd(F, r[e], fmul(F, pw[4 * c + e], cw[(int64_t)c * n + j]));
+    memcpy(out + 4 * j, r, 16);
+  }
+  free(pw);
+}
+
 /* ----------------------------------------------------------- transcript ---- */
 /* DuplexTranscript (zorch/transcript.py:239-481), width 16, rate 8. */
 void orc_duplex_init(orc_duplex* t) { memset(t, 0, sizeof(*t)); }
@@ -556,7 +579,7 @@ void orc_duplex_sample(const orc_p2* P, orc_duplex* t, int n, uint32_t* out) {
  * (zorch/pcs/fri/prover.py:151-187).
  * rows: per layer [Q][2*limbs_i]; paths: per layer [depth_i][Q][8]. */
 int orc_fri_commit_phase(const orc_p2* P, int field, const uint32_t* codeword, int log_n,
-                         uint32_t shift_mont, uint32_t generator, int num_rounds,
+                         int ef_in, uint32_t shift_mont, uint32_t generator, int num_rounds,
                          int num_queries, int beta_limbs, orc_duplex* t, uint32_t* roots,
                          uint32_t* betas, uint32_t* final_layer, int32_t* positions,
                          uint32_t* rows, uint32_t* paths) {
@@ -564,11 +587,11 @@ int orc_fri_commit_phase(const orc_p2* P, int field, const uint32_t* codeword, i
   if (num_rounds < 0 || num_rounds >= log_n) return 1;
   const int64_t n0 = (int64_t)1 << log_n;
   uint32_t** cws = (uint32_t**)calloc((size_t)num_rounds + 1, sizeof(uint32_t*));
-  uint32_t** lays = (uint32_t**)calloc((size_t)num_rounds, sizeof(uint32_t*));
+  uint32_t** lays = (uint32_t**)calloc((size_t)num_rounds + 1, sizeof(uint32_t*));
   int* limbs = (int*)calloc((size_t)num_rounds + 1, sizeof(int));
-  cws[0] = (uint32_t*)malloc(sizeof(uint32_t) * (size_t)n0);
-  memcpy(cws[0], codeword, sizeof(uint32_t) * (size_t)n0);
-  limbs[0] = 1;
+  limbs[0] = ef_in ? 4 : 1;
+  cws[0] = (uint32_t*)malloc(sizeof(uint32_t) * (size_t)n0 * limbs[0]);
+  memcpy(cws[0], codeword, sizeof(uint32_t) * (size_t)n0 * limbs[0]);
   uint32_t shift = shift_mont ? shift_mont : F->one;
   for (int r = 0; r < num_rounds; r++) {
     const int64_t n = n0 >> r, L = n / 2;

@@ -104,8 +104,10 @@ void orc_duplex_observe(const orc_p2* p, orc_duplex* t, const uint32_t* v, int64
 void orc_duplex_sample(const orc_p2* p, orc_duplex* t, int n, uint32_t* out);
 
 /* FRI / Basefold commit phase (pre-fold pair commit rounds, then queries). */
+void orc_rlc_columns(int field, const uint32_t* cw, int64_t n, int w, const uint32_t* alpha,
+                     uint32_t* out);
 int orc_fri_commit_phase(const orc_p2* p, int field, const uint32_t* codeword,
-                         int log_n, uint32_t shift_mont, uint32_t generator,
+                         int log_n, int ef_in, uint32_t shift_mont, uint32_t generator,
                          int num_rounds, int num_queries, int beta_limbs,
                          orc_duplex* t, uint32_t* roots, uint32_t* betas,
                          uint32_t* final_layer, int32_t* positions,

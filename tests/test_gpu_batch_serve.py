@@ -1,0 +1,180 @@
+"""Batched and served paths: identical bytes to the per-matrix path and to the
+oracle, whatever the batch composition (integer work: exact equality)."""
+
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+torch = pytest.importorskip("torch")
+pytestmark = pytest.mark.gpu
+
+from zorch_gb300 import _lib  # noqa: E402
+from zorch_gb300.field import BABYBEAR, to_host  # noqa: E402
+
+SHAPES = [  # (width, log_h, log_blowup)
+    (1, 12, 1), (3, 10, 2), (64, 13, 2), (5, 15, 1), (17, 9, 3), (2, 16, 2), (128, 12, 3),
+    (1, 17, 1), (9, 14, 2), (4, 4, 1), (1, 0, 1),
+]
+
+
+@pytest.fixture(scope="module", autouse=True)
+def _cuda():
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    _lib.check(_lib.lib().zc_init(0), "init")
+
+
+def _mats(seed=0):
+    from zorch_gb300.field import ptr, stream_handle
+
+    out = []
+    for i, (w, lh, lb) in enumerate(SHAPES):
+        x = torch.empty((w, 1 << lh), dtype=torch.int32, device="cuda")
+        _lib.check(_lib.lib().zc_fill_uniform(0, ptr(x), x.numel(), 1000 * seed + i,
+                                              stream_handle()), "fill")
+        from zorch_gb300.field import to_mont
+
+        out.append((to_mont(BABYBEAR, x), lb))
+    return out
+
+
+@pytest.mark.parametrize("tile", [0, 13, 15])
+def test_batched_encode_equals_per_matrix(tile):
+    from zorch_gb300.batch import BatchCommitter, MatrixJob
+    from zorch_gb300.coding import rs_encode
+
+    mats = _mats(1)
+    bc = BatchCommitter(tile_override=tile)
+    outs = bc.encode([MatrixJob(x, lb) for x, lb in mats])
+    for (x, lb), o in zip(mats, outs):
+        want = rs_encode(BABYBEAR, x, lb, BABYBEAR.mont(31), 0)
+        assert torch.equal(o, want)
+
+
+def test_batched_encode_small_workspace_waves():
+    """A workspace that fits only one intermediate at a time forces waves and
+    the chunked single-job path; the bytes do not change."""
+    from zorch_gb300.batch import BatchCommitter, MatrixJob
+    from zorch_gb300.coding import rs_encode
+
+    mats = _mats(2)
+    bc = BatchCommitter()
+    ws = torch.empty((1 << 17) // 4 + 64, dtype=torch.int32, device="cuda")
+    outs = bc.encode([MatrixJob(x, lb) for x, lb in mats], workspace=ws)
+    for (x, lb), o in zip(mats, outs):
+        assert torch.equal(o, rs_encode(BABYBEAR, x, lb, BABYBEAR.mont(31), 0))
+
+
+def test_batched_merkle_equals_per_matrix_and_oracle(orc):
+    from zorch_gb300.batch import BatchCommitter, MatrixJob
+    from zorch_gb300.commit import MerkleTree
+
+    mats = _mats(3)
+    bc = BatchCommitter()
+    committed = bc.commit([MatrixJob(x, lb) for x, lb in mats])
+    tree = MerkleTree(bc.perm, column_major=True)
+    p2 = orc.Poseidon2.babybear16()
+    for c in committed:
+        root, layers = tree.commit(c.codeword)
+        assert torch.equal(c.layers.flat, layers.flat)
+        if c.codeword.numel() <= (1 << 16):
+            want = orc.merkle_commit_columns(p2, to_host(c.codeword))
+            assert np.array_equal(to_host(c.root), want[-1][0])
+
+
+def test_graphed_batch_replay():
+    from zorch_gb300.batch import BatchCommitter, GraphedBatch, MatrixJob
+
+    mats = _mats(4)
+    bc = BatchCommitter()
+    g = GraphedBatch(bc, [(x.shape[0], x.shape[1], lb) for x, lb in mats])
+    for seed in (5, 6):
+        mats = _mats(seed)
+        got = g.replay([x for x, _ in mats])
+        want = bc.commit([MatrixJob(x, lb) for x, lb in mats])
+        for a, b in zip(got, want):
+            assert torch.equal(a.codeword, b.codeword)
+            assert torch.equal(a.layers.flat, b.layers.flat)
+
+
+def test_autotuner_choice_keeps_bytes(tmp_path):
+    from zorch_gb300.batch import Autotuner, BatchCommitter, MatrixJob
+
+    tuner = Autotuner(tmp_path / "tune.json")
+    tl = tuner.tune(14, 8, 2)
+    assert tl in (13, 14, 15)
+    tuner.save()
+    assert Autotuner(tmp_path / "tune.json").tile_log(16, 8) == tl
+    mats = _mats(7)
+    a = BatchCommitter(tuner=tuner).commit([MatrixJob(x, lb) for x, lb in mats])
+    b = BatchCommitter().commit([MatrixJob(x, lb) for x, lb in mats])
+    for x, y in zip(a, b):
+        assert torch.equal(x.layers.flat, y.layers.flat)
+
+
+def _small_stream(seed, n=10):
+    from zorch_gb300.serve import fill_request, make_stream
+
+    reqs = make_stream(n, seed, rate_hz=0.0, log_h=(9, 13), log_w=(0.0, 4.0), fold_frac=0.5)
+    for r in reqs:
+        fill_request(r)
+    torch.cuda.synchronize()
+    return reqs
+
+
+def test_served_results_same_alone_and_in_the_mix():
+    from zorch_gb300.serve import Server
+
+    reqs = _small_stream(11)
+    mixed = Server(max_batch=6, streams=2).run(reqs)
+    assert [r.rid for r in mixed] == [r.rid for r in reqs]
+    for r, m in zip(reqs, mixed):
+        alone = Server(max_batch=1, streams=1).run([r])[0]
+        assert alone.proof == m.proof and len(m.proof) > 32
+
+
+def test_served_fold_proofs_match_oracle(orc):
+    """Root of the row-leaf tree and the fold-and-open proof bytes of a served
+    request equal the oracle's, replayed from the same seeded data."""
+    from zorch_gb300.serve import FOLD_FINAL_LOG, FOLD_QUERIES, Server
+
+    reqs = [r for r in _small_stream(12, 8) if r.fold][:2]
+    res = Server().run(reqs)
+    p2 = orc.Poseidon2.babybear16()
+    for r, got in zip(reqs, res):
+        x = orc.to_mont(0, to_host(r.resident))
+        cw = orc.rs_encode(0, x, r.log_blowup, BABYBEAR.mont(31))
+        layers = orc.merkle_commit_columns(p2, cw)
+        root = layers[-1][0]
+        words = np.frombuffer(got.proof, dtype=np.uint32)
+        assert np.array_equal(words[:8], root)
+        t = orc.Transcript(p2)
+        t.observe(root)
+        alpha = t.sample(4)
+        rlc = orc.rlc_columns(0, cw, alpha)
+        rounds = r.log_h + r.log_blowup - FOLD_FINAL_LOG
+        proof = orc.fri_commit_phase(p2, 0, rlc, rounds, FOLD_QUERIES, 4, t, BABYBEAR.mont(31))
+        n = cw.shape[1]
+        rows, paths = orc.merkle_open(cw, n, cw.shape[0], 1, n, layers, proof.positions)
+        parts = [root, proof.roots.reshape(-1), proof.final_layer.reshape(-1),
+                 proof.positions.astype(np.uint32), rows.reshape(-1), paths.reshape(-1)]
+        for rr, pp in zip(proof.rows, proof.paths):
+            parts += [rr.reshape(-1), pp.reshape(-1)]
+        assert np.array_equal(words, np.concatenate(parts))
+
+
+def test_plain_path_per_polynomial_roots(orc):
+    from zorch_gb300.serve import run_plain
+
+    reqs = [r for r in _small_stream(13, 6)][:3]
+    res = run_plain(reqs)
+    p2 = orc.Poseidon2.babybear16()
+    for r, got in zip(reqs, res):
+        x = orc.to_mont(0, to_host(r.resident))
+        words = np.frombuffer(got.proof, dtype=np.uint32)
+        for c in range(r.width):
+            cw = orc.rs_encode(0, x[c], r.log_blowup, BABYBEAR.mont(31))
+            L = cw.size // 2
+            root = orc.merkle_commit(p2, cw, L, 2, 1, L)[-1][0]
+            assert np.array_equal(words[8 * c: 8 * c + 8], root)

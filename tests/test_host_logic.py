@@ -1,0 +1,77 @@
+"""Host-side logic that needs no GPU: admission under the HBM budget, the
+config-5 request stream, and the replicas' max-over-ranks timing on two gloo
+ranks."""
+
+from __future__ import annotations
+
+import os
+from collections import deque
+
+import pytest
+
+
+def test_stream_is_seeded_and_shaped():
+    from zorch_gb300.serve import make_stream
+
+    a = make_stream(200, 5, rate_hz=10.0)
+    b = make_stream(200, 5, rate_hz=10.0)
+    assert [(r.log_h, r.width, r.log_blowup, r.fold, r.arrival) for r in a] == \
+        [(r.log_h, r.width, r.log_blowup, r.fold, r.arrival) for r in b]
+    assert all(14 <= r.log_h <= 24 and 1 <= r.width <= 256 and r.log_blowup in (1, 2) for r in a)
+    arr = [r.arrival for r in a]
+    assert arr == sorted(arr) and arr[0] > 0
+    assert 0.15 < sum(r.fold for r in a) / len(a) < 0.45
+
+
+def test_admission_fifo_budget_and_rejection():
+    from zorch_gb300.serve import Request, admit
+
+    def req(i, arrival, log_h, width):
+        return Request(i, arrival, log_h, width, 1, False, i)
+
+    small = req(0, 0.0, 10, 1).footprint()
+    q = deque([req(0, 0.0, 10, 1), req(1, 0.1, 10, 1), req(2, 0.2, 30, 256),
+               req(3, 0.3, 10, 1), req(4, 5.0, 10, 1)])
+    # budget for two small requests: FIFO up to the budget; a request larger than
+    # the whole budget can never fit, so it is rejected rather than blocking the queue
+    ready, rej, used = admit(q, 1.0, 0, 2 * small, 8)
+    assert [r.rid for r in ready] == [0, 1] and used == 2 * small
+    assert [r.rid for r in rej] == [2] and q[0].rid == 3
+    # memory freed: the next arrived request is admitted
+    ready, rej, used = admit(q, 1.0, 0, 2 * small, 8)
+    assert not rej and [r.rid for r in ready] == [3]
+    # not yet arrived
+    ready, rej, used = admit(q, 1.0, 0, 1e18, 8)
+    assert not ready and [r.rid for r in q] == [4]
+    # max_batch caps one admission
+    q = deque([req(i, 0.0, 10, 1) for i in range(10)])
+    ready, _, _ = admit(q, 0.0, 0, 1e18, 3)
+    assert len(ready) == 3 and len(q) == 7
+
+
+def _worker(rank, world, port, out):
+    import torch.distributed as dist
+
+    os.environ.update(MASTER_ADDR="127.0.0.1", MASTER_PORT=str(port))
+    dist.init_process_group("gloo", rank=rank, world_size=world)
+    import bench
+
+    out[rank] = bench.max_over_ranks(1.0 + rank, device="cpu")
+    dist.destroy_process_group()
+
+
+def test_max_over_ranks_gloo_two_ranks():
+    mp = pytest.importorskip("torch.multiprocessing")
+    import random
+
+    ctx = mp.get_context("spawn")
+    mgr = ctx.Manager()
+    out = mgr.dict()
+    port = random.randint(20000, 40000)
+    procs = [ctx.Process(target=_worker, args=(r, 2, port, out)) for r in range(2)]
+    for p in procs:
+        p.start()
+    for p in procs:
+        p.join(120)
+        assert p.exitcode == 0
+    assert dict(out) == {0: 2.0, 1: 2.0}

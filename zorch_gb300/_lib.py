@@ -26,11 +26,21 @@ class ZcError(RuntimeError):
         self.status = status
 
 
+class LdeJob(C.Structure):
+    _fields_ = [("coeffs", C.c_void_p), ("out", C.c_void_p), ("batch", C.c_int64),
+                ("log_k", C.c_int32), ("log_blowup", C.c_int32), ("shift_mont", C.c_uint32),
+                ("tile_log", C.c_int32)]
+
+
 class Leaves(C.Structure):
     """zc_leaves: leaf p = concat_q base[q*group_stride + p*group_len ...]."""
 
     _fields_ = [("base", C.c_void_p), ("num_leaves", C.c_int64), ("groups", C.c_int32),
                 ("group_len", C.c_int32), ("group_stride", C.c_int64)]
+
+
+class MerkleJob(C.Structure):
+    _fields_ = [("leaves", Leaves), ("layers", C.c_void_p)]
 
 
 _lock = threading.Lock()
@@ -62,6 +72,11 @@ def _declare(lib: C.CDLL) -> None:
         "zc_duplex_hop": (st, [vp, vp, vp, vp, vp, vp, vp, i64, i32, vp, vp, vp, vp, vp, vp, vp]),
         "zc_duplex_hop_host": (st, [vp, vp, vp, vp, vp, vp, vp, i64, i32, vp, vp, vp, vp, vp, vp]),
         "zc_duplex_step": (st, [vp, vp, vp, i64, i32, vp, vp, i64, vp]),
+        "zc_rlc_columns": (st, [st, vp, i64, i32, vp, vp, vp]),
+        "zc_fill_uniform": (st, [st, vp, i64, C.c_uint64, vp]),
+        "zc_rs_encode_batch_workspace_bytes": (sz, [vp, i32]),
+        "zc_rs_encode_batch": (st, [st, vp, i32, u32, vp, sz, vp]),
+        "zc_merkle_commit_batch": (st, [vp, vp, i32, vp, sz, vp]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(lib, name)

@@ -1,0 +1,212 @@
+"""Batched matrix commits: many polynomial matrices per launch.
+
+`BatchCommitter.commit(jobs)` runs the coset LDE of every matrix in two
+persistent launches over a (matrix, NTT tile) work list (zc_rs_encode_batch)
+and all their row-leaf Merkle trees in 1 + (max depth - 8) + 1 launches over
+(matrix, subtree chunk) work lists (zc_merkle_commit_batch). Each matrix gets
+exactly the root a per-matrix BasefoldProver.commit would produce
+(zorch/pcs/basefold/prover.py:437-455): batching changes launches, never bytes.
+
+`GraphedBatch` captures one batch composition into a CUDA graph and replays
+it on new inputs of the same shapes. `Autotuner` picks the LDE shared-memory
+tile per (log_n, width) bucket by timing candidates and caches the choice.
+"""
+
+from __future__ import annotations
+
+import ctypes as C
+import json
+import os
+from dataclasses import dataclass
+from pathlib import Path
+
+import torch
+
+from . import _lib
+from .commit import DigestLayers, Poseidon2
+from .field import BABYBEAR, field_of, ptr, stream_handle
+
+_TILE_CANDIDATES = (13, 14, 15)
+
+
+@dataclass
+class MatrixJob:
+    """One matrix to commit: columns [w, h] (Montgomery), blowup 2^log_blowup,
+    coset shift (canonical) or None."""
+
+    columns: torch.Tensor
+    log_blowup: int
+    shift: int | None = 31
+
+    @property
+    def width(self) -> int:
+        return self.columns.shape[0]
+
+    @property
+    def height(self) -> int:
+        return self.columns.shape[1]
+
+    @property
+    def log_n(self) -> int:
+        return (self.height << self.log_blowup).bit_length() - 1
+
+
+@dataclass
+class CommittedMatrix:
+    codeword: torch.Tensor        # [w, n] column-major LDE (leaves are its rows)
+    layers: DigestLayers
+
+    @property
+    def root(self) -> torch.Tensor:
+        return self.layers.root
+
+
+def _bucket(log_n: int, width: int) -> str:
+    return f"{log_n}:{max(width, 1).bit_length() - 1}"
+
+
+class Autotuner:
+    """Per-(log_n, log2 width) choice of the LDE shared-memory tile, measured
+    with CUDA events on synthetic data and cached in a JSON file."""
+
+    def __init__(self, path: str | os.PathLike | None = None) -> None:
+        default = Path(__file__).resolve().parent / "_build" / "autotune.json"
+        self.path = Path(path or os.environ.get("ZC_AUTOTUNE_CACHE", default))
+        self.table: dict[str, int] = {}
+        if self.path.exists():
+            try:
+                self.table = json.loads(self.path.read_text())
+            except ValueError:
+                self.table = {}
+
+    def tile_log(self, log_n: int, width: int) -> int:
+        return int(self.table.get(_bucket(log_n, width), 0))
+
+    def save(self) -> None:
+        self.path.parent.mkdir(parents=True, exist_ok=True)
+        self.path.write_text(json.dumps(self.table, indent=1, sort_keys=True))
+
+    def tune(self, log_h: int, width: int, log_blowup: int, field=BABYBEAR, reps: int = 3) -> int:
+        """Time every candidate tile on a [width, 2^log_h] matrix; record the best."""
+        f = field_of(field)
+        cols = torch.empty((width, 1 << log_h), dtype=torch.int32, device="cuda")
+        _lib.check(_lib.lib().zc_fill_uniform(f.id, ptr(cols), cols.numel(), 7, stream_handle()),
+                   "fill")
+        best, best_ms = 0, float("inf")
+        for tl in _TILE_CANDIDATES:
+            bc = BatchCommitter(field=f, tuner=None, tile_override=tl)
+            job = MatrixJob(cols, log_blowup)
+            try:
+                bc.encode([job])
+            except (NotImplementedError, ValueError):
+                continue
+            torch.cuda.synchronize()
+            s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            s.record()
+            for _ in range(reps):
+                bc.encode([job])
+            e.record()
+            torch.cuda.synchronize()
+            ms = s.elapsed_time(e) / reps
+            if ms < best_ms:
+                best, best_ms = tl, ms
+        self.table[_bucket(log_h + log_blowup, width)] = best
+        return best
+
+
+class BatchCommitter:
+    def __init__(self, perm: Poseidon2 | None = None, field=BABYBEAR, generator: int | None = None,
+                 tuner: Autotuner | None = None, tile_override: int = 0) -> None:
+        self.field = field_of(field)
+        self.perm = perm if perm is not None else Poseidon2.builtin(self.field)
+        self.generator = generator or 0
+        self.tuner = tuner
+        self.tile_override = tile_override
+
+    # -- LDE -----------------------------------------------------------------
+    def _lde_jobs(self, jobs: list[MatrixJob], outs: list[torch.Tensor]):
+        arr = (_lib.LdeJob * len(jobs))()
+        for i, (j, o) in enumerate(zip(jobs, outs)):
+            h = j.height
+            tl = self.tile_override or (self.tuner.tile_log(j.log_n, j.width) if self.tuner else 0)
+            arr[i] = _lib.LdeJob(ptr(j.columns), ptr(o), j.width, h.bit_length() - 1,
+                                 j.log_blowup, self.field.mont(j.shift) if j.shift else 0, tl)
+        return arr
+
+    def encode(self, jobs: list[MatrixJob], outs: list[torch.Tensor] | None = None,
+               workspace: torch.Tensor | None = None) -> list[torch.Tensor]:
+        for j in jobs:
+            h = j.height
+            if h & (h - 1) or h == 0:
+                raise ValueError(f"message_len must be a power of two, got {h}")
+        if outs is None:
+            outs = [torch.empty((j.width, j.height << j.log_blowup), dtype=torch.int32,
+                                device=j.columns.device) for j in jobs]
+        arr = self._lde_jobs(jobs, outs)
+        L = _lib.lib()
+        need = L.zc_rs_encode_batch_workspace_bytes(arr, len(jobs))
+        if workspace is None or workspace.numel() * 4 < need:
+            workspace = torch.empty((need + 3) // 4, dtype=torch.int32, device=jobs[0].columns.device)
+        _lib.check(L.zc_rs_encode_batch(self.field.id, arr, len(jobs), self.generator,
+                                        ptr(workspace), workspace.numel() * 4, stream_handle()),
+                   "rs_encode_batch")
+        return outs
+
+    # -- Merkle ----------------------------------------------------------------
+    def merkle(self, codewords: list[torch.Tensor], flats: list[torch.Tensor] | None = None,
+               counters: torch.Tensor | None = None) -> list[DigestLayers]:
+        if flats is None:
+            flats = [torch.empty((2 * cw.shape[1] - 1, 8), dtype=torch.int32, device=cw.device)
+                     for cw in codewords]
+        arr = (_lib.MerkleJob * len(codewords))()
+        for i, (cw, fl) in enumerate(zip(codewords, flats)):
+            w, n = cw.shape
+            arr[i] = _lib.MerkleJob(_lib.Leaves(ptr(cw), n, w, 1, n), ptr(fl))
+        if counters is None:
+            counters = torch.empty(64, dtype=torch.int32, device=codewords[0].device)
+        _lib.check(_lib.lib().zc_merkle_commit_batch(self.perm.handle, arr, len(codewords),
+                                                     ptr(counters), counters.numel() * 4,
+                                                     stream_handle()), "merkle_commit_batch")
+        return [DigestLayers(fl, cw.shape[1]) for fl, cw in zip(flats, codewords)]
+
+    def commit(self, jobs: list[MatrixJob]) -> list[CommittedMatrix]:
+        cws = self.encode(jobs)
+        layers = self.merkle(cws)
+        return [CommittedMatrix(c, l) for c, l in zip(cws, layers)]
+
+
+class GraphedBatch:
+    """A batch composition captured once into a CUDA graph: inputs are copied
+    into static buffers, the graph replays the batched LDE + Merkle launches."""
+
+    def __init__(self, committer: BatchCommitter, shapes: list[tuple[int, int, int]],
+                 device="cuda") -> None:
+        self.bc = committer
+        self.inputs = [torch.zeros((w, h), dtype=torch.int32, device=device) for w, h, _ in shapes]
+        self.jobs = [MatrixJob(x, lb) for x, (_, _, lb) in zip(self.inputs, shapes)]
+        self.outs = [torch.empty((w, h << lb), dtype=torch.int32, device=device)
+                     for w, h, lb in shapes]
+        self.flats = [torch.empty((2 * (h << lb) - 1, 8), dtype=torch.int32, device=device)
+                      for w, h, lb in shapes]
+        arr = committer._lde_jobs(self.jobs, self.outs)
+        need = _lib.lib().zc_rs_encode_batch_workspace_bytes(arr, len(self.jobs))
+        self.ws = torch.empty((need + 3) // 4, dtype=torch.int32, device=device)
+        self.ctr = torch.empty(64, dtype=torch.int32, device=device)
+        # warm up once outside capture (sets kernel attributes), then capture
+        self._run()
+        torch.cuda.synchronize()
+        self.graph = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(self.graph):
+            self._run()
+        self.layers = [DigestLayers(fl, o.shape[1]) for fl, o in zip(self.flats, self.outs)]
+
+    def _run(self) -> None:
+        self.bc.encode(self.jobs, self.outs, self.ws)
+        self.bc.merkle(self.outs, self.flats, self.ctr)
+
+    def replay(self, inputs: list[torch.Tensor] | None = None) -> list[CommittedMatrix]:
+        if inputs is not None:
+            for dst, src in zip(self.inputs, inputs):
+                dst.copy_(src, non_blocking=True)
+        self.graph.replay()
+        return [CommittedMatrix(o, l) for o, l in zip(self.outs, self.layers)]

@@ -8,6 +8,8 @@
 // compress T child pairs), keep the digests in shared memory and compress up to
 // the subtree root, writing every level (the tree keeps all layers for
 // openings, zorch/commit/merkle.py:187-202) without reading a level back.
+#include <string.h>
+
 #include "internal.cuh"
 
 namespace zc {
@@ -312,6 +314,205 @@ zc_status fold_commit_launch(const uint32_t* cw, int64_t n, const uint32_t* beta
   return commit_tree<K>(leaf, layers, n >> 2, rt, st);
 }
 
+// ------------------------------------------------------------ batched ----
+// Many trees (leaf layouts of different widths and heights) per launch: a leaf
+// launch over (tree, 256-leaf chunk) items, one launch per level over
+// (tree, 256-parent chunk) items for every tree that still has a wide level,
+// and one top launch with one CTA per tree compressing its last <= 256 nodes
+// to the root in shared memory. The tree table is a __grid_constant__ kernel
+// parameter; CTAs claim items from an atomic counter (dynamic balance across
+// cheap 1-element and expensive 128-element leaves).
+constexpr int kMaxTreeJobs = 48;
+constexpr int kTopLog = 8;
+
+struct TreeJobDev {
+  const uint32_t* base;
+  uint32_t* layers;
+  int64_t L;
+  int64_t gs;
+  int32_t G, g;
+  int32_t depth, top;
+};
+
+struct TreeBatch {
+  int32_t njobs;
+  int32_t level;  // level phase: the level being produced
+  int64_t total;
+  int64_t prefix[kMaxTreeJobs + 1];
+  TreeJobDev job[kMaxTreeJobs];
+};
+
+__device__ __forceinline__ int find_tree(const int64_t* prefix, int njobs, int64_t it) {
+  int lo = 0, hi = njobs - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (prefix[mid] <= it) lo = mid;
+    else hi = mid - 1;
+  }
+  return lo;
+}
+
+// LEVEL = 0: leaf chunks; LEVEL = 1: parent chunks of B.level.
+template <class K, int LEVEL>
+__global__ void __launch_bounds__(kMaxT) k_tree_batch(const __grid_constant__ TreeBatch B,
+                                                      unsigned long long* counter,
+                                                      const P2Params* rt) {
+  __shared__ P2Params s_rt;
+  __shared__ long long s_item;
+  K k = KIn<K>::make(rt, &s_rt);
+  for (;;) {
+    if (threadIdx.x == 0) s_item = (long long)atomicAdd(counter, 1ull);
+    __syncthreads();
+    const int64_t it = s_item;
+    __syncthreads();
+    if (it >= B.total) break;
+    const int j = find_tree(B.prefix, B.njobs, it);
+    const TreeJobDev& J = B.job[j];
+    const int64_t p = (it - B.prefix[j]) * kMaxT + threadIdx.x;
+    uint32_t d[8];
+    if (LEVEL == 0) {
+      if (p < J.L) {
+        LayoutLeaf leaf{J.base, J.G, J.g, J.gs};
+        leaf.digest(p, d, k);
+        store_digest(J.layers + 8 * p, d);
+      }
+    } else {
+      const int l = B.level;
+      if (p < (J.L >> l)) {
+        NodeLeaf nl{J.layers + 8 * level_offset(J.L, l - 1)};
+        nl.digest(p, d, k);
+        store_digest(J.layers + 8 * (level_offset(J.L, l) + p), d);
+      }
+    }
+  }
+}
+
+// One CTA per tree: level `top` (<= 256 nodes, already stored) to the root.
+template <class K>
+__global__ void __launch_bounds__(kMaxT) k_tree_top(const __grid_constant__ TreeBatch B,
+                                                    const P2Params* rt) {
+  __shared__ P2Params s_rt;
+  __shared__ uint32_t sm[8 * kMaxT];
+  K k = KIn<K>::make(rt, &s_rt);
+  const TreeJobDev& J = B.job[blockIdx.x];
+  int lvl = J.top;
+  int width = (int)(J.L >> lvl);
+  const uint32_t* src = J.layers + 8 * level_offset(J.L, lvl);
+  for (int i = threadIdx.x; i < width * 8; i += blockDim.x) sm[(i & 7) * kMaxT + (i >> 3)] = src[i];
+  const int t = threadIdx.x;
+  while (width > 1) {
+    __syncthreads();
+    width >>= 1;
+    lvl++;
+    uint32_t a[8], b[8], d[8];
+    if (t < width) {
+#pragma unroll
+      for (int i = 0; i < 8; i++) {
+        a[i] = sm[i * kMaxT + 2 * t];
+        b[i] = sm[i * kMaxT + 2 * t + 1];
+      }
+    }
+    __syncthreads();
+    if (t < width) {
+      p2_compress(a, b, d, k);
+      store_digest(J.layers + 8 * (level_offset(J.L, lvl) + t), d);
+#pragma unroll
+      for (int i = 0; i < 8; i++) sm[i * kMaxT + t] = d[i];
+    }
+  }
+}
+
+template <class K>
+zc_status tree_batch_wave(const zc_merkle_job* jobs, int n, unsigned long long* ctr,
+                          const P2Params* rt, cudaStream_t st) {
+  TreeBatch B;
+  memset(&B, 0, sizeof(B));
+  B.njobs = n;
+  int max_top = 0;
+  for (int i = 0; i < n; i++) {
+    TreeJobDev& d = B.job[i];
+    d.base = jobs[i].leaves.base;
+    d.layers = jobs[i].layers;
+    d.L = jobs[i].leaves.num_leaves;
+    d.gs = jobs[i].leaves.group_stride;
+    d.G = jobs[i].leaves.groups;
+    d.g = jobs[i].leaves.group_len;
+    d.depth = ilog2(d.L);
+    d.top = d.depth > kTopLog ? d.depth - kTopLog : 0;
+    max_top = d.top > max_top ? d.top : max_top;
+  }
+  int dev = 0, sms = 0;
+  ZC_CUDA(cudaGetDevice(&dev));
+  ZC_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+  ZC_CUDA(cudaMemsetAsync(ctr, 0, sizeof(unsigned long long) * (max_top + 1), st));
+  int occ = 0;
+  ZC_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_tree_batch<K, 0>, kMaxT, 0));
+  if (occ < 1) occ = 1;
+  for (int l = 0; l <= max_top; l++) {
+    int64_t tot = 0;
+    for (int i = 0; i < n; i++) {
+      B.prefix[i] = tot;
+      if (l == 0 || l <= B.job[i].top) tot += ((B.job[i].L >> l) + kMaxT - 1) / kMaxT;
+    }
+    B.prefix[n] = tot;
+    B.total = tot;
+    B.level = l;
+    if (tot == 0) continue;
+    int64_t grid = (int64_t)occ * sms;
+    if (grid > tot) grid = tot;
+    if (l == 0)
+      k_tree_batch<K, 0><<<(unsigned)grid, kMaxT, 0, st>>>(B, ctr + l, rt);
+    else
+      k_tree_batch<K, 1><<<(unsigned)grid, kMaxT, 0, st>>>(B, ctr + l, rt);
+    ZC_TRY(launch_check());
+  }
+  k_tree_top<K><<<n, kMaxT / 2, 0, st>>>(B, rt);
+  return launch_check();
+}
+
+// out[j] = sum_c alpha^c * cw[c][j] (EF4 alpha on the device, base columns):
+// the columns of a committed matrix batched into one EF4 codeword before its
+// fold rounds. Powers of alpha are staged in shared memory per block.
+template <class F>
+__global__ void k_rlc(const uint32_t* cw, int64_t n, int w, const uint32_t* alpha,
+                      uint32_t* out) {
+  extern __shared__ uint32_t pw[];  // w x 4
+  if (threadIdx.x == 0) {
+    ef4 a{{alpha[0], alpha[1], alpha[2], alpha[3]}};
+    ef4 acc{{F::ONE, 0u, 0u, 0u}};
+    for (int c = 0; c < w; c++) {
+      for (int e = 0; e < 4; e++) pw[4 * c + e] = acc.c[e];
+      acc = ef_mul<F>(acc, a);
+    }
+  }
+  __syncthreads();
+  for (int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; j < n;
+       j += (int64_t)gridDim.x * blockDim.x) {
+    uint32_t r[4] = {0, 0, 0, 0};
+    for (int c = 0; c < w; c++) {
+      const uint32_t x = __ldg(cw + (int64_t)c * n + j);
+#pragma unroll
+      for (int e = 0; e < 4; e++) r[e] = madd<F>(r[e], mmul<F>(pw[4 * c + e], x));
+    }
+    uint4 o = make_uint4(r[0], r[1], r[2], r[3]);
+    reinterpret_cast<uint4*>(out)[j] = o;
+  }
+}
+
+// Seeded synthetic field data: SplitMix64(seed, index) reduced mod p.
+__host__ __device__ __forceinline__ uint64_t splitmix64(uint64_t x) {
+  x += 0x9E3779B97F4A7C15ull;
+  x = (x ^ (x >> 30)) * 0xBF58476D1CE4E5B9ull;
+  x = (x ^ (x >> 27)) * 0x94D049BB133111EBull;
+  return x ^ (x >> 31);
+}
+
+__global__ void k_fill_uniform(uint32_t* out, int64_t n, uint64_t seed, uint32_t p) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x)
+    out[i] = (uint32_t)(splitmix64(seed * 0x100000001B3ull + (uint64_t)i) % p);
+}
+
 }  // namespace zc
 
 using namespace zc;
@@ -385,6 +586,57 @@ zc_status zc_fri_fold_commit(const zc_poseidon2* p, const uint32_t* cw, int64_t 
       return fold_commit_launch<K, 1, 4>(cw, n, beta, shift_mont, generator, out, next_layers, rt, st);
     return fold_commit_launch<K, 1, 1>(cw, n, beta, shift_mont, generator, out, next_layers, rt, st);
   });
+}
+
+zc_status zc_merkle_commit_batch(const zc_poseidon2* p, const zc_merkle_job* jobs,
+                                 int32_t njobs, void* workspace, size_t workspace_bytes,
+                                 void* stream) {
+  if (njobs < 0 || (njobs > 0 && !jobs) || !workspace || workspace_bytes < 256) return ZC_BAD_ARG;
+  if ((uintptr_t)workspace % 256) return ZC_BAD_ARG;
+  for (int i = 0; i < njobs; i++) {
+    const zc_merkle_job& j = jobs[i];
+    if (!j.layers || (uintptr_t)j.layers % 16) return ZC_BAD_ARG;
+    if (!is_pow2(j.leaves.num_leaves)) return ZC_NOT_POW2;
+    if (j.leaves.groups < 0 || j.leaves.group_len < 0 ||
+        (!j.leaves.base && j.leaves.groups * j.leaves.group_len > 0))
+      return ZC_BAD_ARG;
+    if (ilog2(j.leaves.num_leaves) - kTopLog + 1 > 30) return ZC_BAD_SHAPE;
+  }
+  cudaStream_t st = (cudaStream_t)stream;
+  unsigned long long* ctr = (unsigned long long*)workspace;
+  return with_perm(p, [&](auto k, const P2Params* rt) -> zc_status {
+    using K = decltype(k);
+    for (int i = 0; i < njobs; i += kMaxTreeJobs) {
+      const int n = njobs - i < kMaxTreeJobs ? njobs - i : kMaxTreeJobs;
+      ZC_TRY(tree_batch_wave<K>(jobs + i, n, ctr, rt, st));
+    }
+    return ZC_OK;
+  });
+}
+
+zc_status zc_rlc_columns(zc_field field, const uint32_t* cw, int64_t n, int32_t w,
+                         const uint32_t* alpha, uint32_t* out, void* stream) {
+  if (!cw || !alpha || !out || n < 0 || w < 1 || w > 4096) return ZC_BAD_ARG;
+  if ((uintptr_t)out % 16) return ZC_BAD_ARG;
+  if (n == 0) return ZC_OK;
+  cudaStream_t st = (cudaStream_t)stream;
+  return with_field(field, [&](auto f) {
+    using F = decltype(f);
+    int64_t blocks = (n + 255) / 256;
+    if (blocks > 152 * 8) blocks = 152 * 8;
+    k_rlc<F><<<(unsigned)blocks, 256, (size_t)w * 16, st>>>(cw, n, w, alpha, out);
+    return launch_check();
+  });
+}
+
+zc_status zc_fill_uniform(zc_field field, uint32_t* out, int64_t n, uint64_t seed, void* stream) {
+  if (!out || n < 0) return ZC_BAD_ARG;
+  if (n == 0) return ZC_OK;
+  const uint32_t p = field == ZC_FIELD_BABYBEAR ? BabyBear::P : KoalaBear::P;
+  int64_t blocks = (n + 255) / 256;
+  if (blocks > 152 * 16) blocks = 152 * 16;
+  k_fill_uniform<<<(unsigned)blocks, 256, 0, (cudaStream_t)stream>>>(out, n, seed, p);
+  return launch_check();
 }
 
 }  // extern "C"

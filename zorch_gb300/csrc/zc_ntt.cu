@@ -16,6 +16,8 @@
 // In shared memory the transform is an iterative radix-2 DIT whose input is
 // stored bit-reversed as it is loaded (the bit reversal folded into the load),
 // processed 4 stages per register pass (16 elements per thread).
+#include <string.h>
+
 #include "internal.cuh"
 
 namespace zc {
@@ -135,16 +137,15 @@ __device__ void smem_ntt(uint32_t* a, int rows, int logm, int rs, const uint32_t
 
 constexpr int kThreads = 512;
 
+// One column, all b cosets (single pass). `sm` is the block's dynamic smem.
 template <class F>
-__global__ void __launch_bounds__(kThreads) k_lde_small(const uint32_t* x, uint32_t* out,
-                                                        int log_k, int log_b, uint32_t h) {
-  extern __shared__ uint32_t sm[];
+__device__ void lde_small_body(const uint32_t* x, uint32_t* out, int log_k, int log_b,
+                               uint32_t h, int64_t c, uint32_t* sm) {
   const int k = 1 << log_k, b = 1 << log_b, log_n = log_k + log_b;
   const int rs = padded(k);
   uint32_t* work = sm;
   uint32_t* tw = work + b * rs;
   uint32_t* hp = tw + (k > 1 ? k / 2 : 1);
-  const int64_t c = blockIdx.x;
   const uint32_t* xc = x + (c << log_k);
   pow_table<F>(tw, k > 1 ? k / 2 : 1, log_k ? omega_pow<F>(log_k, 1) : F::ONE);
   pow_table<F>(hp, k, h);
@@ -163,12 +164,18 @@ __global__ void __launch_bounds__(kThreads) k_lde_small(const uint32_t* x, uint3
   }
 }
 
-// Pass 1: grid (coset s, i1 tile, column). z layout per column: [b][k2][k1].
 template <class F>
-__global__ void __launch_bounds__(kThreads) k_lde_pass1(const uint32_t* x, uint32_t* z, int log_k1,
-                                                        int log_k2, int log_b, int log_ti,
-                                                        uint32_t h) {
+__global__ void __launch_bounds__(kThreads) k_lde_small(const uint32_t* x, uint32_t* out,
+                                                        int log_k, int log_b, uint32_t h) {
   extern __shared__ uint32_t sm[];
+  lde_small_body<F>(x, out, log_k, log_b, h, blockIdx.x, sm);
+}
+
+// Pass 1 item (coset s, i1 tile, column c). z layout per column: [b][k2][k1].
+template <class F>
+__device__ void lde_pass1_body(const uint32_t* x, uint32_t* z, int log_k1, int log_k2, int log_b,
+                               int log_ti, uint32_t h, int s, int tile, int64_t c,
+                               uint32_t* sm) {
   const int k1 = 1 << log_k1, k2 = 1 << log_k2, TI = 1 << log_ti;
   const int log_k = log_k1 + log_k2, log_n = log_k + log_b;
   const int rs = padded(k2);
@@ -176,9 +183,7 @@ __global__ void __launch_bounds__(kThreads) k_lde_pass1(const uint32_t* x, uint3
   uint32_t* tw = work + TI * rs;
   uint32_t* R = tw + (k2 > 1 ? k2 / 2 : 1);
   uint32_t* gi = R + k2;
-  const int s = blockIdx.x;
-  const int i1_0 = blockIdx.y * TI;
-  const int64_t c = blockIdx.z;
+  const int i1_0 = tile * TI;
   const uint32_t gs = mmul<F>(h, s ? omega_pow<F>(log_n, (uint32_t)s) : F::ONE);
   const uint32_t G = mpow<F>(gs, (uint64_t)k1);
   pow_table<F>(tw, k2 > 1 ? k2 / 2 : 1, log_k2 ? omega_pow<F>(log_k2, 1) : F::ONE);
@@ -203,20 +208,26 @@ __global__ void __launch_bounds__(kThreads) k_lde_pass1(const uint32_t* x, uint3
   }
 }
 
-// Pass 2: grid (t2 tile, column); all b cosets of TT rows per CTA.
 template <class F>
-__global__ void __launch_bounds__(kThreads) k_lde_pass2(const uint32_t* z, uint32_t* out,
-                                                        int log_k1, int log_k2, int log_b,
-                                                        int log_tt) {
+__global__ void __launch_bounds__(kThreads) k_lde_pass1(const uint32_t* x, uint32_t* z, int log_k1,
+                                                        int log_k2, int log_b, int log_ti,
+                                                        uint32_t h) {
   extern __shared__ uint32_t sm[];
+  lde_pass1_body<F>(x, z, log_k1, log_k2, log_b, log_ti, h, blockIdx.x, blockIdx.y, blockIdx.z,
+                    sm);
+}
+
+// Pass 2 item (t2 tile, column c): all b cosets of TT rows.
+template <class F>
+__device__ void lde_pass2_body(const uint32_t* z, uint32_t* out, int log_k1, int log_k2,
+                               int log_b, int log_tt, int tile, int64_t c, uint32_t* sm) {
   const int k1 = 1 << log_k1, TT = 1 << log_tt, b = 1 << log_b;
   const int log_k = log_k1 + log_k2, log_n = log_k + log_b;
   const int rows = b * TT;
   const int rs = padded(k1);
   uint32_t* work = sm;
   uint32_t* tw = work + rows * rs;
-  const int t2_0 = blockIdx.x * TT;
-  const int64_t c = blockIdx.y;
+  const int t2_0 = tile * TT;
   pow_table<F>(tw, k1 > 1 ? k1 / 2 : 1, log_k1 ? omega_pow<F>(log_k1, 1) : F::ONE);
   const uint32_t* zc_ = z + (c << log_n);
   for (int idx = threadIdx.x; idx < (rows << log_k1); idx += blockDim.x) {
@@ -236,6 +247,14 @@ __global__ void __launch_bounds__(kThreads) k_lde_pass2(const uint32_t* z, uint3
   }
 }
 
+template <class F>
+__global__ void __launch_bounds__(kThreads) k_lde_pass2(const uint32_t* z, uint32_t* out,
+                                                        int log_k1, int log_k2, int log_b,
+                                                        int log_tt) {
+  extern __shared__ uint32_t sm[];
+  lde_pass2_body<F>(z, out, log_k1, log_k2, log_b, log_tt, blockIdx.x, blockIdx.y, sm);
+}
+
 struct LdePlan {
   bool small;
   int log_k1, log_k2, log_ti, log_tt;
@@ -246,19 +265,20 @@ constexpr int kSmallMaxLogK = 12;
 constexpr int kSmallMaxLogN = 14;
 constexpr int kTileLog = 14;  // elements per shared-memory tile (2^14 = 64 KB)
 
-inline LdePlan plan_lde(int log_k, int log_b) {
+inline LdePlan plan_lde(int log_k, int log_b, int tile_log = 0) {
   LdePlan p{};
   const int k = 1 << log_k, b = 1 << log_b;
+  const int tl = tile_log > 0 ? tile_log : kTileLog;
   p.small = log_k <= kSmallMaxLogK && log_k + log_b <= kSmallMaxLogN;
   p.smem_small = 4 * ((size_t)b * padded(k) + (k > 1 ? k / 2 : 1) + k);
   p.log_k2 = log_k / 2;
   p.log_k1 = log_k - p.log_k2;
-  int ti = kTileLog - p.log_k2;
+  int ti = tl - p.log_k2;
   if (p.log_k2 >= 12 && ti < 3) ti = 3;
   if (ti > p.log_k1) ti = p.log_k1;
   if (ti < 0) ti = 0;
   p.log_ti = ti;
-  int tt = kTileLog - p.log_k1 - log_b;
+  int tt = tl - p.log_k1 - log_b;
   if (tt > p.log_k2) tt = p.log_k2;
   if (tt < 0) tt = 0;
   p.log_tt = tt;
@@ -319,6 +339,178 @@ zc_status lde_launch(const uint32_t* x, int64_t batch, int log_k, int log_b, uin
   return ZC_OK;
 }
 
+// ------------------------------------------------------------ batched ----
+// Many LDE jobs (matrices of different heights, widths and blowups) in two
+// launches: phase A runs every single-pass column and every pass-1 tile of
+// every job, phase B every pass-2 tile. The job table is a __grid_constant__
+// kernel parameter; persistent CTAs claim (job, tile) items from an atomic
+// counter in the workspace, so large and small jobs share the machine.
+constexpr int kMaxLdeJobs = 48;
+
+struct LdeJobDev {
+  const uint32_t* x;
+  uint32_t* out;
+  uint32_t* z;
+  int64_t batch;
+  uint32_t h;
+  int8_t log_k, log_b, log_k1, log_k2, log_ti, log_tt, small, pad_;
+};
+
+struct LdeBatch {
+  int32_t njobs;
+  int32_t phase;
+  int64_t total;
+  int64_t prefix[kMaxLdeJobs + 1];
+  LdeJobDev job[kMaxLdeJobs];
+};
+
+__device__ __forceinline__ int find_job(const int64_t* prefix, int njobs, int64_t it) {
+  int lo = 0, hi = njobs - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (prefix[mid] <= it) lo = mid;
+    else hi = mid - 1;
+  }
+  return lo;
+}
+
+template <class F>
+__global__ void __launch_bounds__(kThreads) k_lde_batch(const __grid_constant__ LdeBatch B,
+                                                        unsigned long long* counter) {
+  extern __shared__ uint32_t sm[];
+  __shared__ long long s_item;
+  for (;;) {
+    if (threadIdx.x == 0) s_item = (long long)atomicAdd(counter, 1ull);
+    __syncthreads();
+    const int64_t it = s_item;
+    if (it >= B.total) break;
+    const int j = find_job(B.prefix, B.njobs, it);
+    const LdeJobDev& J = B.job[j];
+    const int64_t local = it - B.prefix[j];
+    if (B.phase == 0 && J.small) {
+      lde_small_body<F>(J.x, J.out, J.log_k, J.log_b, J.h, local, sm);
+    } else if (B.phase == 0) {
+      const int b = 1 << J.log_b;
+      const int64_t per_col = (int64_t)b << (J.log_k1 - J.log_ti);
+      const int64_t c = local / per_col;
+      const int r = (int)(local - c * per_col);
+      lde_pass1_body<F>(J.x, J.z, J.log_k1, J.log_k2, J.log_b, J.log_ti, J.h, r & (b - 1),
+                        r >> J.log_b, c, sm);
+    } else {
+      const int64_t tiles = (int64_t)1 << (J.log_k2 - J.log_tt);
+      const int64_t c = local / tiles;
+      lde_pass2_body<F>(J.z, J.out, J.log_k1, J.log_k2, J.log_b, J.log_tt,
+                        (int)(local - c * tiles), c, sm);
+    }
+    __syncthreads();  // the item's shared memory is free again
+  }
+}
+
+inline size_t job_z_bytes(const zc_lde_job& j) {
+  const LdePlan p = plan_lde(j.log_k, j.log_blowup, j.tile_log);
+  return p.small ? 0 : (((size_t)j.batch * 4) << (j.log_k + j.log_blowup));
+}
+
+constexpr size_t kCounterBytes = 256;
+
+template <class F>
+zc_status lde_batch_wave(const zc_lde_job* jobs, int n, uint32_t* zbase, unsigned long long* ctr,
+                         cudaStream_t st) {
+  LdeBatch B;  // launch parameters (copied into the launch)
+  memset(&B, 0, sizeof(B));
+  B.njobs = n;
+  size_t smem_a = 0, smem_b = 0;
+  uint32_t* z = zbase;
+  int64_t totA = 0, totB = 0;
+  int64_t prefB[kMaxLdeJobs + 1];
+  for (int i = 0; i < n; i++) {
+    const zc_lde_job& j = jobs[i];
+    const LdePlan p = plan_lde(j.log_k, j.log_blowup, j.tile_log);
+    LdeJobDev& d = B.job[i];
+    d.x = j.coeffs;
+    d.out = j.out;
+    d.batch = j.batch;
+    d.h = j.shift_mont ? j.shift_mont : F::ONE;
+    d.log_k = (int8_t)j.log_k;
+    d.log_b = (int8_t)j.log_blowup;
+    d.log_k1 = (int8_t)p.log_k1;
+    d.log_k2 = (int8_t)p.log_k2;
+    d.log_ti = (int8_t)p.log_ti;
+    d.log_tt = (int8_t)p.log_tt;
+    d.small = p.small ? 1 : 0;
+    d.z = p.small ? nullptr : z;
+    if (!p.small) z += ((size_t)j.batch) << (j.log_k + j.log_blowup);
+    B.prefix[i] = totA;
+    prefB[i] = totB;
+    if (p.small) {
+      totA += j.batch;
+      smem_a = smem_a > p.smem_small ? smem_a : p.smem_small;
+    } else {
+      totA += (j.batch << j.log_blowup) << (p.log_k1 - p.log_ti);
+      totB += j.batch << (p.log_k2 - p.log_tt);
+      smem_a = smem_a > p.smem1 ? smem_a : p.smem1;
+      smem_b = smem_b > p.smem2 ? smem_b : p.smem2;
+    }
+  }
+  B.prefix[n] = totA;
+  prefB[n] = totB;
+  int dev = 0, sms = 0;
+  ZC_CUDA(cudaGetDevice(&dev));
+  ZC_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+  ZC_CUDA(cudaMemsetAsync(ctr, 0, 2 * sizeof(unsigned long long), st));
+  for (int phase = 0; phase < 2; phase++) {
+    const int64_t total = phase ? totB : totA;
+    const size_t smem = phase ? smem_b : smem_a;
+    if (total == 0) continue;
+    B.phase = phase;
+    B.total = total;
+    if (phase) memcpy(B.prefix, prefB, sizeof(prefB));
+    ZC_CUDA(cudaFuncSetAttribute(k_lde_batch<F>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)smem));
+    int occ = 0;
+    ZC_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_lde_batch<F>, kThreads, smem));
+    if (occ < 1) occ = 1;
+    int64_t grid = (int64_t)occ * sms;
+    if (grid > total) grid = total;
+    k_lde_batch<F><<<(unsigned)grid, kThreads, smem, st>>>(B, ctr + phase);
+    ZC_TRY(launch_check());
+  }
+  return ZC_OK;
+}
+
+template <class F>
+zc_status lde_batch_launch(const zc_lde_job* jobs, int njobs, void* ws, size_t ws_bytes,
+                           cudaStream_t st) {
+  if ((uintptr_t)ws % 256) return ZC_BAD_ARG;
+  unsigned long long* ctr = (unsigned long long*)ws;
+  uint32_t* zbase = (uint32_t*)((char*)ws + kCounterBytes);
+  const size_t zcap = ws_bytes > kCounterBytes ? ws_bytes - kCounterBytes : 0;
+  int i = 0;
+  while (i < njobs) {
+    // a job whose intermediate alone exceeds the workspace runs chunked, alone
+    const size_t zi = job_z_bytes(jobs[i]);
+    if (zi > zcap) {
+      const zc_lde_job& j = jobs[i];
+      ZC_TRY(lde_launch<F>(j.coeffs, j.batch, j.log_k, j.log_blowup,
+                           j.shift_mont ? j.shift_mont : F::ONE, j.out, zbase, zcap, st));
+      i++;
+      continue;
+    }
+    int n = 0;
+    size_t used = 0;
+    while (i + n < njobs && n < kMaxLdeJobs) {
+      const size_t zb = job_z_bytes(jobs[i + n]);
+      if (zb > zcap) break;
+      if (used + zb > zcap) break;
+      used += zb;
+      n++;
+    }
+    ZC_TRY(lde_batch_wave<F>(jobs + i, n, zbase, ctr, st));
+    i += n;
+  }
+  return ZC_OK;
+}
+
 }  // namespace zc
 
 using namespace zc;
@@ -355,6 +547,45 @@ zc_status zc_rs_encode(zc_field field, const uint32_t* coeffs, int64_t batch, in
     const uint32_t h = shift_mont ? shift_mont : F::ONE;
     return lde_launch<F>(coeffs, batch, log_k, log_blowup, h, out, workspace, workspace_bytes,
                          (cudaStream_t)stream);
+  });
+}
+
+size_t zc_rs_encode_batch_workspace_bytes(const zc_lde_job* jobs, int32_t njobs) {
+  if (!jobs || njobs <= 0) return kCounterBytes;
+  size_t z = 0;
+  for (int i = 0; i < njobs; i++) z += job_z_bytes(jobs[i]);
+  const size_t cap = (size_t)8 << 30;  // waves bound the intermediate at 8 GiB by default
+  size_t biggest = 0;
+  for (int i = 0; i < njobs; i++) {
+    const size_t zi = job_z_bytes(jobs[i]);
+    biggest = zi > biggest ? zi : biggest;
+  }
+  if (z > cap) z = biggest > cap ? biggest : cap;
+  return kCounterBytes + z;
+}
+
+zc_status zc_rs_encode_batch(zc_field field, const zc_lde_job* jobs, int32_t njobs,
+                             uint32_t generator, void* workspace, size_t workspace_bytes,
+                             void* stream) {
+  if (njobs < 0 || (njobs > 0 && !jobs) || !workspace) return ZC_BAD_ARG;
+  if (njobs == 0) return ZC_OK;
+  return with_field(field, [&](auto f) -> zc_status {
+    using F = decltype(f);
+    if (generator != 0 && generator != F::GEN) {
+      set_error("only the field's canonical generator is built");
+      return ZC_UNSUPPORTED;
+    }
+    for (int i = 0; i < njobs; i++) {
+      const zc_lde_job& j = jobs[i];
+      if (!j.coeffs || !j.out || j.batch < 0 || j.log_k < 0 || j.log_blowup < 0) return ZC_BAD_ARG;
+      if (j.log_k + j.log_blowup > F::TWO_ADICITY || j.log_k > 24) return ZC_BAD_SHAPE;
+      const LdePlan p = plan_lde(j.log_k, j.log_blowup, j.tile_log);
+      const size_t cap = 227 * 1024;
+      if ((p.small && p.smem_small > cap) || (!p.small && (p.smem1 > cap || p.smem2 > cap)))
+        return ZC_UNSUPPORTED;
+    }
+    ZC_TRY(ensure_init());
+    return lde_batch_launch<F>(jobs, njobs, workspace, workspace_bytes, (cudaStream_t)stream);
   });
 }
 

@@ -188,11 +188,11 @@ class FriProver:
     def __init__(self, params: FriParams) -> None:
         self.params = params
 
-    def commit_one(self, coeffs: torch.Tensor) -> FriCommittedPoly:
+    def commit_one(self, coeffs: torch.Tensor, out: torch.Tensor | None = None) -> FriCommittedPoly:
         """_commit_one (zorch/pcs/fri/prover.py:141-148): encode, then the
         pair-leaf Merkle commit of the codeword."""
         code, tree = self.params.code, self.params.tree
-        cw = code.encode(coeffs)
+        cw = code.encode(coeffs, out)
         _, layers = tree.commit_layout(pair_layout(cw), cw.device)
         return FriCommittedPoly(coeffs, cw, layers)
 
