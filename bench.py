@@ -53,6 +53,14 @@ def parse():
     ap.add_argument("--log-blowup", type=int, default=2)
     ap.add_argument("--queries", type=int, default=128)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--requests", type=int, default=24)
+    ap.add_argument("--rate", type=float, default=400.0, help="served stream arrivals per second")
+    ap.add_argument("--seed", type=int, default=5)
+    ap.add_argument("--min-log-h", type=int, default=14)
+    ap.add_argument("--max-log-h", type=int, default=24)
+    ap.add_argument("--budget-gb", type=float, default=150.0)
+    ap.add_argument("--max-batch", type=int, default=32)
+    ap.add_argument("--streams", type=int, default=3)
     return ap.parse_args()
 
 
@@ -219,6 +227,44 @@ def trace_workload(args, device):
     return step, info
 
 
+def served_workload(args, device, rank):
+    """Config-5 stream: Poisson arrivals, log2 heights 14..24, widths
+    log-uniform 1..256, blowup 2 or 4, 30% fold-and-open. The same seeded
+    stream is served by the continuous-batching server and by the plain
+    one-call-per-polynomial path."""
+    import torch
+
+    from zorch_gb300.batch import Autotuner
+    from zorch_gb300.serve import Server, fill_request, make_stream, run_plain
+
+    reqs = make_stream(args.requests, args.seed, rate_hz=args.rate, log_h=(args.min_log_h,
+                                                                            args.max_log_h))
+    for r in reqs:
+        fill_request(r, device)
+    torch.cuda.synchronize()
+    server = Server(budget_bytes=args.budget_gb * 1e9, max_batch=args.max_batch,
+                    streams=args.streams, tuner=Autotuner())
+    elements = sum(r.elements for r in reqs)
+
+    def served(host_fed=False):
+        t0 = time.perf_counter()
+        res = server.run(reqs, host_fed=host_fed)
+        torch.cuda.synchronize()
+        return res, time.perf_counter() - t0
+
+    def plain():
+        t0 = time.perf_counter()
+        res = run_plain(reqs, perm=server.perm)
+        torch.cuda.synchronize()
+        return res, time.perf_counter() - t0
+
+    return reqs, served, plain, elements
+
+
+def pct(xs, q):
+    return float(np.percentile(np.asarray(xs), q)) if len(xs) else None
+
+
 def main():
     args = parse()
     rank, world, local = dist_env()
@@ -284,6 +330,60 @@ def main():
     elems_total = info["elements"] * args.steps * world
     value = elems_total / (ms_max / 1e3)
     e2e_value = elems_total / e2e_s
+    served_info = None
+    if args.workload == "served":
+        reqs, served, plain, elements = served_workload(args, device, rank)
+        for _ in range(max(args.warmup, 3)):
+            served()
+        sv_launch0 = _lib.lib().zc_launch_count()
+        clocks = Clocks(local).start()
+        barrier()
+        times, lat = [], []
+        for _ in range(args.steps):
+            res, dt = served()
+            times.append(dt)
+            lat += [r.latency for r in res]
+        barrier()
+        clk = clocks.stop()
+        launches = _lib.lib().zc_launch_count() - sv_launch0
+        sv_s = max_over_ranks(sum(times), device)
+        plain(); torch.cuda.synchronize()  # warm
+        p_res, p_dt = plain()
+        e2e_res, e2e_dt = served(host_fed=False)
+        # host-fed: inputs from pinned host memory, H2D inside the timed region
+        for r in reqs:
+            r.host = r.resident.cpu().pin_memory()
+        torch.cuda.synchronize()
+        served(host_fed=True)
+        h0 = time.perf_counter()
+        h_res, _ = served(host_fed=True)
+        torch.cuda.synchronize()
+        h_dt = max_over_ranks(time.perf_counter() - h0, device)
+        value = elements * args.steps * world / sv_s
+        e2e_value = elements * world / h_dt
+        plain_value = elements / p_dt
+        served_info = {
+            "requests": len(reqs), "elements_per_step": elements,
+            "fold_requests": sum(r.fold for r in reqs),
+            "latency_ms": {"p50": 1e3 * pct(lat, 50), "p99": 1e3 * pct(lat, 99)},
+            "plain": {"value": plain_value, "unit": "elem/s",
+                      "latency_ms": {"p50": 1e3 * pct([r.latency for r in p_res], 50),
+                                     "p99": 1e3 * pct([r.latency for r in p_res], 99)},
+                      "path": "one call per polynomial (FriProver.commit), host sync per call"},
+            "served_over_plain": value / world / plain_value,
+            "bytes_identical_across_runs": all(a.proof == b.proof for a, b in zip(res, e2e_res))
+            and all(a.proof == b.proof for a, b in zip(res, h_res)),
+        }
+        info["h2d_bytes"] = 4 * elements
+        info["d2h_bytes"] = sum(len(r.proof) for r in res)
+        ms_max = sv_s * 1e3
+        info["config"] = {"workload": f"served commit stream: {len(reqs)} requests, Poisson "
+                                      f"{args.rate:g}/s, log2 h {args.min_log_h}..{args.max_log_h}, "
+                                      "w log-uniform 1..256, blowup 2|4, 30% fold to 2^8 + 64 "
+                                      "queries", "budget_gb": args.budget_gb,
+                          "max_batch": args.max_batch, "streams": args.streams,
+                          "field": "babybear", "hash": "poseidon2-16 (built-in)",
+                          "l2": "inputs larger than L2"}
 
     peaks = {}
     try:
@@ -307,6 +407,7 @@ def main():
         "steps": args.steps,
         "warmup": max(args.warmup, 3),
         "ms_per_step": ms_max / args.steps,
+        "workload": args.workload,
         "higher_is_better": True,
         "scaling": "weak",
         "vs_baseline": None,
@@ -327,6 +428,8 @@ def main():
         "clocks": clk,
         "gpu_launches": int(launches),
     }
+    if served_info is not None:
+        out["served"] = served_info
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         v, secs, thr = cpu_trace_sample(16, args.cols, args.log_blowup, args.queries, reps=1)
         out["cpu_baseline"] = {"value": v, "unit": "elem/s", "cores": thr, "kind": "port",

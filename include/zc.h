@@ -176,13 +176,14 @@ zc_status zc_fri_fold_commit(const zc_poseidon2* p, const uint32_t* cw, int64_t 
                              uint32_t generator, uint32_t* out, uint32_t* next_layers,
                              void* stream);
 
-/* out[j] = sum_c alpha^c * cw[c][j] over w base columns of n words (EF4
- * alpha, device): batches a committed matrix's columns into one EF4 codeword
- * for its fold rounds, the role of batch_staggered in the Basefold batch open
- * (zorch/pcs/basefold/batching.py:38-78), here with powers of one challenge.
- * out: [n, 4], 16-byte aligned; w <= 4096. */
+/* Staggered partial-Lagrange batching of a committed matrix's w base columns
+ * (n words each) into one EF4 codeword [n, 4] (16-byte aligned): weights =
+ * eq(., r) over nbv = ceil(log2 w) EF4 challenges (challenges: nbv x 4 words,
+ * challenge 0 the most significant index bit), column c weighted by entry c
+ * -- sample_rlc_coeffs_bits + batch_staggered (zorch/pcs/jagged/open.py:88-105,
+ * zorch/pcs/basefold/batching.py:66-80). w <= 4096. */
 zc_status zc_rlc_columns(zc_field field, const uint32_t* cw, int64_t n, int32_t w,
-                         const uint32_t* alpha, uint32_t* out, void* stream);
+                         const uint32_t* challenges, uint32_t* out, void* stream);
 /* Synthetic benchmark data (no reference counterpart): out[i] =
  * SplitMix64(seed * 0x100000001B3 + i) mod p, canonical form. */
 zc_status zc_fill_uniform(zc_field field, uint32_t* out, int64_t n, uint64_t seed, void* stream);

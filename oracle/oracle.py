@@ -303,11 +303,14 @@ class CommitPhaseProof:
         return b"".join(np.ascontiguousarray(x, dtype="<u4").tobytes() for x in parts)
 
 
-def rlc_columns(field: int, cw, alpha) -> np.ndarray:
+def rlc_columns(field: int, cw, challenges) -> np.ndarray:
+    """Partial-Lagrange batching; `challenges` = ceil(log2 w) EF4 values (4 words each)."""
     cw = u32(cw)
     w, n = cw.shape
     out = np.zeros((n, 4), np.uint32)
-    LIB.orc_rlc_columns(field, cw.reshape(-1), n, w, u32(alpha), out.reshape(-1))
+    ch = u32(challenges).reshape(-1)
+    LIB.orc_rlc_columns(field, cw.reshape(-1), n, w, ch if ch.size else np.zeros(4, np.uint32),
+                        out.reshape(-1))
     return out
 
 

@@ -492,27 +492,37 @@ int orc_fri_fold(int field, const uint32_t* cw, int64_t n, int ef_in, const uint
   return 0;
 }
 
-/* out[j] = sum_c alpha^c * cw[c][j]: the columns of a committed matrix
- * combined into one EF4 codeword with powers of one EF4 challenge. */
-void orc_rlc_columns(int field, const uint32_t* cw, int64_t n, int w, const uint32_t* alpha,
+/* sample_rlc_coeffs_bits + batch_staggered (zorch/pcs/jagged/open.py:88-105,
+ * zorch/pcs/basefold/batching.py:66-80): eq(., r) over nbv = ceil(log2 w) EF4
+ * challenges expanded MSB-first (zorch/poly/eq.py:55-62, 92-115), column c
+ * weighted by entry c of the table. */
+void orc_rlc_columns(int field, const uint32_t* cw, int64_t n, int w, const uint32_t* chal,
                      uint32_t* out) {
   const fld* F = FLD(field);
-  uint32_t* pw = (uint32_t*)malloc(sizeof(uint32_t) * 4 * (size_t)(w > 0 ? w : 1));
-  uint32_t acc[4] = {F->one, 0, 0, 0};
-  for (int c = 0; c < w; c++) {
-    memcpy(pw + 4 * c, acc, 16);
-    uint32_t nx[4];
-    ef4_mul(F, acc, alpha, nx);
-    memcpy(acc, nx, 16);
+  int nbv = 0;
+  while ((1 << nbv) < w) nbv++;
+  uint32_t* st = (uint32_t*)calloc((size_t)4 << nbv, sizeof(uint32_t));
+  st[0] = F->one;
+  for (int j = 0; j < nbv; j++) {
+    uint32_t* nx = (uint32_t*)calloc((size_t)4 << (j + 1), sizeof(uint32_t));
+    for (int i = 0; i < (1 << j); i++) {
+      uint32_t hi[4], lo[4];
+      ef4_mul(F, st + 4 * i, chal + 4 * j, hi);
+      for (int e = 0; e < 4; e++) lo[e] = fsub(F, st[4 * i + e], hi[e]);
+      memcpy(nx + 4 * (2 * i), lo, 16);
+      memcpy(nx + 4 * (2 * i + 1), hi, 16);
+    }
+    memcpy(st, nx, sizeof(uint32_t) * ((size_t)4 << (j + 1)));
+    free(nx);
   }
 #pragma omp parallel for num_threads(orc_get_threads()) schedule(static)
   for (int64_t j = 0; j < n; j++) {
     uint32_t r[4] = {0, 0, 0, 0};
     for (int c = 0; c < w; c++)
-      for (int e = 0; e < 4; e++) r[e] = fadd(F, r[e], fmul(F, pw[4 * c + e], cw[(int64_t)c * n + j]));
+      for (int e = 0; e < 4; e++) r[e] = fadd(F, r[e], fmul(F, st[4 * c + e], cw[(int64_t)c * n + j]));
     memcpy(out + 4 * j, r, 16);
   }
-  free(pw);
+  free(st);
 }
 
 /* ----------------------------------------------------------- transcript ---- */

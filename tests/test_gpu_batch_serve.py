@@ -151,9 +151,10 @@ def test_served_fold_proofs_match_oracle(orc):
         assert np.array_equal(words[:8], root)
         t = orc.Transcript(p2)
         t.observe(root)
-        alpha = t.sample(4)
-        rlc = orc.rlc_columns(0, cw, alpha)
+        nbv = (cw.shape[0] - 1).bit_length()
+        rlc = orc.rlc_columns(0, cw, t.sample(4 * nbv) if nbv else [])
         rounds = r.log_h + r.log_blowup - FOLD_FINAL_LOG
+        t.observe([BABYBEAR.mont(rounds)])
         proof = orc.fri_commit_phase(p2, 0, rlc, rounds, FOLD_QUERIES, 4, t, BABYBEAR.mont(31))
         n = cw.shape[1]
         rows, paths = orc.merkle_open(cw, n, cw.shape[0], 1, n, layers, proof.positions)
@@ -162,6 +163,27 @@ def test_served_fold_proofs_match_oracle(orc):
         for rr, pp in zip(proof.rows, proof.paths):
             parts += [rr.reshape(-1), pp.reshape(-1)]
         assert np.array_equal(words, np.concatenate(parts))
+
+
+def test_partial_lagrange_batching_matches_oracle(orc):
+    from zorch_gb300.serve import batch_columns
+    from zorch_gb300.transcript import DuplexTranscript
+
+    for w in (1, 2, 5, 8, 33):
+        x = np.random.default_rng(w).integers(0, BABYBEAR.p, size=(w, 64),
+                                                dtype=np.uint64).astype(np.uint32)
+        xm = orc.to_mont(0, x)
+        from zorch_gb300.commit import Poseidon2
+        from zorch_gb300.field import to_device
+
+        t = DuplexTranscript.new(Poseidon2.builtin())
+        got = to_host(batch_columns(to_device(xm).reshape(w, 64), t))
+        to = orc.Transcript(orc.Poseidon2.babybear16())
+        nbv = (w - 1).bit_length()
+        want = orc.rlc_columns(0, xm, to.sample(4 * nbv) if nbv else [])
+        assert np.array_equal(got.reshape(want.shape), want)
+        if w == 1:
+            assert np.array_equal(want[:, 0], xm[0]) and not want[:, 1:].any()
 
 
 def test_plain_path_per_polynomial_roots(orc):

@@ -470,19 +470,30 @@ zc_status tree_batch_wave(const zc_merkle_job* jobs, int n, unsigned long long* 
   return launch_check();
 }
 
-// out[j] = sum_c alpha^c * cw[c][j] (EF4 alpha on the device, base columns):
-// the columns of a committed matrix batched into one EF4 codeword before its
-// fold rounds. Powers of alpha are staged in shared memory per block.
+// Staggered partial-Lagrange batching of one committed matrix's columns into
+// one EF4 codeword (sample_rlc_coeffs_bits + batch_staggered,
+// zorch/pcs/jagged/open.py:88-105, zorch/pcs/basefold/batching.py:66-80):
+// weights = eq(., r) over nbv = ceil(log2 w) EF4 challenges, table built by
+// the MSB-first interleaving step (zorch/poly/eq.py:55-62: high = s*r,
+// low = s - high), column c weighted by entry c; out[j] = sum_c wt_c cw[c][j].
 template <class F>
-__global__ void k_rlc(const uint32_t* cw, int64_t n, int w, const uint32_t* alpha,
+__global__ void k_rlc(const uint32_t* cw, int64_t n, int w, const uint32_t* chal, int nbv,
                       uint32_t* out) {
-  extern __shared__ uint32_t pw[];  // w x 4
+  extern __shared__ uint32_t wt[];  // 2^nbv x 4 (EF4)
   if (threadIdx.x == 0) {
-    ef4 a{{alpha[0], alpha[1], alpha[2], alpha[3]}};
-    ef4 acc{{F::ONE, 0u, 0u, 0u}};
-    for (int c = 0; c < w; c++) {
-      for (int e = 0; e < 4; e++) pw[4 * c + e] = acc.c[e];
-      acc = ef_mul<F>(acc, a);
+    wt[0] = F::ONE;
+    wt[1] = wt[2] = wt[3] = 0;
+    for (int j = 0; j < nbv; j++) {
+      const ef4 r{{chal[4 * j], chal[4 * j + 1], chal[4 * j + 2], chal[4 * j + 3]}};
+      for (int i = (1 << j) - 1; i >= 0; i--) {  // in place, from the top
+        const ef4 s{{wt[4 * i], wt[4 * i + 1], wt[4 * i + 2], wt[4 * i + 3]}};
+        const ef4 hi = ef_mul<F>(s, r);
+        const ef4 lo = ef_sub<F>(s, hi);
+        for (int e = 0; e < 4; e++) {
+          wt[4 * (2 * i) + e] = lo.c[e];
+          wt[4 * (2 * i + 1) + e] = hi.c[e];
+        }
+      }
     }
   }
   __syncthreads();
@@ -492,10 +503,9 @@ __global__ void k_rlc(const uint32_t* cw, int64_t n, int w, const uint32_t* alph
     for (int c = 0; c < w; c++) {
       const uint32_t x = __ldg(cw + (int64_t)c * n + j);
 #pragma unroll
-      for (int e = 0; e < 4; e++) r[e] = madd<F>(r[e], mmul<F>(pw[4 * c + e], x));
+      for (int e = 0; e < 4; e++) r[e] = madd<F>(r[e], mmul<F>(wt[4 * c + e], x));
     }
-    uint4 o = make_uint4(r[0], r[1], r[2], r[3]);
-    reinterpret_cast<uint4*>(out)[j] = o;
+    reinterpret_cast<uint4*>(out)[j] = make_uint4(r[0], r[1], r[2], r[3]);
   }
 }
 
@@ -615,8 +625,10 @@ zc_status zc_merkle_commit_batch(const zc_poseidon2* p, const zc_merkle_job* job
 }
 
 zc_status zc_rlc_columns(zc_field field, const uint32_t* cw, int64_t n, int32_t w,
-                         const uint32_t* alpha, uint32_t* out, void* stream) {
-  if (!cw || !alpha || !out || n < 0 || w < 1 || w > 4096) return ZC_BAD_ARG;
+                         const uint32_t* challenges, uint32_t* out, void* stream) {
+  if (!cw || !out || n < 0 || w < 1 || w > 4096) return ZC_BAD_ARG;
+  const int nbv = ilog2(w);
+  if (nbv > 0 && !challenges) return ZC_BAD_ARG;
   if ((uintptr_t)out % 16) return ZC_BAD_ARG;
   if (n == 0) return ZC_OK;
   cudaStream_t st = (cudaStream_t)stream;
@@ -624,7 +636,7 @@ zc_status zc_rlc_columns(zc_field field, const uint32_t* cw, int64_t n, int32_t 
     using F = decltype(f);
     int64_t blocks = (n + 255) / 256;
     if (blocks > 152 * 8) blocks = 152 * 8;
-    k_rlc<F><<<(unsigned)blocks, 256, (size_t)w * 16, st>>>(cw, n, w, alpha, out);
+    k_rlc<F><<<(unsigned)blocks, 256, ((size_t)16) << nbv, st>>>(cw, n, w, challenges, nbv, out);
     return launch_check();
   });
 }

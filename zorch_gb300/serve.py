@@ -113,25 +113,41 @@ FOLD_FINAL_LOG = 8
 FOLD_QUERIES = 64
 
 
+def batch_columns(cw: torch.Tensor, t: DuplexTranscript) -> torch.Tensor:
+    """Draw ceil(log2 w) EF4 challenges (sample_challenge, 4 squeezes each) and
+    combine the columns with their partial-Lagrange weights (zc_rlc_columns):
+    the single-round case of sample_rlc_coeffs_bits + batch_staggered
+    (zorch/pcs/jagged/open.py:88-105, zorch/pcs/basefold/batching.py:66-80)."""
+    w, n = cw.shape
+    nbv = (w - 1).bit_length()
+    chal = t.sample_(4 * nbv) if nbv else None
+    out = torch.empty((n, 4), dtype=torch.int32, device=cw.device)
+    _lib.check(_lib.lib().zc_rlc_columns(BABYBEAR.id, ptr(cw), n, w, ptr(chal), ptr(out),
+                                         stream_handle()), "rlc_columns")
+    return out
+
+
 def fold_and_open(req: Request, cw: torch.Tensor, root: torch.Tensor, perm: Poseidon2,
-                  tree: MerkleTree) -> tuple:
-    """Basefold-style open of a committed matrix: observe the root, draw an EF4
-    alpha, batch the columns into one EF4 codeword (zc_rlc_columns), fold with
-    EF4 challenges down to 2^8 committing every layer, observe the final layer,
-    sample 64 positions, open the matrix rows and every fold layer there."""
+                  tree: MerkleTree, layers=None) -> tuple:
+    """Open a committed matrix the Basefold way without the sumcheck: observe
+    the root, batch the columns into one EF4 codeword, observe the fold-round
+    count (the domain separation of zorch/pcs/jagged/open.py:262-263), fold
+    with EF4 challenges down to 2^8 committing every layer, observe the final
+    layer, sample 64 positions, and open the matrix rows and every fold layer
+    there."""
     n = cw.shape[1]
     t = DuplexTranscript.new(perm, device=cw.device)
-    alpha = t.observe_and_sample_(root, 4)
-    rlc = torch.empty((n, 4), dtype=torch.int32, device=cw.device)
-    _lib.check(_lib.lib().zc_rlc_columns(BABYBEAR.id, ptr(cw), n, cw.shape[0], ptr(alpha),
-                                         ptr(rlc), stream_handle()), "rlc_columns")
+    t.observe_(root)
+    rlc = batch_columns(cw, t)
+    rounds = max(req.log_n - FOLD_FINAL_LOG, 0)
+    t.observe_(torch.tensor([BABYBEAR.mont(rounds)], dtype=torch.int32, device=cw.device))
     code = ReedSolomon(1 << req.log_h, 1 << req.log_blowup, BABYBEAR, coset_shift=31,
                        generator=31)
-    rounds = max(req.log_n - FOLD_FINAL_LOG, 0)
     prover = FriProver(FriParams(code, tree, rounds, FOLD_QUERIES, 4))
     proof, t, _ = prover.commit_phase(rlc, t)
-    rows = tree.open_layout(leaves_layout(cw, n, cw.shape[0], 1, n),
-                            _ResidentLayers.get(req.rid), proof.positions, cw.shape[0])
+    layers = layers if layers is not None else _ResidentLayers.get(req.rid)
+    rows = tree.open_layout(leaves_layout(cw, n, cw.shape[0], 1, n), layers, proof.positions,
+                            cw.shape[0])
     return proof, rows
 
 
@@ -304,11 +320,10 @@ def run_plain(requests: list[Request], host_fed: bool = False,
         parts = [stacked.reshape(-1)]
         if r.fold:
             t = DuplexTranscript.new(perm, device=x.device)
-            alpha = t.observe_and_sample_(stacked, 4)
-            rlc = torch.empty((n, 4), dtype=torch.int32, device=x.device)
-            _lib.check(_lib.lib().zc_rlc_columns(BABYBEAR.id, ptr(cw), n, r.width, ptr(alpha),
-                                                 ptr(rlc), stream_handle()), "rlc_columns")
+            t.observe_(stacked)
+            rlc = batch_columns(cw, t)
             rounds = max(r.log_n - FOLD_FINAL_LOG, 0)
+            t.observe_(torch.tensor([BABYBEAR.mont(rounds)], dtype=torch.int32, device=x.device))
             fri = FriProver(FriParams(code, tree, rounds, FOLD_QUERIES, 4))
             proof, t, _ = fri.commit_phase(rlc, t)
             parts += [proof.roots.reshape(-1), proof.final_layer.reshape(-1),
