@@ -58,6 +58,8 @@ def _load() -> C.CDLL:
         "orc_rs_encode": (i32, [i32, _u32p, i64, i32, i32, u32, u32, _u32p]),
         "orc_rs_encode_horner": (i32, [i32, _u32p, i32, i32, u32, u32, _u32p]),
         "orc_eval_domain": (None, [i32, i32, u32, u32, _u32p]),
+        "orc_eval_poly": (u32, [i32, _u32p, i64, u32]),
+        "orc_domain_point": (u32, [i32, i32, u32, u32, i64]),
         "orc_fri_fold": (i32, [i32, _u32p, i64, i32, _u32p, i32, u32, u32, _u32p]),
         "orc_duplex_init": (None, [vp]),
         "orc_duplex_observe": (None, [vp, vp, _u32p, i64]),
@@ -236,6 +238,25 @@ def rs_encode_horner(field, coeffs, log_blowup, shift_mont=0, generator=0) -> np
     out = np.zeros(k << log_blowup, np.uint32)
     LIB.orc_rs_encode_horner(field, c, k.bit_length() - 1, log_blowup, shift_mont, generator, out)
     return out
+
+
+def eval_poly(field: int, coeffs, x: int) -> int:
+    c = u32(coeffs).reshape(-1)
+    return int(LIB.orc_eval_poly(field, c, c.size, x))
+
+
+def domain_point(field: int, log_n: int, shift_mont: int, j: int, generator: int = 0) -> int:
+    return int(LIB.orc_domain_point(field, log_n, shift_mont, generator, j))
+
+
+def reconstruct_root(p2: "Poseidon2", row, index: int, path) -> np.ndarray:
+    """Rebuild a root from an opened row and its sibling path (leaf first),
+    MerkleTree.reconstruct_root (zorch/commit/merkle.py:264-285)."""
+    node = p2.hash(row)
+    for sib in path:
+        node = p2.compress(node, sib) if index % 2 == 0 else p2.compress(sib, node)
+        index //= 2
+    return node
 
 
 def eval_domain(field: int, log_n: int, shift_mont: int = 0, generator: int = 0) -> np.ndarray:

@@ -437,6 +437,22 @@ int orc_rs_encode_horner(int field, const uint32_t* coeffs, int log_k, int log_b
   return 0;
 }
 
+/* Horner evaluation of one polynomial at one point: sum_i c_i x^i. */
+uint32_t orc_eval_poly(int field, const uint32_t* coeffs, int64_t k, uint32_t x) {
+  const fld* F = FLD(field);
+  uint32_t acc = 0;
+  for (int64_t i = k - 1; i >= 0; i--) acc = fadd(F, fmul(F, acc, x), coeffs[i]);
+  return acc;
+}
+
+/* The j-th point of the coset domain shift * w_n^j. */
+uint32_t orc_domain_point(int field, int log_n, uint32_t shift_mont, uint32_t generator,
+                          int64_t j) {
+  const fld* F = FLD(field);
+  uint32_t w = log_n ? root_of_unity(F, log_n, generator) : F->one;
+  return fmul(F, shift_mont ? shift_mont : F->one, fpow(F, w, (uint64_t)j));
+}
+
 /* eval_domain (zorch/coding/reed_solomon.py:49-68): [shift * w^j]. */
 void orc_eval_domain(int field, int log_n, uint32_t shift_mont, uint32_t generator,
                      uint32_t* out) {

@@ -90,6 +90,9 @@ int orc_rs_encode(int field, const uint32_t* coeffs, int64_t batch, int log_k,
 int orc_rs_encode_horner(int field, const uint32_t* coeffs, int log_k,
                          int log_blowup, uint32_t shift_mont, uint32_t generator,
                          uint32_t* out);
+uint32_t orc_eval_poly(int field, const uint32_t* coeffs, int64_t k, uint32_t x);
+uint32_t orc_domain_point(int field, int log_n, uint32_t shift_mont, uint32_t generator,
+                          int64_t j);
 void orc_eval_domain(int field, int log_n, uint32_t shift_mont, uint32_t generator,
                      uint32_t* out);
 
