@@ -109,6 +109,28 @@ zc_status zc_rs_encode(zc_field field, const uint32_t* coeffs, int64_t batch, in
                        uint32_t* out, void* workspace, size_t workspace_bytes,
                        void* stream);
 
+/* The LDE of zc_rs_encode without any device allocation and without a
+ * caller workspace: no counterpart in the reference. For callers that cannot
+ * allocate device memory at call time -- a handler inside an XLA/FRX custom
+ * call (the framework owns the device memory and by default preallocates most
+ * of it, so a cudaMalloc there can fail or fragment its pool), code being
+ * recorded into a CUDA graph (cudaMalloc is not a stream operation and cannot
+ * be captured), or a serving loop that must not stall on the allocator. The
+ * four-step intermediate lives in a fixed 64 MiB (2^24-word) static device
+ * array that every GPU loading this library holds until the process exits;
+ * columns are processed in chunks that fit it, and a size whose single column
+ * needs more (2^(log_k+log_blowup) > 2^24 words) is rejected with
+ * ZC_BAD_SHAPE. The array is shared by every call and keeps the last call's
+ * contents (nothing in it needs to start at zero); calls that overlap on the
+ * GPU (different streams, or different host threads) race on it -- serialise
+ * them. The first call on a device performs set-up (root tables, the device
+ * address of the array) and synchronises that device: make it before any
+ * stream capture, and early, before another runtime preallocates the memory.
+ * Arguments and results as zc_rs_encode. */
+zc_status zc_rs_encode_noalloc(zc_field field, const uint32_t* coeffs, int64_t batch, int log_k,
+                               int log_blowup, uint32_t shift_mont, uint32_t generator,
+                               uint32_t* out, void* stream);
+
 /* Batched LDE: many jobs (matrices of different heights, widths, blowups) in
  * two persistent launches over a (job, tile) work list -- the batched form of
  * the one-call-per-matrix encode of zorch/pcs/basefold/prover.py:437-447.

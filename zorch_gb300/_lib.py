@@ -65,6 +65,7 @@ def _declare(lib: C.CDLL) -> None:
         "zc_poseidon2_permute": (st, [vp, vp, i64, vp]),
         "zc_rs_encode_workspace_bytes": (sz, [i64, C.c_int, C.c_int]),
         "zc_rs_encode": (st, [st, vp, i64, C.c_int, C.c_int, u32, u32, vp, vp, sz, vp]),
+        "zc_rs_encode_noalloc": (st, [st, vp, i64, C.c_int, C.c_int, u32, u32, vp, vp]),
         "zc_merkle_commit": (st, [vp, Leaves, vp, vp]),
         "zc_merkle_open": (st, [Leaves, vp, vp, i32, vp, vp, vp, vp]),
         "zc_fri_fold": (st, [st, vp, i64, C.c_int, vp, C.c_int, u32, u32, vp, vp]),

@@ -18,6 +18,8 @@
 // processed 4 stages per register pass (16 elements per thread).
 #include <string.h>
 
+#include <mutex>
+
 #include "internal.cuh"
 
 namespace zc {
@@ -511,6 +513,36 @@ zc_status lde_batch_launch(const zc_lde_job* jobs, int njobs, void* ws, size_t w
   return ZC_OK;
 }
 
+// ----------------------------------------------------- allocation-free --
+// Scratch for zc_rs_encode_noalloc: the four-step intermediate of one chunk of
+// columns lives in this fixed device array instead of a caller workspace. It is
+// reserved when the library's device code is loaded on a GPU and held until the
+// process exits, on every GPU that loads the library.
+constexpr size_t kNoAllocScratchWords = (size_t)1 << 24;  // 64 MiB
+static __device__ __align__(256) uint32_t g_noalloc_scratch[kNoAllocScratchWords];
+
+static std::mutex g_noalloc_mu;
+static uint32_t* g_noalloc_ptr[64];
+
+// The device address of the scratch array on the current device. In host code
+// the symbol names a host-side stand-in, never a device address, so the
+// address is fetched with cudaGetSymbolAddress once per device, with that
+// device current, and cached.
+static zc_status noalloc_scratch(uint32_t** out) {
+  int dev = 0;
+  ZC_CUDA(cudaGetDevice(&dev));
+  if (dev < 0 || dev >= 64) return ZC_BAD_ARG;
+  std::lock_guard<std::mutex> lock(g_noalloc_mu);
+  if (!g_noalloc_ptr[dev]) {
+    void* p = nullptr;
+    const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+    if (e != cudaSuccess) return cuda_fail(e);
+    g_noalloc_ptr[dev] = (uint32_t*)p;
+  }
+  *out = g_noalloc_ptr[dev];
+  return ZC_OK;
+}
+
 }  // namespace zc
 
 using namespace zc;
@@ -547,6 +579,36 @@ zc_status zc_rs_encode(zc_field field, const uint32_t* coeffs, int64_t batch, in
     const uint32_t h = shift_mont ? shift_mont : F::ONE;
     return lde_launch<F>(coeffs, batch, log_k, log_blowup, h, out, workspace, workspace_bytes,
                          (cudaStream_t)stream);
+  });
+}
+
+zc_status zc_rs_encode_noalloc(zc_field field, const uint32_t* coeffs, int64_t batch, int log_k,
+                               int log_blowup, uint32_t shift_mont, uint32_t generator,
+                               uint32_t* out, void* stream) {
+  if (!coeffs || !out || batch < 0 || log_k < 0 || log_blowup < 0) return ZC_BAD_ARG;
+  if (batch == 0) return ZC_OK;
+  return with_field(field, [&](auto f) -> zc_status {
+    using F = decltype(f);
+    if (log_k + log_blowup > F::TWO_ADICITY || log_k > 24) {
+      set_error("LDE size exceeds the supported two-adic range");
+      return ZC_BAD_SHAPE;
+    }
+    if (generator != 0 && generator != F::GEN) {
+      set_error("only the field's canonical generator is built");
+      return ZC_UNSUPPORTED;
+    }
+    const LdePlan p = plan_lde(log_k, log_blowup);
+    if (!p.small && (((size_t)1) << (log_k + log_blowup)) > kNoAllocScratchWords) {
+      set_error("zc_rs_encode_noalloc: one column's LDE (2^(log_k+log_blowup) words) exceeds "
+                "the 2^24-word (64 MiB) fixed scratch; use zc_rs_encode with a workspace");
+      return ZC_BAD_SHAPE;
+    }
+    ZC_TRY(ensure_init());
+    uint32_t* scratch = nullptr;
+    ZC_TRY(noalloc_scratch(&scratch));
+    const uint32_t h = shift_mont ? shift_mont : F::ONE;
+    return lde_launch<F>(coeffs, batch, log_k, log_blowup, h, out, scratch,
+                         kNoAllocScratchWords * 4, (cudaStream_t)stream);
   });
 }
 
