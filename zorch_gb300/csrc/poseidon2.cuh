@@ -36,8 +36,55 @@ static __constant__ uint32_t c_bb16_ext_term[64] = ZC_BB16_EXT_TERM_MONT_INIT;
 static __constant__ uint32_t c_bb16_int_rc[ZC_BB16_ROUNDS_P] = ZC_BB16_INT_RC_MONT_INIT;
 static __constant__ uint32_t c_bb16_diag[16] = ZC_BB16_DIAG_MONT_INIT;
 
+// Multiplications by the built-in BabyBear diagonal entries without a
+// Montgomery product (the representation is linear, so a constant c acts on
+// Mont(x) as on x). p = 15 * 2^27 + 1, so for k <= 27 and q = (-x) mod 2^k,
+// x + q*p is divisible by 2^k and x * 2^-k = ((x + q) >> k) + q * 15 * 2^(27-k).
+struct Bb {
+  static constexpr uint32_t P = BabyBear::P;
+  __device__ __forceinline__ static uint32_t dbl(uint32_t x) { return madd<BabyBear>(x, x); }
+  __device__ __forceinline__ static uint32_t half(uint32_t x) {
+    return (x & 1u) ? (x >> 1) + ((P + 1) >> 1) : (x >> 1);
+  }
+  template <int K>
+  __device__ __forceinline__ static uint32_t div2exp(uint32_t x) {
+    static_assert(K >= 1 && K <= 27, "k out of range");
+    const uint32_t q = (0u - x) & ((1u << K) - 1u);
+    const uint32_t r = ((x + q) >> K) + q * (15u << (27 - K));
+    const uint32_t t = r - P;
+    return t < r ? t : r;
+  }
+};
+
 struct Bb16Builtin {
   using F = BabyBear;
+  // Internal layer s_i <- sum + d_i s_i for the built-in diagonal
+  // [-2, 1, 2, 1/2, 3, 4, -1/2, -3, -4, 2^-8, 1/4, 1/8, 2^-27, -2^-8, -1/16, -2^-27]
+  // on the integer ALU pipe instead of 16 Montgomery products.
+  __device__ __forceinline__ void internal_layer(uint32_t* s) const {
+    using B = Bb;
+    uint32_t part = madd<F>(madd<F>(madd<F>(s[1], s[2]), madd<F>(s[3], s[4])),
+                            madd<F>(madd<F>(s[5], s[6]), madd<F>(s[7], s[8])));
+    part = madd<F>(part, madd<F>(madd<F>(madd<F>(s[9], s[10]), madd<F>(s[11], s[12])),
+                                 madd<F>(madd<F>(s[13], s[14]), s[15])));
+    const uint32_t sum = madd<F>(part, s[0]);
+    s[0] = msub<F>(part, s[0]);  // sum - 2 s0
+    s[1] = madd<F>(sum, s[1]);
+    s[2] = madd<F>(sum, B::dbl(s[2]));
+    s[3] = madd<F>(sum, B::half(s[3]));
+    s[4] = madd<F>(sum, madd<F>(B::dbl(s[4]), s[4]));
+    s[5] = madd<F>(sum, B::dbl(B::dbl(s[5])));
+    s[6] = msub<F>(sum, B::half(s[6]));
+    s[7] = msub<F>(sum, madd<F>(B::dbl(s[7]), s[7]));
+    s[8] = msub<F>(sum, B::dbl(B::dbl(s[8])));
+    s[9] = madd<F>(sum, B::div2exp<8>(s[9]));
+    s[10] = madd<F>(sum, B::div2exp<2>(s[10]));
+    s[11] = madd<F>(sum, B::div2exp<3>(s[11]));
+    s[12] = madd<F>(sum, B::div2exp<27>(s[12]));
+    s[13] = msub<F>(sum, B::div2exp<8>(s[13]));
+    s[14] = msub<F>(sum, B::div2exp<4>(s[14]));
+    s[15] = msub<F>(sum, B::div2exp<27>(s[15]));
+  }
   static constexpr int RF_HALF = ZC_BB16_ROUNDS_F_HALF;
   __device__ __forceinline__ int rf_half() const { return RF_HALF; }
   __device__ __forceinline__ int rp() const { return ZC_BB16_ROUNDS_P; }
@@ -74,6 +121,16 @@ struct RtParams {
     }
   }
   ZC_HD uint32_t jsum(uint32_t s) const { return p->j_is_one ? s : mmul<F>(s, p->j_scale); }
+  // Generic internal layer s_i <- j*sum(s) + diag_i * s_i.
+  ZC_HD void internal_layer(uint32_t* s) const {
+    uint32_t a0 = madd<F>(madd<F>(s[0], s[1]), madd<F>(s[2], s[3]));
+    uint32_t a1 = madd<F>(madd<F>(s[4], s[5]), madd<F>(s[6], s[7]));
+    uint32_t a2 = madd<F>(madd<F>(s[8], s[9]), madd<F>(s[10], s[11]));
+    uint32_t a3 = madd<F>(madd<F>(s[12], s[13]), madd<F>(s[14], s[15]));
+    uint32_t sum = jsum(madd<F>(madd<F>(a0, a1), madd<F>(a2, a3)));
+#pragma unroll
+    for (int i = 0; i < 16; i++) s[i] = madd<F>(sum, mmul<F>(dg(i), s[i]));
+  }
 };
 
 // External (M4 block-circulant) linear layer.
@@ -112,13 +169,7 @@ ZC_HD void p2_permute(uint32_t* s, const K& k) {
 #pragma unroll 1
   for (int r = 0; r < k.rp(); r++) {
     s[0] = k.sbox(madd<F>(s[0], k.ir(r)));
-    uint32_t a0 = madd<F>(madd<F>(s[0], s[1]), madd<F>(s[2], s[3]));
-    uint32_t a1 = madd<F>(madd<F>(s[4], s[5]), madd<F>(s[6], s[7]));
-    uint32_t a2 = madd<F>(madd<F>(s[8], s[9]), madd<F>(s[10], s[11]));
-    uint32_t a3 = madd<F>(madd<F>(s[12], s[13]), madd<F>(s[14], s[15]));
-    uint32_t sum = k.jsum(madd<F>(madd<F>(a0, a1), madd<F>(a2, a3)));
-#pragma unroll
-    for (int i = 0; i < 16; i++) s[i] = madd<F>(sum, mmul<F>(k.dg(i), s[i]));
+    k.internal_layer(s);
   }
 #pragma unroll 1
   for (int r = 0; r < k.rf_half(); r++) {
