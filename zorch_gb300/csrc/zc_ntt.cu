@@ -70,6 +70,9 @@ __device__ __forceinline__ int brev(int i, int bits) {
   return bits ? (int)(__brev((unsigned)i) >> (32 - bits)) : 0;
 }
 __host__ __device__ __forceinline__ int padded(int m) { return m + (m >> 5); }
+// Row stride of a tile of rows of m words: padded, then odd, so that threads
+// of a warp reading the same position of consecutive rows hit distinct banks.
+__host__ __device__ __forceinline__ int row_stride(int m) { return padded(m) | 1; }
 
 // tab[i] = base^i for i < count (count a power of two), by doubling.
 template <class F>
@@ -86,83 +89,104 @@ __device__ void pow_table(uint32_t* tab, int count, uint32_t base) {
   }
 }
 
-// Stages s0 .. s0+R-1 of the DIT over `rows` rows of m = 2^logm (padded row
-// stride rs), twiddles tw[e] = w_m^e.
+// One radix-2^R pass of a decimation-in-frequency NTT over `rows` rows of
+// m = 2^logm words (row stride rs): the stages of half-size 2^h0 down to
+// 2^(h0-R+1). A group is the 2^R elements base + j*S, S = 2^(h0-R+1); the
+// butterfly (u, v) -> (u + v, (u - v) * w_{2H}^pos) with pos the offset in the
+// 2H-block. Consecutive threads take consecutive rows (row-major tiles) so a
+// warp's shared-memory accesses fall on distinct banks.
 template <class F, int R>
-__device__ __forceinline__ void dit_pass(uint32_t* a, int rows, int logm, int rs,
-                                         const uint32_t* tw, int s0) {
+__device__ __forceinline__ void dif_pass(uint32_t* a, int log_rows, int logm, int rs,
+                                         const uint32_t* tw, int h0) {
   constexpr int G = 1 << R;
+  const int lS = h0 - R + 1;
   const int glog = logm - R;
-  const int total = rows << glog;
+  const int total = 1 << (log_rows + glog);
+  const int rmask = (1 << log_rows) - 1;
   for (int gi = threadIdx.x; gi < total; gi += blockDim.x) {
-    const int row = gi >> glog, q = gi & ((1 << glog) - 1);
-    const int off = q & ((1 << s0) - 1), blk = q >> s0;
-    const int base = (blk << (s0 + R)) | off;
+    const int row = gi & rmask, g = gi >> log_rows;
+    const int off = g & ((1 << lS) - 1), blk = g >> lS;
+    const int base = (blk << (h0 + 1)) | off;
     uint32_t* ar = a + row * rs;
     uint32_t v[G];
 #pragma unroll
-    for (int j = 0; j < G; j++) v[j] = ar[pad(base + (j << s0))];
+    for (int j = 0; j < G; j++) v[j] = ar[pad(base + (j << lS))];
 #pragma unroll
     for (int r = 0; r < R; r++) {
-      const int s = s0 + r;
+      const int hb = R - 1 - r;  // local bit of this stage
+      const int H = h0 - r;      // log2 of the half size
 #pragma unroll
       for (int j = 0; j < G; j++) {
-        if (!(j & (1 << r))) {
-          const int j2 = j | (1 << r);
-          const int pos = off + ((j & ((1 << r) - 1)) << s0);
-          const uint32_t w = tw[pos << (logm - 1 - s)];
-          const uint32_t t = mmul<F>(v[j2], w);
-          v[j2] = msub<F>(v[j], t);
-          v[j] = madd<F>(v[j], t);
+        if (!(j & (1 << hb))) {
+          const int j2 = j | (1 << hb);
+          const int pos = off + ((j & ((1 << hb) - 1)) << lS);
+          const uint32_t w = tw[pos << (logm - 1 - H)];
+          const uint32_t u = v[j], t = v[j2];
+          v[j] = madd<F>(u, t);
+          v[j2] = mmul<F>(msub<F>(u, t), w);
         }
       }
     }
 #pragma unroll
-    for (int j = 0; j < G; j++) ar[pad(base + (j << s0))] = v[j];
+    for (int j = 0; j < G; j++) ar[pad(base + (j << lS))] = v[j];
   }
 }
 
-// Natural-order NTT of each row (input stored bit-reversed).
+// DIF NTT of each row, natural order in, bit-reversed order out (position p
+// holds output index brev(p)); stages split into balanced passes of <= 4.
 template <class F>
-__device__ void smem_ntt(uint32_t* a, int rows, int logm, int rs, const uint32_t* tw) {
-  for (int s0 = 0; s0 < logm; s0 += 4) {
-    const int R = logm - s0 < 4 ? logm - s0 : 4;
+__device__ void smem_ntt_dif(uint32_t* a, int log_rows, int logm, int rs, const uint32_t* tw) {
+  const int passes = (logm + 3) / 4;
+  int h0 = logm - 1;
+  for (int q = 0; q < passes; q++) {
+    const int remaining = h0 + 1;
+    const int R = (remaining + (passes - q) - 1) / (passes - q);
     switch (R) {
-      case 4: dit_pass<F, 4>(a, rows, logm, rs, tw, s0); break;
-      case 3: dit_pass<F, 3>(a, rows, logm, rs, tw, s0); break;
-      case 2: dit_pass<F, 2>(a, rows, logm, rs, tw, s0); break;
-      default: dit_pass<F, 1>(a, rows, logm, rs, tw, s0); break;
+      case 4: dif_pass<F, 4>(a, log_rows, logm, rs, tw, h0); break;
+      case 3: dif_pass<F, 3>(a, log_rows, logm, rs, tw, h0); break;
+      case 2: dif_pass<F, 2>(a, log_rows, logm, rs, tw, h0); break;
+      default: dif_pass<F, 1>(a, log_rows, logm, rs, tw, h0); break;
     }
     __syncthreads();
+    h0 -= R;
   }
 }
 
 constexpr int kThreads = 512;
 
 // One column, all b cosets (single pass). `sm` is the block's dynamic smem.
+// Layout: work[b][rs] | tw[k/2] | hp[k] | wl[128] | wh[128].
 template <class F>
 __device__ void lde_small_body(const uint32_t* x, uint32_t* out, int log_k, int log_b,
                                uint32_t h, int64_t c, uint32_t* sm) {
   const int k = 1 << log_k, b = 1 << log_b, log_n = log_k + log_b;
-  const int rs = padded(k);
+  const int rs = row_stride(k);
   uint32_t* work = sm;
   uint32_t* tw = work + b * rs;
   uint32_t* hp = tw + (k > 1 ? k / 2 : 1);
+  uint32_t* wl = hp + k;    // w_n^e, e < 128
+  uint32_t* wh = wl + 128;  // w_n^(128 e), e < 128
   const uint32_t* xc = x + (c << log_k);
+  const uint32_t wn = log_n ? omega_pow<F>(log_n, 1) : F::ONE;
   pow_table<F>(tw, k > 1 ? k / 2 : 1, log_k ? omega_pow<F>(log_k, 1) : F::ONE);
   pow_table<F>(hp, k, h);
+  pow_table<F>(wl, 128, wn);
+  pow_table<F>(wh, 128, mpow<F>(wn, 128));
   for (int idx = threadIdx.x; idx < (b << log_k); idx += blockDim.x) {
     const int s = idx >> log_k, i = idx & (k - 1);
     uint32_t v = mmul<F>(__ldg(xc + i), hp[i]);
-    if (s) v = mmul<F>(v, omega_pow<F>(log_n, (uint32_t)(s * i)));
-    work[s * rs + pad(brev(i, log_k))] = v;
+    if (s) {
+      const int e = s * i;  // < n <= 2^14
+      v = mmul<F>(v, mmul<F>(wl[e & 127], wh[e >> 7]));
+    }
+    work[s * rs + pad(i)] = v;
   }
   __syncthreads();
-  smem_ntt<F>(work, b, log_k, rs, tw);
+  smem_ntt_dif<F>(work, log_b, log_k, rs, tw);
   uint32_t* oc = out + (c << log_n);
   for (int idx = threadIdx.x; idx < (b << log_k); idx += blockDim.x) {
     const int t = idx >> log_b, s = idx & (b - 1);
-    oc[idx] = work[s * rs + pad(t)];
+    oc[idx] = work[s * rs + pad(brev(t, log_k))];
   }
 }
 
@@ -173,14 +197,17 @@ __global__ void __launch_bounds__(kThreads) k_lde_small(const uint32_t* x, uint3
   lde_small_body<F>(x, out, log_k, log_b, h, blockIdx.x, sm);
 }
 
-// Pass 1 item (coset s, i1 tile, column c). z layout per column: [b][k2][k1].
+// Pass 1 item (coset s, i1 tile, column c): the k2-point DIF NTTs down the
+// strided columns i1 of the message scaled by g_s^(i1 + k1 i2); writes the
+// untwiddled intermediate z[c][s][t2][i1] (t2 = bit-reversed position).
+// Layout: work[TI][rs] | tw[k2/2] | R[k2] | gi[TI].
 template <class F>
 __device__ void lde_pass1_body(const uint32_t* x, uint32_t* z, int log_k1, int log_k2, int log_b,
                                int log_ti, uint32_t h, int s, int tile, int64_t c,
                                uint32_t* sm) {
   const int k1 = 1 << log_k1, k2 = 1 << log_k2, TI = 1 << log_ti;
   const int log_k = log_k1 + log_k2, log_n = log_k + log_b;
-  const int rs = padded(k2);
+  const int rs = row_stride(k2);
   uint32_t* work = sm;
   uint32_t* tw = work + TI * rs;
   uint32_t* R = tw + (k2 > 1 ? k2 / 2 : 1);
@@ -197,16 +224,14 @@ __device__ void lde_pass1_body(const uint32_t* x, uint32_t* z, int log_k1, int l
     const int d = idx & (TI - 1), i2 = idx >> log_ti;
     uint32_t v = __ldg(xc + i1_0 + d + ((int64_t)i2 << log_k1));
     v = mmul<F>(mmul<F>(v, gi[d]), R[i2]);
-    work[d * rs + pad(brev(i2, log_k2))] = v;
+    work[d * rs + pad(i2)] = v;
   }
   __syncthreads();
-  smem_ntt<F>(work, TI, log_k2, rs, tw);
+  smem_ntt_dif<F>(work, log_ti, log_k2, rs, tw);
   uint32_t* zc_ = z + ((c << log_b) + s) * ((int64_t)1 << log_k);
   for (int idx = threadIdx.x; idx < (TI << log_k2); idx += blockDim.x) {
-    const int d = idx & (TI - 1), t2 = idx >> log_ti;
-    uint32_t v = work[d * rs + pad(t2)];
-    v = mmul<F>(v, omega_pow<F>(log_k, (uint32_t)((i1_0 + d) * t2)));
-    zc_[((int64_t)t2 << log_k1) + i1_0 + d] = v;
+    const int d = idx & (TI - 1), p = idx >> log_ti;
+    zc_[((int64_t)brev(p, log_k2) << log_k1) + i1_0 + d] = work[d * rs + pad(p)];
   }
 }
 
@@ -219,33 +244,53 @@ __global__ void __launch_bounds__(kThreads) k_lde_pass1(const uint32_t* x, uint3
                     sm);
 }
 
-// Pass 2 item (t2 tile, column c): all b cosets of TT rows.
+constexpr int kTwLoLog = 6;  // pass-2 twiddle tables: w^(t2 i1) = lo[i1 & 63] * hi[i1 >> 6]
+
+// Pass 2 item (t2 tile, column c): rows (s, t2) for all b cosets and TT
+// values of t2; each row is multiplied by w_k^(t2 i1), transformed by a
+// k1-point DIF NTT, and written to out[b (t2 + k2 t1) + s] (t1 = bit-reversed
+// position) in contiguous runs of b*TT words.
+// Layout: work[b*TT][rs] | tw[k1/2] | lo[TT][64] | hi[TT][k1/64].
 template <class F>
 __device__ void lde_pass2_body(const uint32_t* z, uint32_t* out, int log_k1, int log_k2,
                                int log_b, int log_tt, int tile, int64_t c, uint32_t* sm) {
-  const int k1 = 1 << log_k1, TT = 1 << log_tt, b = 1 << log_b;
+  const int k1 = 1 << log_k1, TT = 1 << log_tt;
   const int log_k = log_k1 + log_k2, log_n = log_k + log_b;
-  const int rows = b * TT;
-  const int rs = padded(k1);
+  const int log_rows = log_b + log_tt;
+  const int rs = row_stride(k1);
+  const int lo_n = k1 < (1 << kTwLoLog) ? k1 : (1 << kTwLoLog);
+  const int hi_n = k1 >> kTwLoLog > 0 ? k1 >> kTwLoLog : 1;
   uint32_t* work = sm;
-  uint32_t* tw = work + rows * rs;
+  uint32_t* tw = work + (rs << log_rows);
+  uint32_t* lo = tw + (k1 > 1 ? k1 / 2 : 1);
+  uint32_t* hi = lo + TT * lo_n;
   const int t2_0 = tile * TT;
   pow_table<F>(tw, k1 > 1 ? k1 / 2 : 1, log_k1 ? omega_pow<F>(log_k1, 1) : F::ONE);
-  const uint32_t* zc_ = z + (c << log_n);
-  for (int idx = threadIdx.x; idx < (rows << log_k1); idx += blockDim.x) {
-    const int i1 = idx & (k1 - 1), row = idx >> log_k1;
-    const int s = row >> log_tt, dt = row & (TT - 1);
-    const uint32_t v =
-        zc_[((int64_t)s << log_k) + ((int64_t)(t2_0 + dt) << log_k1) + i1];
-    work[row * rs + pad(brev(i1, log_k1))] = v;
+  for (int e = threadIdx.x; e < TT * (lo_n + hi_n); e += blockDim.x) {
+    const int dt = e / (lo_n + hi_n), r = e - dt * (lo_n + hi_n);
+    const uint32_t base = omega_pow<F>(log_k, (uint32_t)(t2_0 + dt));
+    if (r < lo_n)
+      lo[dt * lo_n + r] = mpow<F>(base, (uint64_t)r);
+    else
+      hi[dt * hi_n + (r - lo_n)] = mpow<F>(base, (uint64_t)(r - lo_n) << kTwLoLog);
   }
   __syncthreads();
-  smem_ntt<F>(work, rows, log_k1, rs, tw);
+  const uint32_t* zc_ = z + (c << log_n);
+  for (int idx = threadIdx.x; idx < (1 << (log_rows + log_k1)); idx += blockDim.x) {
+    const int i1 = idx & (k1 - 1), row = idx >> log_k1;
+    const int s = row >> log_tt, dt = row & (TT - 1);
+    uint32_t v = zc_[((int64_t)s << log_k) + ((int64_t)(t2_0 + dt) << log_k1) + i1];
+    v = mmul<F>(v, mmul<F>(lo[dt * lo_n + (i1 & (lo_n - 1))], hi[dt * hi_n + (i1 >> kTwLoLog)]));
+    work[row * rs + pad(i1)] = v;
+  }
+  __syncthreads();
+  smem_ntt_dif<F>(work, log_rows, log_k1, rs, tw);
   uint32_t* oc = out + (c << log_n);
-  for (int idx = threadIdx.x; idx < (rows << log_k1); idx += blockDim.x) {
-    const int s = idx & (b - 1), dt = (idx >> log_b) & (TT - 1), t1 = idx >> (log_b + log_tt);
-    const uint32_t v = work[((s << log_tt) + dt) * rs + pad(t1)];
-    oc[((int64_t)(t2_0 + dt + ((int64_t)t1 << log_k2)) << log_b) + s] = v;
+  for (int idx = threadIdx.x; idx < (1 << (log_rows + log_k1)); idx += blockDim.x) {
+    const int s = idx & ((1 << log_b) - 1), dt = (idx >> log_b) & (TT - 1);
+    const int p = idx >> (log_b + log_tt);
+    const uint32_t v = work[((s << log_tt) + dt) * rs + pad(p)];
+    oc[((int64_t)(t2_0 + dt + ((int64_t)brev(p, log_k1) << log_k2)) << log_b) + s] = v;
   }
 }
 
@@ -272,7 +317,7 @@ inline LdePlan plan_lde(int log_k, int log_b, int tile_log = 0) {
   const int k = 1 << log_k, b = 1 << log_b;
   const int tl = tile_log > 0 ? tile_log : kTileLog;
   p.small = log_k <= kSmallMaxLogK && log_k + log_b <= kSmallMaxLogN;
-  p.smem_small = 4 * ((size_t)b * padded(k) + (k > 1 ? k / 2 : 1) + k);
+  p.smem_small = 4 * ((size_t)b * row_stride(k) + (k > 1 ? k / 2 : 1) + k + 256);
   p.log_k2 = log_k / 2;
   p.log_k1 = log_k - p.log_k2;
   int ti = tl - p.log_k2;
@@ -285,9 +330,12 @@ inline LdePlan plan_lde(int log_k, int log_b, int tile_log = 0) {
   if (tt < 0) tt = 0;
   p.log_tt = tt;
   const int k1 = 1 << p.log_k1, k2 = 1 << p.log_k2;
-  p.smem1 = 4 * ((size_t)(1 << p.log_ti) * padded(k2) + (k2 > 1 ? k2 / 2 : 1) + k2 +
+  p.smem1 = 4 * ((size_t)(1 << p.log_ti) * row_stride(k2) + (k2 > 1 ? k2 / 2 : 1) + k2 +
                  (1 << p.log_ti));
-  p.smem2 = 4 * ((size_t)(b << p.log_tt) * padded(k1) + (k1 > 1 ? k1 / 2 : 1));
+  const int lo_n = k1 < (1 << kTwLoLog) ? k1 : (1 << kTwLoLog);
+  const int hi_n = (k1 >> kTwLoLog) > 0 ? (k1 >> kTwLoLog) : 1;
+  p.smem2 = 4 * ((size_t)(b << p.log_tt) * row_stride(k1) + (k1 > 1 ? k1 / 2 : 1) +
+                 ((size_t)1 << p.log_tt) * (lo_n + hi_n));
   return p;
 }
 
