@@ -47,7 +47,7 @@ def parse():
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["zorch", "reference"], default="zorch")
-    ap.add_argument("--workload", choices=["trace", "served"], default="trace")
+    ap.add_argument("--workload", choices=["trace", "served", "fri", "uneven"], default="served")
     ap.add_argument("--log-rows", type=int, default=20)
     ap.add_argument("--cols", type=int, default=64)
     ap.add_argument("--log-blowup", type=int, default=2)
@@ -166,6 +166,42 @@ def cpu_trace_sample(log_rows, cols, log_blowup, queries, threads=0, reps=1):
     return (cols << log_rows) / best, best, orc.threads()
 
 
+def cpu_served_sample(args, cap_log_h=12):
+    """The oracle on a bounded sample of the served stream: every request of
+    the seeded stream with its height capped at 2^cap_log_h rows -- LDE,
+    row-leaf Merkle commit, and for fold requests the partial-Lagrange
+    batching, EF4 fold rounds to 2^8 and 64 query openings."""
+    from oracle import oracle as orc
+    from zorch_gb300.serve import FOLD_FINAL_LOG, FOLD_QUERIES, make_stream
+
+    reqs = make_stream(args.requests, args.seed, rate_hz=args.rate,
+                       log_h=(args.min_log_h, args.max_log_h))
+    p2 = orc.Poseidon2.babybear16()
+    shift = int(orc.to_mont(0, np.array([31], np.uint32))[0])
+    rng = np.random.default_rng(11)
+    elements = 0
+    t0 = time.perf_counter()
+    for r in reqs:
+        lh = min(r.log_h, cap_log_h)
+        x = rng.integers(0, P, size=(r.width, 1 << lh), dtype=np.uint64).astype(np.uint32)
+        cw = orc.rs_encode(0, orc.to_mont(0, x), r.log_blowup, shift)
+        layers = orc.merkle_commit_columns(p2, cw)
+        elements += r.width << lh
+        if r.fold:
+            t = orc.Transcript(p2)
+            t.observe(layers[-1][0])
+            nbv = (r.width - 1).bit_length()
+            rlc = orc.rlc_columns(0, cw, t.sample(4 * nbv) if nbv else [])
+            rounds = max(lh + r.log_blowup - FOLD_FINAL_LOG, 0)
+            t.observe(orc.to_mont(0, np.array([rounds], np.uint32)))
+            if rounds:
+                proof = orc.fri_commit_phase(p2, 0, rlc, rounds, FOLD_QUERIES, 4, t, shift)
+                n = cw.shape[1]
+                orc.merkle_open(cw, n, r.width, 1, n, layers, proof.positions)
+    dt = time.perf_counter() - t0
+    return elements / dt, dt, orc.threads(), elements
+
+
 # ---------------------------------------------------------- workloads -----
 def trace_workload(args, device):
     import torch
@@ -261,6 +297,77 @@ def served_workload(args, device, rank):
     return reqs, served, plain, elements
 
 
+def fri_workload(args, device):
+    """Config 3: one 2^22-coefficient polynomial, blowup 2, FRI commit phase with
+    EF4 challenges down to 2^8 (15 rounds) and 100 query openings."""
+    import torch
+
+    from zorch_gb300.coding import ReedSolomon
+    from zorch_gb300.commit import MerkleTree, Poseidon2
+    from zorch_gb300.field import BABYBEAR, ptr, stream_handle, to_mont
+    from zorch_gb300.pcs import FriParams, FriProver
+    from zorch_gb300.transcript import DuplexTranscript
+    from zorch_gb300 import _lib
+
+    log_k = 22
+    perm = Poseidon2.builtin(BABYBEAR)
+    code = ReedSolomon(1 << log_k, 2, BABYBEAR, coset_shift=31, generator=31)
+    prover = FriProver(FriParams(code, MerkleTree(perm), 15, 100, 4))
+    x = torch.empty(1 << log_k, dtype=torch.int32, device=device)
+    _lib.check(_lib.lib().zc_fill_uniform(0, ptr(x), x.numel(), 3, stream_handle()), "fill")
+
+    pinned = x.cpu().pin_memory()
+
+    def run(e2e=False):
+        src = pinned.to(device, non_blocking=True) if e2e else x
+        cw = code.encode(to_mont(BABYBEAR, src))
+        proof, _, _ = prover.commit_phase(cw, DuplexTranscript.new(perm, device=device))
+        return proof
+
+    return run, 1 << log_k
+
+
+def uneven_workload(args, device):
+    """Config 4: 48 matrices, log2 heights 12..22, widths 1..128, blowup
+    2/4/8 (one seeded draw each): one batched commit vs 48 plain calls."""
+    import torch
+
+    from zorch_gb300.batch import Autotuner, BatchCommitter, MatrixJob
+    from zorch_gb300.coding import ReedSolomon
+    from zorch_gb300.commit import MerkleTree, Poseidon2
+    from zorch_gb300.field import BABYBEAR, ptr, stream_handle, to_mont
+    from zorch_gb300.pcs import BasefoldProver
+    from zorch_gb300 import _lib
+
+    rng = np.random.default_rng(args.seed)
+    shapes = [(int(rng.integers(1, 129)), int(rng.integers(12, 23)), int(rng.choice([1, 2, 3])))
+              for _ in range(48)]
+    mats = []
+    for i, (w, lh, lb) in enumerate(shapes):
+        xx = torch.empty((w, 1 << lh), dtype=torch.int32, device=device)
+        _lib.check(_lib.lib().zc_fill_uniform(0, ptr(xx), xx.numel(), 900 + i, stream_handle()),
+                   "fill")
+        mats.append((xx, lb))
+    perm = Poseidon2.builtin(BABYBEAR)
+    bc = BatchCommitter(perm, BABYBEAR, tuner=Autotuner())
+    tree = MerkleTree(perm, column_major=True)
+    elements = sum(w << lh for w, lh, _ in shapes)
+
+    def batched():
+        return bc.commit([MatrixJob(to_mont(BABYBEAR, x), lb) for x, lb in mats])
+
+    def plain():
+        roots = []
+        for x, lb in mats:
+            code = ReedSolomon(x.shape[1], 1 << lb, BABYBEAR, coset_shift=31, generator=31)
+            root, _ = BasefoldProver(code, tree).commit_columns(to_mont(BABYBEAR, x))
+            roots.append(root)
+            torch.cuda.synchronize()
+        return roots
+
+    return batched, plain, elements, shapes
+
+
 def pct(xs, q):
     return float(np.percentile(np.asarray(xs), q)) if len(xs) else None
 
@@ -331,6 +438,62 @@ def main():
     value = elems_total / (ms_max / 1e3)
     e2e_value = elems_total / e2e_s
     served_info = None
+    if args.workload == "fri":
+        run, elements = fri_workload(args, device)
+        for _ in range(max(args.warmup, 3)):
+            run()
+        torch.cuda.synchronize()
+        clocks = Clocks(local).start()
+        l0 = _lib.lib().zc_launch_count()
+        s0 = torch.cuda.Event(enable_timing=True)
+        s1 = torch.cuda.Event(enable_timing=True)
+        s0.record(stream)
+        for _ in range(args.steps):
+            proof = run()
+        s1.record(stream)
+        torch.cuda.synchronize()
+        clk = clocks.stop()
+        launches = _lib.lib().zc_launch_count() - l0
+        ms_max = max_over_ranks(s0.elapsed_time(s1), device)
+        value = elements * args.steps * world / (ms_max / 1e3)
+        e0 = time.perf_counter()
+        for _ in range(args.steps):
+            b = run(e2e=True).to_bytes()
+        e2e_value = elements * args.steps / max_over_ranks(time.perf_counter() - e0, device)
+        info["h2d_bytes"] = 4 * elements
+        info["d2h_bytes"] = len(b)
+        info["config"] = {"workload": "FRI commit phase: 2^22 coefficients, blowup 2, shift 31, "
+                                      "15 arity-2 rounds to 2^8 with EF4 challenges, 100 queries",
+                          "field": "babybear", "hash": "poseidon2-16 (built-in)",
+                          "l2": "inputs larger than L2 (32 MiB codeword x 2 + layers)"}
+    if args.workload == "uneven":
+        batched, plain, elements, shapes = uneven_workload(args, device)
+        for _ in range(2):
+            batched()
+        plain()
+        torch.cuda.synchronize()
+        clocks = Clocks(local).start()
+        l0 = _lib.lib().zc_launch_count()
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            batched()
+        torch.cuda.synchronize()
+        b_s = max_over_ranks(time.perf_counter() - t0, device)
+        clk = clocks.stop()
+        launches = _lib.lib().zc_launch_count() - l0
+        t0 = time.perf_counter()
+        plain()
+        p_s = max_over_ranks(time.perf_counter() - t0, device)
+        ms_max = b_s * 1e3
+        value = elements * args.steps * world / b_s
+        e2e_value = value
+        served_info = {"plain_per_matrix": {"value": elements / p_s, "unit": "elem/s",
+                                             "path": "48 BasefoldProver.commit calls, sync each"},
+                       "batched_over_plain": (elements * args.steps / b_s) / (elements / p_s),
+                       "elements_per_step": elements}
+        info["config"] = {"workload": "uneven batch: 48 matrices, log2 h 12..22, w 1..128, "
+                                      "blowup 2|4|8, one batched commit", "field": "babybear",
+                          "l2": "inputs larger than L2"}
     if args.workload == "served":
         reqs, served, plain, elements = served_workload(args, device, rank)
         for _ in range(max(args.warmup, 3)):
@@ -429,12 +592,18 @@ def main():
         "gpu_launches": int(launches),
     }
     if served_info is not None:
-        out["served"] = served_info
+        out["served" if args.workload == "served" else "batched"] = served_info
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
-        v, secs, thr = cpu_trace_sample(16, args.cols, args.log_blowup, args.queries, reps=1)
+        if args.workload == "served":
+            v, secs, thr, e = cpu_served_sample(args)
+            sample = (f"oracle C restatement on the served stream with heights capped at 2^12 "
+                      f"({e} elements, {secs:.2f} s)")
+        else:
+            v, secs, thr = cpu_trace_sample(16, args.cols, args.log_blowup, args.queries, reps=1)
+            sample = (f"oracle C restatement, 2^16 x {args.cols} slice of the trace workload "
+                      f"({secs:.2f} s)")
         out["cpu_baseline"] = {"value": v, "unit": "elem/s", "cores": thr, "kind": "port",
-                               "sample": f"oracle C restatement, 2^16 x {args.cols} slice of the "
-                                         f"trace workload ({secs:.2f} s)"}
+                               "sample": sample}
     if rank == 0:
         print(json.dumps(out), flush=True)
     if world > 1:
@@ -449,14 +618,23 @@ def reference_arm(args, rank, world):
     if rank != 0:
         return
     log_rows = 16
+    served = args.workload == "served"
     for _ in range(max(args.warmup, 1)):
-        cpu_trace_sample(12, args.cols, args.log_blowup, args.queries)
-    vals, secs = [], 0.0
+        if served:
+            cpu_served_sample(args, cap_log_h=10)
+        else:
+            cpu_trace_sample(12, args.cols, args.log_blowup, args.queries)
+    vals, secs, elems = [], 0.0, 0
     for _ in range(args.steps):
-        v, s, thr = cpu_trace_sample(log_rows, args.cols, args.log_blowup, args.queries)
+        if served:
+            v, s, thr, e = cpu_served_sample(args)
+        else:
+            v, s, thr = cpu_trace_sample(log_rows, args.cols, args.log_blowup, args.queries)
+            e = args.cols << log_rows
         vals.append(v)
         secs += s
-    value = len(vals) * (args.cols << log_rows) / secs
+        elems += e
+    value = elems / secs
     out = {
         "impl": "reference",
         "metric": METRIC,
@@ -471,12 +649,16 @@ def reference_arm(args, rank, world):
         "vs_baseline": None,
         "dtype": "u32 (BabyBear, Montgomery)",
         "data": "synthetic: seeded uniform [0, p) canonical BabyBear elements",
-        "config": {"workload": f"trace commit 2^{log_rows}x{args.cols} slice, blowup "
-                               f"{1 << args.log_blowup}, row leaves, {args.queries} openings"},
+        "config": {"workload": (f"served stream sample: the {args.requests}-request stream with "
+                                "heights capped at 2^12" if served else
+                                f"trace commit 2^{log_rows}x{args.cols} slice, blowup "
+                                f"{1 << args.log_blowup}, row leaves, {args.queries} openings")},
         "cpu_baseline": {"value": value, "unit": "elem/s", "cores": thr, "kind": "port",
-                         "sample": f"2^{log_rows} x {args.cols} per step; the reference is Python "
-                                   "over FRX/hash-frx wheels absent here, so its C restatement "
-                                   "(oracle/) runs instead"},
+                         "sample": ("each step: every request of the served stream, height capped "
+                                    "at 2^12, incl. fold-and-open" if served else
+                                    f"2^{log_rows} x {args.cols} per step") +
+                                   "; the reference is Python over FRX/hash-frx wheels absent "
+                                   "here, so its C restatement (oracle/) runs instead"},
         "e2e": {"value": value, "unit": "elem/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(out), flush=True)

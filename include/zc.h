@@ -96,6 +96,10 @@ zc_status zc_poseidon2_destroy(zc_poseidon2* p);
 zc_status zc_poseidon2_permute(const zc_poseidon2* p, uint32_t* states, int64_t count,
                                void* stream);
 
+/* The same permutation on the calling CPU thread over host memory (for
+ * verifiers: MerkleTree.reconstruct_root / verify, zorch/commit/merkle.py:264-331). */
+zc_status zc_poseidon2_permute_host(const zc_poseidon2* p, uint32_t* states, int64_t count);
+
 /* ---- Reed-Solomon coset LDE ------------------------------------------ */
 /* Replaces ReedSolomon.encode (zorch/coding/reed_solomon.py:177-188):
  * out[b, j] = sum_i coeffs[b, i] * (shift * w^j)^i for j < 2^(log_k+log_blowup),

@@ -47,3 +47,23 @@ def test_workspace_sizes():
     assert L.zc_rs_encode_workspace_bytes(3, 10, 2) == 0  # single pass
     assert L.zc_rs_encode_workspace_bytes(2, 16, 1) == 2 * 4 * (1 << 17)
     assert L.zc_rs_encode_workspace_bytes(64, 20, 2) == 1 << 30  # capped chunk
+
+
+def test_host_permutation_matches_oracle(orc):
+    """The host form of the permutation (no GPU needed) equals the oracle's,
+    for the built-in BabyBear instance and the golden KoalaBear instance."""
+    import numpy as np
+
+    from zorch_gb300.commit import Poseidon2, koalabear16_params
+
+    try:
+        bb = Poseidon2.builtin()
+    except Exception:  # creating a handle needs a CUDA context
+        import pytest
+
+        pytest.skip("no CUDA device for the handle's device copy")
+    kb = koalabear16_params(orc.load_koalabear_fixture())
+    for gpu, cpu, f in ((bb, orc.Poseidon2.babybear16(), 0),
+                        (kb, orc.Poseidon2.koalabear16_golden(), 1)):
+        st = orc.to_mont(f, np.arange(16 * 5, dtype=np.uint32).reshape(5, 16))
+        assert np.array_equal(gpu.permute_host(st), np.stack([cpu.permute(s) for s in st]))

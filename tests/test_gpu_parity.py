@@ -303,3 +303,26 @@ def test_config1_plain_commit(orc, perms):
     cw_o = orc.rs_encode(0, orc.to_mont(0, coeffs_c), 1, BABYBEAR.mont(31))
     assert np.array_equal(to_host(cw), cw_o)
     assert np.array_equal(to_host(root), orc.merkle_commit_rows(cpu, cw_o.reshape(-1, 1))[-1][0])
+
+
+def test_merkle_verify_roundtrip_and_tamper(orc, perms):
+    """open -> verify (zorch/commit/merkle.py:327-331), a tampered sibling or
+    row fails, an out-of-range index is rejected."""
+    from zorch_gb300.commit import MerkleTree, Opening
+
+    for which in ("bb", "kb"):
+        gpu, _, f = perms[which]
+        m = dev(rand_mont(orc, f, (64, 9), 17)).reshape(64, 9)
+        tree = MerkleTree(gpu)
+        root, layers = tree.commit(m)
+        for i in (0, 1, 37, 63):
+            op = tree.open(m, layers, i)
+            assert tree.verify(root, i, op)
+        op = tree.open(m, layers, 5)
+        bad_path = op.path.clone()
+        bad_path[3, 0] ^= 1
+        assert not tree.verify(root, 5, Opening(op.row, bad_path))
+        bad_row = op.row.clone()
+        bad_row[0] ^= 1
+        assert not tree.verify(root, 5, Opening(bad_row, op.path))
+        assert not tree.verify(root, 64, op)

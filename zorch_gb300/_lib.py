@@ -63,6 +63,7 @@ def _declare(lib: C.CDLL) -> None:
                                      C.POINTER(vp)]),
         "zc_poseidon2_destroy": (st, [vp]),
         "zc_poseidon2_permute": (st, [vp, vp, i64, vp]),
+        "zc_poseidon2_permute_host": (st, [vp, vp, i64]),
         "zc_rs_encode_workspace_bytes": (sz, [i64, C.c_int, C.c_int]),
         "zc_rs_encode": (st, [st, vp, i64, C.c_int, C.c_int, u32, u32, vp, vp, sz, vp]),
         "zc_rs_encode_noalloc": (st, [st, vp, i64, C.c_int, C.c_int, u32, u32, vp, vp]),

@@ -64,6 +64,27 @@ class Poseidon2:
                                                    stream_handle()), "poseidon2_permute")
         return s
 
+    def permute_host(self, states: np.ndarray) -> np.ndarray:
+        """Permute [count, 16] host states on the CPU (a copy is returned)."""
+        s = np.ascontiguousarray(np.asarray(states, np.uint32)).copy()
+        _lib.check(_lib.lib().zc_poseidon2_permute_host(self._h, s.ctypes.data, s.size // 16),
+                   "poseidon2_permute_host")
+        return s
+
+    def hash_host(self, row) -> np.ndarray:
+        """PaddingFreeSponge<16, 8, 8> on the CPU."""
+        row = np.asarray(row, np.uint32).reshape(-1)
+        st = np.zeros(16, np.uint32)
+        for i in range(0, row.size, 8):
+            blk = row[i: i + 8]
+            st[: blk.size] = blk
+            st = self.permute_host(st)
+        return st[:8].copy()
+
+    def compress_host(self, left, right) -> np.ndarray:
+        st = np.concatenate([np.asarray(left, np.uint32), np.asarray(right, np.uint32)])
+        return self.permute_host(st)[:8].copy()
+
     def __del__(self) -> None:
         if getattr(self, "_owned", False) and self._h:
             try:
@@ -187,6 +208,27 @@ class MerkleTree:
         m = matrix.contiguous()
         lv = leaves_layout(m, m.shape[0], 1, m.shape[1], 0)
         return self.open_layout(lv, layers, indices, m.shape[1])
+
+    def reconstruct_root(self, index: int, opening: Opening) -> np.ndarray:
+        """Rebuild the raw root from an opening's row and leaf-first path
+        (zorch/commit/merkle.py:264-285), on the host."""
+        node = self.perm.hash_host(opening.row.detach().cpu().numpy().view(np.uint32))
+        path = opening.path.detach().cpu().numpy().view(np.uint32)
+        idx = int(index)
+        for sib in path.reshape(-1, 8):
+            node = self.perm.compress_host(node, sib) if idx % 2 == 0 else \
+                self.perm.compress_host(sib, node)
+            idx //= 2
+        return node
+
+    def verify(self, root: torch.Tensor, index: int, opening: Opening) -> bool:
+        """zorch/commit/merkle.py:327-331: out-of-range indices are rejected,
+        else the rebuilt root must equal the committed one."""
+        depth = opening.path.reshape(-1, 8).shape[0]
+        if not 0 <= int(index) < (1 << depth):
+            return False
+        want = root.detach().cpu().numpy().view(np.uint32).reshape(-1)
+        return bool(np.array_equal(self.reconstruct_root(index, opening), want))
 
     def open(self, matrix: torch.Tensor, layers: DigestLayers, index: int) -> Opening:
         if not 0 <= int(index) < matrix.shape[0]:

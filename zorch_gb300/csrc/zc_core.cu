@@ -331,6 +331,17 @@ zc_status zc_from_mont(zc_field field, const uint32_t* in, uint32_t* out, int64_
   return convert(field, in, out, n, 0, stream);
 }
 
+zc_status zc_poseidon2_permute_host(const zc_poseidon2* p, uint32_t* states, int64_t count) {
+  if (!p || (!states && count > 0) || count < 0) return ZC_BAD_ARG;
+  for (int64_t i = 0; i < count; i++) {
+    if (p->field == ZC_FIELD_BABYBEAR)
+      p2_permute(states + 16 * i, RtParams<BabyBear>{&p->host});
+    else
+      p2_permute(states + 16 * i, RtParams<KoalaBear>{&p->host});
+  }
+  return ZC_OK;
+}
+
 zc_status zc_duplex_step(const zc_poseidon2* p, uint32_t* state, const uint32_t* values,
                          int64_t m, int32_t n, uint32_t* out, int32_t* positions,
                          int64_t block_len, void* stream) {
