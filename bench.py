@@ -558,7 +558,11 @@ def main():
     # Hash kernel (dominant): integer instructions executed per Poseidon2
     # permutation of the built-in BabyBear-16 instance, from the ncu capture
     # summarised in profiles/ (thread-level SASS instructions).
-    inst_per_perm = float(os.environ.get("ZC_INST_PER_PERM", "7200"))
+    inst_per_perm = float(os.environ.get("ZC_INST_PER_PERM", "7128"))
+    # DRAM bytes per hashed LDE word of the k_leaf launch (134.34 MB read +
+    # 8.54 MB written for 2^19 leaves x 64 words, profiles/), scaled to this
+    # workload's leaf launch by its word count.
+    traffic_per_word = (134.341376e6 + 8.544e6) / float(1 << 25)
     perms = info["perms_leaf"] + info["perms_node"]
     int_peak = 152 * 128 * sm_mhz * 1e6 / 1e9  # Ginst/s: 152 SMs x 128 lanes x clock
     achieved = perms * inst_per_perm / (hash_ms / 1e3) / 1e9
@@ -579,9 +583,12 @@ def main():
         "config": info["config"] | {"parallelism": f"replicas x{world}"},
         "e2e": {"value": e2e_value, "unit": "elem/s", "h2d_bytes_per_step": info["h2d_bytes"],
                 "d2h_bytes_per_step": info["d2h_bytes"]},
-        "roofline": {"bound": "int32", "kernel": "merkle leaf/subtree Poseidon2 (k_subtree)",
+        "roofline": {"bound": "int32",
+                     "kernel": "Poseidon2 Merkle hashing (k_leaf leaves + levels + fused top)",
                      "achieved": achieved, "peak": int_peak, "unit": "Ginst/s",
-                     "frac": achieved / int_peak, "traffic": None,
+                     "frac": achieved / int_peak,
+                     "traffic": traffic_per_word * info["leaves"] * args.cols,
+                     "traffic_note": "bytes per launch, scaled from the 2^19 x 64 ncu capture",
                      "peak_source": "152 SMs x 128 INT32 lanes x sm_max_mhz (MEASURED_PEAKS.json)",
                      "ms": hash_ms, "perms": perms},
         "roofline_ntt": {"bound": "hbm", "kernel": "coset LDE (k_lde_pass1+pass2)",

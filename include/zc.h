@@ -80,6 +80,11 @@ zc_status zc_to_mont(zc_field field, const uint32_t* in, uint32_t* out, int64_t 
 zc_status zc_from_mont(zc_field field, const uint32_t* in, uint32_t* out, int64_t n,
                        void* stream);
 
+/* out[i] = in[i] * s (Montgomery scalar): the 1/n of an inverse NTT
+ * (lax.ntt INTT, used by ReedSolomon.extend, zorch/coding/reed_solomon.py:190-208). */
+zc_status zc_scale(zc_field field, const uint32_t* in, uint32_t* out, int64_t n, uint32_t s_mont,
+                   void* stream);
+
 /* ---- Poseidon2 parameters -------------------------------------------- */
 /* The built-in BabyBear width-16 instance (x^7, 4+4 full, 13 partial rounds).
  * The reference ships no BabyBear instance; see gen_poseidon2_babybear16.py. */

@@ -326,3 +326,59 @@ def test_merkle_verify_roundtrip_and_tamper(orc, perms):
         bad_row[0] ^= 1
         assert not tree.verify(root, 5, Opening(bad_row, op.path))
         assert not tree.verify(root, 64, op)
+
+
+def _dft_inverse(orc, f, evals):
+    """O(k^2) inverse DFT with the oracle's field ops (independent of any NTT)."""
+    k = len(evals)
+    w = orc.root_of_unity(f, k.bit_length() - 1)
+    p = orc.MODULUS[f]
+    winv = orc.to_mont(f, [pow(int(orc.from_mont(f, [w])[0]), p - 2, p)])[0]
+    kinv = orc.to_mont(f, [pow(k, p - 2, p)])[0]
+    out = []
+    for i in range(k):
+        acc = 0
+        x = int(orc.to_mont(f, [1])[0])
+        step = int(orc.to_mont(f, [1])[0])
+        for _ in range(i):
+            step = orc.LIB.orc_mul(f, step, int(winv))
+        for j in range(k):
+            acc = (acc + orc.LIB.orc_mul(f, int(evals[j]), x)) % p
+            x = orc.LIB.orc_mul(f, x, step)
+        out.append(orc.LIB.orc_mul(f, acc, int(kinv)))
+    return np.array(out, np.uint32)
+
+
+@pytest.mark.parametrize("k,blowup,shift", [(4, 2, None), (8, 4, 7), (16, 2, 3), (64, 2, 31)])
+def test_extend_matches_coset_polynomial_evaluation(orc, k, blowup, shift):
+    """reed_solomon_test.py:179-199: extend(evals) == Horner(INTT(evals)) on the
+    (coset) domain, with INTT by an independent O(k^2) inverse DFT."""
+    from zorch_gb300.coding import ReedSolomon
+
+    evals = rand_mont(orc, 0, k, k + blowup)
+    rs = ReedSolomon(k, blowup, BABYBEAR, coset_shift=shift)
+    got = to_host(rs.extend(dev(evals)))
+    coeffs = _dft_inverse(orc, 0, evals)
+    sh = BABYBEAR.mont(shift) if shift else 0
+    assert np.array_equal(got, orc.rs_encode_horner(0, coeffs, blowup.bit_length() - 1, sh))
+    if shift is None:  # the LDE agrees with the evaluations on the base subgroup
+        assert np.array_equal(got[::blowup], evals)
+
+
+def test_codeword_is_low_degree_and_ef4_encode(orc):
+    """reed_solomon_test.py:211-217 (INTT of a codeword has zero top
+    coefficients) and :247-253 (EF4 messages encode limb by limb)."""
+    from zorch_gb300.coding import ReedSolomon, intt
+
+    k, blowup = 8, 2
+    rs = ReedSolomon(k, blowup, BABYBEAR)
+    coeffs = rand_mont(orc, 0, k, 2)
+    rec = to_host(intt(BABYBEAR, rs.encode(dev(coeffs))))
+    assert np.array_equal(rec[:k], coeffs) and not rec[k:].any()
+    rsc = ReedSolomon(k, blowup, BABYBEAR, coset_shift=3)
+    msg = rand_mont(orc, 0, (3, k, 4), 25)
+    cw = to_host(rsc.encode(dev(msg).reshape(3, k, 4), ef4=True))
+    for r in range(3):
+        for e in range(4):
+            want = orc.rs_encode(0, msg[r, :, e], 1, BABYBEAR.mont(3))
+            assert np.array_equal(cw[r, :, e], want)

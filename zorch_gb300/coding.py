@@ -42,6 +42,24 @@ def rs_encode(field: Field, message: torch.Tensor, log_blowup: int, shift_mont: 
     return out
 
 
+def ntt(field, x: torch.Tensor, generator: int = 0) -> torch.Tensor:
+    """Forward NTT over the last axis, natural order in and out (lax.ntt NTT)."""
+    return rs_encode(field_of(field), x, 0, 0, generator)
+
+
+def intt(field, x: torch.Tensor, generator: int = 0) -> torch.Tensor:
+    """Inverse NTT over the last axis (lax.ntt INTT): (1/k) * NTT(x)[-i mod k]."""
+    f = field_of(field)
+    k = x.shape[-1]
+    y = ntt(f, x, generator)
+    rev = torch.remainder(-torch.arange(k, device=x.device), k)
+    y = y.index_select(-1, rev).contiguous()
+    out = torch.empty_like(y)
+    _lib.check(_lib.lib().zc_scale(f.id, ptr(y), ptr(out), y.numel(), f.inv_mont(f.mont(k)),
+                                   stream_handle()), "scale")
+    return out
+
+
 def eval_domain(field, n: int, *, shift: int | None = None, generator: int | None = None,
                 device="cuda") -> torch.Tensor:
     """[shift * w^j] in NTT order (zorch/coding/reed_solomon.py:49-68), read off
@@ -97,12 +115,30 @@ class ReedSolomon:
     def log_blowup(self) -> int:
         return _log2(self.blowup)
 
-    def encode(self, message: torch.Tensor, out: torch.Tensor | None = None) -> torch.Tensor:
+    def encode(self, message: torch.Tensor, out: torch.Tensor | None = None, *,
+               ef4: bool = False) -> torch.Tensor:
+        """Coset LDE of the last axis. `ef4=True`: the message is EF4 with the 4
+        coefficients on a trailing axis ([..., k, 4]); the base-field roots make
+        the transform act limb by limb, as lax.ntt decomposes extension fields."""
+        if ef4:
+            if message.shape[-1] != 4:
+                raise ValueError("an EF4 message needs a trailing axis of 4 limbs")
+            limbs = message.movedim(-1, -2).contiguous()  # [..., 4, k]
+            cw = self.encode(limbs)
+            return cw.movedim(-2, -1).contiguous()
         if message.shape[-1] != self.message_len:
             raise ValueError(f"message last axis must be {self.message_len}, "
                              f"got {message.shape[-1]}")
         return rs_encode(self.field, message, self.log_blowup, self._shift_mont,
                          self.generator or 0, out)
+
+    def extend(self, evals: torch.Tensor) -> torch.Tensor:
+        """LDE of the base-subgroup evaluations to the block-length (coset)
+        codeword: encode(INTT(evals)) (zorch/coding/reed_solomon.py:190-208)."""
+        if evals.shape[-1] != self.message_len:
+            raise ValueError(f"evals last axis must be {self.message_len}, "
+                             f"got {evals.shape[-1]}")
+        return self.encode(intt(self.field, evals, self.generator or 0))
 
     def domain(self) -> torch.Tensor:
         return eval_domain(self.field, self.block_len, shift=self.coset_shift,

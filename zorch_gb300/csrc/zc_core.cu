@@ -160,6 +160,13 @@ __global__ void k_convert(const uint32_t* in, uint32_t* out, int64_t n, int to) 
     out[i] = to ? to_mont<F>(in[i]) : from_mont<F>(in[i]);
 }
 
+template <class F>
+__global__ void k_scale(const uint32_t* in, uint32_t* out, int64_t n, uint32_t s) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x)
+    out[i] = mmul<F>(in[i], s);
+}
+
 template <class K>
 __global__ void k_permute(const P2Params* rt, uint32_t* states, int64_t count) {
   __shared__ P2Params s_rt;
@@ -340,6 +347,20 @@ zc_status zc_poseidon2_permute_host(const zc_poseidon2* p, uint32_t* states, int
       p2_permute(states + 16 * i, RtParams<KoalaBear>{&p->host});
   }
   return ZC_OK;
+}
+
+zc_status zc_scale(zc_field field, const uint32_t* in, uint32_t* out, int64_t n, uint32_t s_mont,
+                   void* stream) {
+  if (!in || !out || n < 0) return ZC_BAD_ARG;
+  if (n == 0) return ZC_OK;
+  cudaStream_t st = (cudaStream_t)stream;
+  return with_field(field, [&](auto f) {
+    using F = decltype(f);
+    int64_t blocks = (n + 255) / 256;
+    if (blocks > 152 * 16) blocks = 152 * 16;
+    k_scale<F><<<(unsigned)blocks, 256, 0, st>>>(in, out, n, s_mont);
+    return launch_check();
+  });
 }
 
 zc_status zc_duplex_step(const zc_poseidon2* p, uint32_t* state, const uint32_t* values,
