@@ -220,25 +220,11 @@ __device__ void lde_pass1_body(const uint32_t* x, uint32_t* z, int log_k1, int l
   for (int i = threadIdx.x; i < TI; i += blockDim.x) gi[i] = mpow<F>(gs, (uint64_t)(i1_0 + i));
   __syncthreads();
   const uint32_t* xc = x + (c << log_k);
-  // four independent loads in flight per thread before any is consumed
-  const int total = TI << log_k2, step = blockDim.x;
-  for (int idx0 = threadIdx.x; idx0 < total; idx0 += 4 * step) {
-    uint32_t v[4];
-#pragma unroll
-    for (int u = 0; u < 4; u++) {
-      const int idx = idx0 + u * step;
-      v[u] = idx < total ? __ldg(xc + i1_0 + (idx & (TI - 1)) +
-                                 ((int64_t)(idx >> log_ti) << log_k1))
-                         : 0u;
-    }
-#pragma unroll
-    for (int u = 0; u < 4; u++) {
-      const int idx = idx0 + u * step;
-      if (idx < total) {
-        const int d = idx & (TI - 1), i2 = idx >> log_ti;
-        work[d * rs + pad(i2)] = mmul<F>(mmul<F>(v[u], gi[d]), R[i2]);
-      }
-    }
+  for (int idx = threadIdx.x; idx < (TI << log_k2); idx += blockDim.x) {
+    const int d = idx & (TI - 1), i2 = idx >> log_ti;
+    uint32_t v = __ldg(xc + i1_0 + d + ((int64_t)i2 << log_k1));
+    v = mmul<F>(mmul<F>(v, gi[d]), R[i2]);
+    work[d * rs + pad(i2)] = v;
   }
   __syncthreads();
   smem_ntt_dif<F>(work, log_ti, log_k2, rs, tw);
@@ -290,27 +276,12 @@ __device__ void lde_pass2_body(const uint32_t* z, uint32_t* out, int log_k1, int
   }
   __syncthreads();
   const uint32_t* zc_ = z + (c << log_n);
-  const int total = 1 << (log_rows + log_k1), step = blockDim.x;
-  for (int idx0 = threadIdx.x; idx0 < total; idx0 += 4 * step) {
-    uint32_t v[4];
-#pragma unroll
-    for (int u = 0; u < 4; u++) {
-      const int idx = idx0 + u * step;
-      const int i1 = idx & (k1 - 1), row = idx >> log_k1;
-      v[u] = idx < total ? __ldg(zc_ + ((int64_t)(row >> log_tt) << log_k) +
-                                 ((int64_t)(t2_0 + (row & (TT - 1))) << log_k1) + i1)
-                         : 0u;
-    }
-#pragma unroll
-    for (int u = 0; u < 4; u++) {
-      const int idx = idx0 + u * step;
-      if (idx < total) {
-        const int i1 = idx & (k1 - 1), row = idx >> log_k1, dt = row & (TT - 1);
-        const uint32_t tw2 =
-            mmul<F>(lo[dt * lo_n + (i1 & (lo_n - 1))], hi[dt * hi_n + (i1 >> kTwLoLog)]);
-        work[row * rs + pad(i1)] = mmul<F>(v[u], tw2);
-      }
-    }
+  for (int idx = threadIdx.x; idx < (1 << (log_rows + log_k1)); idx += blockDim.x) {
+    const int i1 = idx & (k1 - 1), row = idx >> log_k1;
+    const int s = row >> log_tt, dt = row & (TT - 1);
+    uint32_t v = zc_[((int64_t)s << log_k) + ((int64_t)(t2_0 + dt) << log_k1) + i1];
+    v = mmul<F>(v, mmul<F>(lo[dt * lo_n + (i1 & (lo_n - 1))], hi[dt * hi_n + (i1 >> kTwLoLog)]));
+    work[row * rs + pad(i1)] = v;
   }
   __syncthreads();
   smem_ntt_dif<F>(work, log_rows, log_k1, rs, tw);
