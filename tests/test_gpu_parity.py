@@ -382,3 +382,22 @@ def test_codeword_is_low_degree_and_ef4_encode(orc):
         for e in range(4):
             want = orc.rs_encode(0, msg[r, :, e], 1, BABYBEAR.mont(3))
             assert np.array_equal(cw[r, :, e], want)
+
+
+def test_graphed_fri_commit_phase_equals_eager(orc, perms):
+    """The CUDA-graph replay of encode + commit phase gives the eager bytes
+    for two different inputs in a row."""
+    from zorch_gb300.coding import ReedSolomon
+    from zorch_gb300.commit import MerkleTree
+    from zorch_gb300.pcs import FriParams, FriProver, GraphedFriCommitPhase
+    from zorch_gb300.transcript import DuplexTranscript
+
+    gpu, _, _ = perms["bb"]
+    code = ReedSolomon(1 << 12, 2, BABYBEAR, coset_shift=31, generator=31)
+    prover = FriProver(FriParams(code, MerkleTree(gpu), 9, 40, 4))
+    g = GraphedFriCommitPhase(prover)
+    for seed in (1, 2):
+        coeffs = dev(rand_mont(orc, 0, 1 << 12, 700 + seed))
+        got = g.replay(coeffs).to_bytes()
+        eager, _, _ = prover.commit_phase(code.encode(coeffs), DuplexTranscript.new(gpu))
+        assert got == eager.to_bytes()

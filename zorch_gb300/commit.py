@@ -188,7 +188,10 @@ class MerkleTree:
         return self.commit_layout(self._layout(matrix), matrix.device)
 
     def open_layout(self, lv: _lib.Leaves, layers: DigestLayers, indices: torch.Tensor,
-                    width: int) -> Opening:
+                    width: int, check: bool = True) -> Opening:
+        """Batched openings. `check` reads the device out-of-range flag back
+        (a host synchronisation); callers whose indices are in range by
+        construction, or that are being captured into a CUDA graph, pass False."""
         idx = indices.to(torch.int32).contiguous()
         q = idx.numel()
         rows = torch.empty((q, width), dtype=torch.int32, device=idx.device)
@@ -197,7 +200,7 @@ class MerkleTree:
         _lib.check(_lib.lib().zc_merkle_open(lv, ptr(layers.flat), ptr(idx), q, ptr(rows),
                                              ptr(paths), ptr(flag), stream_handle()),
                    "merkle_open")
-        if int(flag.item()):
+        if check and not torch.cuda.is_current_stream_capturing() and int(flag.item()):
             raise IndexError(f"leaf index out of range [0, {lv.num_leaves})")
         return Opening(rows, paths)
 

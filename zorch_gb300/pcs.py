@@ -127,10 +127,10 @@ def fold_rounds(rnd, state, transcript, rounds: int):
 
 
 def open_layer(tree: MerkleTree, layer: CommittedLayer, indices: torch.Tensor) -> Opening:
-    """open_rows over a layer's pair leaves (zorch/pcs/fold.py:142-149)."""
-    n = layer.codeword.shape[0]
+    """open_rows over a layer's pair leaves (zorch/pcs/fold.py:142-149); the
+    indices are reduced mod the layer's leaf count, so no range check."""
     return tree.open_layout(pair_layout(layer.codeword), layer.digest_layers, indices,
-                            2 * layer.limbs)
+                            2 * layer.limbs, check=False)
 
 
 @dataclass
@@ -259,3 +259,35 @@ class BasefoldProver:
         K, n = data.codeword.shape
         return self.tree.open_layout(leaves_layout(data.codeword, n, K, 1, n),
                                      data.digest_layers, indices, K)
+
+
+class GraphedFriCommitPhase:
+    """The encode + FRI commit phase of one polynomial shape captured once into
+    a CUDA graph: every round's fused fold-and-commit, the device transcript
+    steps and the query openings replay with one launch. The transcript starts
+    from the empty state; `replay(coeffs)` copies new Montgomery coefficients
+    into the static input and returns the (static) proof tensors, overwritten
+    by each replay."""
+
+    def __init__(self, prover: FriProver, device="cuda") -> None:
+        self.prover = prover
+        code = prover.params.code
+        self.coeffs = torch.zeros(code.message_len, dtype=torch.int32, device=device)
+        self._run()  # kernel attributes, allocator warm-up
+        torch.cuda.synchronize()
+        self.graph = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(self.graph):
+            self.proof = self._run()
+
+    def _run(self) -> CommitPhaseProof:
+        code = self.prover.params.code
+        cw = code.encode(self.coeffs)
+        t = DuplexTranscript.new(self.prover.params.tree.perm, device=self.coeffs.device)
+        proof, _, _ = self.prover.commit_phase(cw, t)
+        return proof
+
+    def replay(self, coeffs: torch.Tensor | None = None) -> CommitPhaseProof:
+        if coeffs is not None:
+            self.coeffs.copy_(coeffs, non_blocking=True)
+        self.graph.replay()
+        return self.proof
