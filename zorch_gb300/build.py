@@ -40,7 +40,13 @@ def _deps() -> list[Path]:
 
 
 def build(force: bool = False, verbose: bool = False, extra: list[str] | None = None) -> Path:
-    if LIB.exists() and not force and not extra:
+    """Compile libzc.so; `extra` (or the ZC_NVCC_FLAGS environment variable)
+    adds nvcc flags, e.g. -DZC_MU_SHIFT. A change of flags forces a rebuild."""
+    extra = list(extra or []) + os.environ.get("ZC_NVCC_FLAGS", "").split()
+    stamp = OUT_DIR / "flags.txt"
+    flags_id = " ".join(extra)
+    same_flags = stamp.exists() and stamp.read_text() == flags_id
+    if LIB.exists() and not force and same_flags:
         newest = max(d.stat().st_mtime for d in _deps())
         if LIB.stat().st_mtime >= newest:
             return LIB
@@ -68,6 +74,7 @@ def build(force: bool = False, verbose: bool = False, extra: list[str] | None = 
     if r.returncode != 0:
         raise RuntimeError(f"link failed:\n{r.stderr}")
     os.replace(tmp, LIB)
+    stamp.write_text(flags_id)
     return LIB
 
 
