@@ -118,6 +118,15 @@ zc_status zc_rs_encode(zc_field field, const uint32_t* coeffs, int64_t batch, in
                        uint32_t* out, void* workspace, size_t workspace_bytes,
                        void* stream);
 
+/* Replaces BitReversedReedSolomon.encode (zorch/coding/reed_solomon.py:476-478):
+ * the codeword of zc_rs_encode with each row in bit-reversed order,
+ * out[b, brev(j)] = sum_i coeffs[b, i] * (shift * w^j)^i, so the fold pairs
+ * (2p, 2p+1) are adjacent. Arguments, workspace and errors as zc_rs_encode. */
+zc_status zc_rs_encode_bitrev(zc_field field, const uint32_t* coeffs, int64_t batch, int log_k,
+                              int log_blowup, uint32_t shift_mont, uint32_t generator,
+                              uint32_t* out, void* workspace, size_t workspace_bytes,
+                              void* stream);
+
 /* The LDE of zc_rs_encode without any device allocation and without a
  * caller workspace: no counterpart in the reference. For callers that cannot
  * allocate device memory at call time -- a handler inside an XLA/FRX custom
@@ -155,6 +164,7 @@ typedef struct {
   int32_t log_blowup;
   uint32_t shift_mont;    /* 0: no coset */
   int32_t tile_log;       /* 0: default */
+  int32_t bit_reversed;   /* 1: bit-reversed codeword (zc_rs_encode_bitrev) */
 } zc_lde_job;
 size_t zc_rs_encode_batch_workspace_bytes(const zc_lde_job* jobs, int32_t njobs);
 zc_status zc_rs_encode_batch(zc_field field, const zc_lde_job* jobs, int32_t njobs,
@@ -206,6 +216,28 @@ zc_status zc_fri_fold_commit(const zc_poseidon2* p, const uint32_t* cw, int64_t 
                              const uint32_t* beta, int ef_beta, uint32_t shift_mont,
                              uint32_t generator, uint32_t* out, uint32_t* next_layers,
                              void* stream);
+
+/* Replaces BitReversedReedSolomon.fold (zorch/coding/reed_solomon.py:484-492,
+ * 532-540) on a bit-reversed layer: out[p] folds the adjacent pair
+ * (cw[2p], cw[2p+1]) at x_p = shift_mont * w_n^brev(p) (p read over
+ * log2(n/2) bits); the output is the next layer, again bit-reversed.
+ * Arguments as zc_fri_fold. */
+zc_status zc_fri_fold_bitrev(zc_field field, const uint32_t* cw, int64_t n, int ef_in,
+                             const uint32_t* beta, int ef_beta, uint32_t shift_mont,
+                             uint32_t generator, uint32_t* out, void* stream);
+/* zc_fri_fold_bitrev fused with the commit of the folded layer as the SP1
+ * stacked open commits it (zorch/pcs/jagged/open.py:270-282): leaf p of
+ * next_layers is out[2p] || out[2p+1] in base limbs (n/4 leaves). n >= 4. */
+zc_status zc_fri_fold_commit_bitrev(const zc_poseidon2* p, const uint32_t* cw, int64_t n,
+                                    int ef_in, const uint32_t* beta, int ef_beta,
+                                    uint32_t shift_mont, uint32_t generator, uint32_t* out,
+                                    uint32_t* next_layers, void* stream);
+/* Replaces SingleMatrixCommitmentScheme.bind_root (zorch/commit/smcs.py:118-140):
+ * out = compress([raw_root, sponge([log_height, width])]), the two shape
+ * words as field elements; raw_root and out are 8 device words (out 16-byte
+ * aligned). */
+zc_status zc_smcs_bind_root(const zc_poseidon2* p, const uint32_t* raw_root, uint32_t log_height,
+                            uint32_t width, uint32_t* out, void* stream);
 
 /* Staggered partial-Lagrange batching of a committed matrix's w base columns
  * (n words each) into one EF4 codeword [n, 4] (16-byte aligned): weights =

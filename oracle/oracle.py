@@ -7,9 +7,12 @@ storage of zk_dtypes' *_mont dtypes), canonical values are converted with
 `to_mont` / `from_mont`.
 
 Parity: Poseidon2/sponge/compression/Merkle are pinned to the reference's
-Plonky3 KoalaBear-16 golden (tests/golden/koalabear16.json); the BabyBear
-Poseidon2 instance is project-defined, so BabyBear roots, challenges and proof
-bytes are "parity unpinned vs reference" (oracle == CUDA only).
+Plonky3 KoalaBear-16 golden (tests/golden/koalabear16.json); the bit-reversed
+KoalaBear encode, the column-major commit and openings, the bit-reversed fold,
+and the SP1 single-matrix commitment are pinned to the reference's SP1
+pipeline dump (tests/golden/sp1_fibonacci). The BabyBear Poseidon2 instance is
+project-defined, so BabyBear roots, challenges and proof bytes are "parity
+unpinned vs reference" (oracle == CUDA only).
 """
 
 from __future__ import annotations
@@ -61,6 +64,9 @@ def _load() -> C.CDLL:
         "orc_eval_poly": (u32, [i32, _u32p, i64, u32]),
         "orc_domain_point": (u32, [i32, i32, u32, u32, i64]),
         "orc_fri_fold": (i32, [i32, _u32p, i64, i32, _u32p, i32, u32, u32, _u32p]),
+        "orc_rs_encode_bitrev": (i32, [i32, _u32p, i64, i32, i32, u32, u32, _u32p]),
+        "orc_fri_fold_bitrev": (i32, [i32, _u32p, i64, i32, _u32p, i32, u32, u32, _u32p]),
+        "orc_smcs_bind_root": (None, [vp, _u32p, u32, u32, _u32p]),
         "orc_duplex_init": (None, [vp]),
         "orc_duplex_observe": (None, [vp, vp, _u32p, i64]),
         "orc_duplex_sample": (None, [vp, vp, i32, _u32p]),
@@ -167,9 +173,30 @@ class Poseidon2:
         return out
 
 
+GOLDEN = Path(__file__).resolve().parent.parent / "tests" / "golden"
+
+
 def load_koalabear_fixture() -> dict:
-    path = Path(__file__).resolve().parent.parent / "tests" / "golden" / "koalabear16.json"
-    return json.loads(path.read_text())
+    return json.loads((GOLDEN / "koalabear16.json").read_text())
+
+
+def load_sp1_fixture() -> dict:
+    """SP1's KoalaBear-16 instance (zorch/commit/testing/sp1_koalabear16.py)."""
+    return json.loads((GOLDEN / "sp1_fibonacci" / "sp1_koalabear16.json").read_text())
+
+
+def sp1_koalabear16() -> "Poseidon2":
+    d = load_sp1_fixture()
+    return Poseidon2.from_canonical(KOALABEAR, d["alpha"], d["external_initial"],
+                                    d["external_terminal"], d["internal_rc"],
+                                    d["internal_diag"], d["internal_j_scale"])
+
+
+def smcs_bind_root(p2: Poseidon2, raw_root, log_height: int, width: int) -> np.ndarray:
+    """SingleMatrixCommitmentScheme.bind_root (zorch/commit/smcs.py:118-140)."""
+    out = np.zeros(8, np.uint32)
+    LIB.orc_smcs_bind_root(p2.ptr, u32(raw_root).reshape(-1), log_height, width, out)
+    return out
 
 
 # ------------------------------------------------------------------ Merkle --
@@ -232,6 +259,21 @@ def rs_encode(field: int, coeffs: np.ndarray, log_blowup: int, shift_mont: int =
     return out.reshape(*batch_shape, k << log_blowup)
 
 
+def rs_encode_bitrev(field: int, coeffs: np.ndarray, log_blowup: int, shift_mont: int = 0,
+                     generator: int = 0) -> np.ndarray:
+    """BitReversedReedSolomon.encode (zorch/coding/reed_solomon.py:476-478)."""
+    c = u32(coeffs)
+    batch_shape = c.shape[:-1]
+    k = c.shape[-1]
+    batch = int(np.prod(batch_shape)) if batch_shape else 1
+    out = np.zeros((batch, k << log_blowup), np.uint32)
+    rc = LIB.orc_rs_encode_bitrev(field, c.reshape(-1), batch, k.bit_length() - 1, log_blowup,
+                                  shift_mont, generator, out.reshape(-1))
+    if rc:
+        raise ValueError(f"rs_encode_bitrev failed ({rc})")
+    return out.reshape(*batch_shape, k << log_blowup)
+
+
 def rs_encode_horner(field, coeffs, log_blowup, shift_mont=0, generator=0) -> np.ndarray:
     c = u32(coeffs)
     k = c.size
@@ -277,6 +319,52 @@ def fri_fold(field, cw, ef_in: bool, beta, ef_beta: bool, shift_mont=0, generato
     if rc:
         raise ValueError("fri_fold needs a power-of-two length >= 2")
     return out
+
+
+def fri_fold_bitrev(field, cw, ef_in: bool, beta, ef_beta: bool, shift_mont=0, generator=0):
+    """BitReversedReedSolomon.fold (zorch/coding/reed_solomon.py:484-492)."""
+    cw = u32(cw)
+    n = cw.shape[0]
+    lo = 4 if (ef_in or ef_beta) else 1
+    out = np.zeros((n // 2, lo) if lo == 4 else (n // 2,), np.uint32)
+    b = np.zeros(4, np.uint32)
+    b[: (4 if ef_beta else 1)] = u32(beta).reshape(-1)[: (4 if ef_beta else 1)]
+    rc = LIB.orc_fri_fold_bitrev(field, cw.reshape(-1), n, int(ef_in), b, int(ef_beta),
+                                 shift_mont, generator, out.reshape(-1))
+    if rc:
+        raise ValueError("fri_fold_bitrev needs a power-of-two length >= 2")
+    return out
+
+
+def bit_reverse(j: int, bits: int) -> int:
+    return int(format(int(j), f"0{bits}b")[::-1], 2) if bits else 0
+
+
+def sp1_query_positions(raw, block_len: int) -> np.ndarray:
+    """SP1's sample_bits rule (zorch/pcs/jagged/open.py:116-125): the CANONICAL
+    value of each squeeze masked to log2(block_len) low bits."""
+    return (u32(raw) & np.uint32(block_len - 1)).astype(np.int32)
+
+
+def sp1_stacked_fold_chain(p2: Poseidon2, field: int, codeword, betas, shift_mont: int = 0):
+    """The commit/fold half of the stacked BaseFold open's fold loop
+    (zorch/pcs/jagged/open.py:262-296) with the betas given (as the reference's
+    byte-match replays them): per round, the EF4 bit-reversed layer viewed as
+    [n/2, 8] base rows is committed through the SP1 SMCS (raw root, bound root)
+    and folded with the round's beta. Returns (raw_roots, bound_roots, layers,
+    final_codeword); layers[i] = (rows [n_i/2, 8], digest layers)."""
+    cw = u32(codeword).reshape(-1, 4)
+    raw, bound, layers = [], [], []
+    for beta in u32(betas).reshape(-1, 4):
+        n = cw.shape[0]
+        leaves = cw.reshape(n // 2, 8)
+        dl = merkle_commit_rows(p2, leaves)
+        raw.append(dl[-1][0])
+        bound.append(smcs_bind_root(p2, dl[-1][0], (n // 2).bit_length() - 1, 8))
+        layers.append((leaves, dl))
+        cw = fri_fold_bitrev(field, cw, True, beta, True, shift_mont)
+        shift_mont = LIB.orc_mul(field, shift_mont, shift_mont) if shift_mont else 0
+    return np.stack(raw), np.stack(bound), layers, cw
 
 
 # -------------------------------------------------------------- transcript --

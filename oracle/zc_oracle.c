@@ -307,6 +307,13 @@ void orc_compress(const orc_p2* P, const uint32_t* l8, const uint32_t* r8, uint3
 /* --------------------------------------------------------------- Merkle ---- */
 static int is_pow2(int64_t x) { return x > 0 && (x & (x - 1)) == 0; }
 
+/* j with its low `bits` bits reversed. */
+static int64_t brev64(int64_t j, int bits) {
+  int64_t r = 0;
+  for (int b = 0; b < bits; b++) r |= ((j >> b) & 1) << (bits - 1 - b);
+  return r;
+}
+
 static void gather_leaf(const uint32_t* base, int64_t p, int groups, int g,
                         int64_t gstride, uint32_t* row) {
   for (int q = 0; q < groups; q++)
@@ -437,6 +444,31 @@ int orc_rs_encode_horner(int field, const uint32_t* coeffs, int log_k, int log_b
   return 0;
 }
 
+/* BitReversedReedSolomon.encode (zorch/coding/reed_solomon.py:476-478): the
+ * natural-order codeword of orc_rs_encode, then bit-reversed along the last
+ * axis (out[b, brev(j)] = natural[b, j]). */
+int orc_rs_encode_bitrev(int field, const uint32_t* coeffs, int64_t batch, int log_k,
+                         int log_blowup, uint32_t shift_mont, uint32_t generator,
+                         uint32_t* out) {
+  const int rc = orc_rs_encode(field, coeffs, batch, log_k, log_blowup, shift_mont, generator, out);
+  if (rc) return rc;
+  const int log_n = log_k + log_blowup;
+  const int64_t n = (int64_t)1 << log_n;
+#pragma omp parallel for num_threads(orc_get_threads()) schedule(static)
+  for (int64_t b = 0; b < batch; b++) {
+    uint32_t* a = out + b * n;
+    for (int64_t j = 0; j < n; j++) {
+      const int64_t r = brev64(j, log_n);
+      if (j < r) {
+        const uint32_t t = a[j];
+        a[j] = a[r];
+        a[r] = t;
+      }
+    }
+  }
+  return 0;
+}
+
 /* Horner evaluation of one polynomial at one point: sum_i c_i x^i. */
 uint32_t orc_eval_poly(int field, const uint32_t* coeffs, int64_t k, uint32_t x) {
   const fld* F = FLD(field);
@@ -506,6 +538,60 @@ int orc_fri_fold(int field, const uint32_t* cw, int64_t n, int ef_in, const uint
     for (int e = 0; e < lo; e++) out[j * lo + e] = fadd(F, sum[e], r[e]);
   }
   return 0;
+}
+
+/* BitReversedReedSolomon.fold (zorch/coding/reed_solomon.py:484-492, 532-540)
+ * on a bit-reversed layer: the pair (cw[2p], cw[2p+1]) = (f(x_p), f(-x_p)) with
+ * x_p = shift * w_n^brev(p) (p read over log2(n/2) bits; x_0 = shift for n = 2),
+ * folded by fri_fold_values (:543-548); the output is the next layer, again
+ * bit-reversed. */
+int orc_fri_fold_bitrev(int field, const uint32_t* cw, int64_t n, int ef_in, const uint32_t* beta,
+                        int ef_beta, uint32_t shift_mont, uint32_t generator, uint32_t* out) {
+  const fld* F = FLD(field);
+  if (!is_pow2(n) || n < 2) return 2;
+  int log_n = 0;
+  while (((int64_t)1 << log_n) < n) log_n++;
+  const int li = ef_in ? 4 : 1, lb = ef_beta ? 4 : 1, lo = (ef_in || ef_beta) ? 4 : 1;
+  const int64_t half = n / 2;
+  const uint32_t w = root_of_unity(F, log_n, generator);
+  const uint32_t two = fadd(F, F->one, F->one);
+  const uint32_t inv2 = finv(F, two);
+  const uint32_t sh = shift_mont ? shift_mont : F->one;
+#pragma omp parallel for num_threads(orc_get_threads()) schedule(static)
+  for (int64_t p = 0; p < half; p++) {
+    const uint32_t x = fmul(F, sh, fpow(F, w, (uint64_t)brev64(p, log_n - 1)));
+    const uint32_t xinv = finv(F, fmul(F, two, x)); /* 1/(2 x_p) */
+    uint32_t a[4] = {0, 0, 0, 0}, b[4] = {0, 0, 0, 0}, sum[4], d[4], bt[4] = {0, 0, 0, 0};
+    for (int e = 0; e < li; e++) {
+      a[e] = cw[(2 * p) * li + e];
+      b[e] = cw[(2 * p + 1) * li + e];
+    }
+    for (int e = 0; e < lb; e++) bt[e] = beta[e];
+    for (int e = 0; e < 4; e++) {
+      sum[e] = fmul(F, fadd(F, a[e], b[e]), inv2);
+      d[e] = fmul(F, fsub(F, a[e], b[e]), xinv);
+    }
+    uint32_t r[4];
+    if (lo == 4) {
+      ef4_mul(F, bt, d, r);
+    } else {
+      r[0] = fmul(F, bt[0], d[0]);
+    }
+    for (int e = 0; e < lo; e++) out[p * lo + e] = fadd(F, sum[e], r[e]);
+  }
+  return 0;
+}
+
+/* SingleMatrixCommitmentScheme.bind_root (zorch/commit/smcs.py:118-140):
+ * compress([raw_root, sponge([log_height, width])]), the two shape words as
+ * field elements. */
+void orc_smcs_bind_root(const orc_p2* P, const uint32_t* raw_root, uint32_t log_height,
+                        uint32_t width, uint32_t* out8) {
+  const fld* F = FLD(P->field);
+  const uint32_t shape[2] = {to_m(F, log_height), to_m(F, width)};
+  uint32_t params[8];
+  orc_sponge_hash(P, shape, 2, params);
+  orc_compress(P, raw_root, params, out8);
 }
 
 /* sample_rlc_coeffs_bits + batch_staggered (zorch/pcs/jagged/open.py:88-105,

@@ -90,6 +90,10 @@ int orc_rs_encode(int field, const uint32_t* coeffs, int64_t batch, int log_k,
 int orc_rs_encode_horner(int field, const uint32_t* coeffs, int log_k,
                          int log_blowup, uint32_t shift_mont, uint32_t generator,
                          uint32_t* out);
+/* BitReversedReedSolomon.encode: orc_rs_encode, each row bit-reversed. */
+int orc_rs_encode_bitrev(int field, const uint32_t* coeffs, int64_t batch, int log_k,
+                         int log_blowup, uint32_t shift_mont, uint32_t generator,
+                         uint32_t* out);
 uint32_t orc_eval_poly(int field, const uint32_t* coeffs, int64_t k, uint32_t x);
 uint32_t orc_domain_point(int field, int log_n, uint32_t shift_mont, uint32_t generator,
                           int64_t j);
@@ -100,6 +104,15 @@ void orc_eval_domain(int field, int log_n, uint32_t shift_mont, uint32_t generat
 int orc_fri_fold(int field, const uint32_t* cw, int64_t n, int ef_in,
                  const uint32_t* beta, int ef_beta, uint32_t shift_mont,
                  uint32_t generator, uint32_t* out);
+
+/* FRI fold of a bit-reversed layer (pairs adjacent); output bit-reversed. */
+int orc_fri_fold_bitrev(int field, const uint32_t* cw, int64_t n, int ef_in,
+                        const uint32_t* beta, int ef_beta, uint32_t shift_mont,
+                        uint32_t generator, uint32_t* out);
+
+/* SP1 single-matrix commitment domain separator. */
+void orc_smcs_bind_root(const orc_p2* p, const uint32_t* raw_root, uint32_t log_height,
+                        uint32_t width, uint32_t* out8);
 
 /* Duplex transcript (overwrite mode, rate 8, width 16) */
 void orc_duplex_init(orc_duplex* t);

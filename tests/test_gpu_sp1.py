@@ -1,0 +1,216 @@
+"""The bit-reversed code, the SP1 single-matrix commitment and the stacked
+fold rounds on the GPU, against the reference's SP1 KoalaBear pipeline dump
+(tests/golden/sp1_fibonacci) and against the oracle.
+
+The prep-round test runs the whole product path -- BitReversedReedSolomon
+encode of the 2^21-word preprocessed column (KoalaBear, blowup 4), the
+column-major SMCS commit with SP1's Poseidon2, the openings at the dumped
+query positions -- and compares every opened row and sibling digest with the
+dump (zorch/pcs/jagged/testing/open_test.py:279-287). The fold test folds the
+dumped opened pairs of a fold layer on the GPU and compares with the next
+layer's dumped values. Integer work: the tolerance is zero.
+"""
+
+from __future__ import annotations
+
+import lzma
+
+import numpy as np
+import pytest
+
+torch = pytest.importorskip("torch")
+pytestmark = pytest.mark.gpu
+
+from zorch_gb300 import _lib  # noqa: E402
+from zorch_gb300.field import BABYBEAR, KOALABEAR, to_device, to_host  # noqa: E402
+
+
+@pytest.fixture(scope="module", autouse=True)
+def _cuda():
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    _lib.check(_lib.lib().zc_init(0), "init")
+
+
+def rand_mont(orc, field, shape, seed):
+    p = orc.MODULUS[field]
+    x = np.random.default_rng(seed).integers(0, p, size=shape, dtype=np.uint64).astype(np.uint32)
+    return orc.to_mont(field, x)
+
+
+def dev(x):
+    return to_device(np.asarray(x, np.uint32))
+
+
+@pytest.fixture(scope="module")
+def sp1(orc):
+    from zorch_gb300.commit import Poseidon2
+
+    d = orc.load_sp1_fixture()
+    gpu = Poseidon2.from_params(KOALABEAR, d["alpha"], d["external_initial"],
+                                d["external_terminal"], d["internal_rc"], d["internal_diag"],
+                                d["internal_j_scale"])
+    return gpu, orc.sp1_koalabear16()
+
+
+@pytest.fixture(scope="module")
+def golden(orc):
+    g = orc.GOLDEN / "sp1_fibonacci"
+    prep = np.frombuffer(lzma.decompress((g / "prep_dense.u32.xz").read_bytes()), "<u4")
+    return {"prep": prep.astype(np.uint32), "round": np.load(g / "prep_round.npz"),
+            "chain": np.load(g / "fold_chain.npz")}
+
+
+def test_prep_round_commit_and_openings_match_sp1_dump(orc, sp1, golden):
+    from zorch_gb300.coding import BitReversedReedSolomon
+    from zorch_gb300.commit import SingleMatrixCommitmentScheme, VerifyCode
+    from zorch_gb300.jagged import sample_query_positions  # noqa: F401  (API surface)
+
+    perm, cpu = sp1
+    z = golden["round"]
+    S = 1 << int(z["log_stacking_height"])
+    code = BitReversedReedSolomon(S, 1 << int(z["log_blowup"]), KOALABEAR)
+    smcs = SingleMatrixCommitmentScheme(perm)
+    block = dev(golden["prep"]).reshape(1, S)  # stacked column-major: one column
+    cw = code.encode(block)  # [1, S * blowup], bit-reversed
+    commitment, layers = smcs.commit(cw, column_major=True)
+    n = cw.shape[1]
+    pos = dev(orc.sp1_query_positions(z["query_indices"], n)).to(torch.int32)
+    rows, proofs = smcs.open_batch(pos, cw.reshape(n, 1), layers)
+    assert np.array_equal(to_host(rows), z["rows"])
+    assert np.array_equal(to_host(proofs), z["paths"])
+    # the separator-bound commitment: device bind == host bind == verifier
+    raw = to_host(layers.root)
+    assert np.array_equal(to_host(commitment), orc.smcs_bind_root(cpu, raw, n.bit_length() - 1, 1))
+    for q in range(0, 52, 13):
+        assert smcs.verify_batch(commitment, (n, 1), int(pos[q]), rows[q], proofs[:, q]) == \
+            VerifyCode.OK
+    bad = rows[0].clone()
+    bad[0] ^= 1
+    assert smcs.verify_batch(commitment, (n, 1), int(pos[0]), bad, proofs[:, 0]) == \
+        VerifyCode.ROOT_MISMATCH
+    assert smcs.verify_batch(commitment, (n, 1), n, rows[0], proofs[:, 0]) == \
+        VerifyCode.INDEX_OUT_OF_BOUNDS
+    assert smcs.verify_batch(commitment, (n, 1), int(pos[0]), rows[0], proofs[:-1, 0]) == \
+        VerifyCode.WRONG_HEIGHT
+
+
+@pytest.mark.parametrize("i", [0, 1, 10, 19, 20])
+def test_bitrev_fold_matches_sp1_dump(orc, golden, i):
+    from zorch_gb300.coding import BitReversedReedSolomon
+
+    ch = golden["chain"]
+    n0 = 1 << 23
+    code = BitReversedReedSolomon(1 << 21, 4, KOALABEAR)
+    qpos = orc.sp1_query_positions(ch["query_indices"], n0)
+    n = n0 >> i
+    rows = ch[f"rows_f{i}"]
+    layer = np.zeros((n, 4), np.uint32)
+    for q in range(rows.shape[0]):
+        p = int(qpos[q]) >> (i + 1)
+        layer[2 * p: 2 * p + 2] = rows[q].reshape(2, 4)
+    g = to_host(code.fold(dev(layer), dev(ch["fri_betas"][i])))
+    last = i + 1 == ch["fri_betas"].shape[0]
+    for q in range(rows.shape[0]):
+        p = int(qpos[q]) >> (i + 1)
+        want = ch["final_poly"] if last else ch[f"rows_f{i + 1}"][q].reshape(2, 4)[p & 1]
+        assert np.array_equal(g[p], want), (i, q)
+
+
+@pytest.mark.parametrize("field", [0, 1])
+@pytest.mark.parametrize("log_k,log_b,batch", [(0, 1, 2), (3, 2, 3), (10, 2, 2), (12, 2, 2),
+                                               (13, 1, 2), (14, 2, 1), (16, 3, 1), (21, 2, 1)])
+def test_bitrev_encode_matches_oracle(orc, field, log_k, log_b, batch):
+    from zorch_gb300.coding import rs_encode
+    from zorch_gb300.field import field_of
+
+    f = field_of(field)
+    m = rand_mont(orc, field, (batch, 1 << log_k), 7 * log_k + log_b)
+    for shift in (None, f.generator):
+        sh = f.mont(shift) if shift else 0
+        got = to_host(rs_encode(f, dev(m).reshape(batch, -1), log_b, sh, bit_reversed=True))
+        want = orc.rs_encode_bitrev(field, m, log_b, sh)
+        assert np.array_equal(got, want), (log_k, log_b, shift)
+
+
+def test_batched_lde_mixes_natural_and_bit_reversed(orc):
+    from zorch_gb300.batch import BatchCommitter, MatrixJob
+
+    bc = BatchCommitter(BABYBEAR)
+    shapes = [(3, 1 << 10, 2, False), (2, 1 << 14, 1, True), (1, 1 << 16, 2, True),
+              (4, 1 << 9, 3, True), (1, 1 << 15, 1, False)]
+    jobs, want = [], []
+    for s, (w, h, lb, br) in enumerate(shapes):
+        m = rand_mont(orc, 0, (w, h), 50 + s)
+        jobs.append(MatrixJob(dev(m).reshape(w, h), lb, 31, bit_reversed=br))
+        enc = orc.rs_encode_bitrev if br else orc.rs_encode
+        want.append(enc(0, m, lb, int(orc.to_mont(0, [31])[0])))
+    outs = bc.encode(jobs)
+    for o_, w_ in zip(outs, want):
+        assert np.array_equal(to_host(o_), w_)
+
+
+def test_smcs_bind_root_matches_oracle(orc, sp1, perms_bb):
+    from zorch_gb300.commit import SingleMatrixCommitmentScheme
+
+    for (gpu, cpu), f in ((sp1, 1), (perms_bb, 0)):
+        smcs = SingleMatrixCommitmentScheme(gpu)
+        for s, (lh, w) in enumerate([(0, 1), (5, 8), (23, 1), (21, 255)]):
+            raw = rand_mont(orc, f, 8, 900 + s)
+            got = to_host(smcs.bind_root(dev(raw), lh, w))
+            assert np.array_equal(got, orc.smcs_bind_root(cpu, raw, lh, w))
+            assert np.array_equal(smcs.bind_root_host(raw, lh, w), got)
+
+
+@pytest.fixture(scope="module")
+def perms_bb(orc):
+    from zorch_gb300.commit import Poseidon2
+
+    return Poseidon2.builtin(BABYBEAR), orc.Poseidon2.babybear16()
+
+
+@pytest.mark.parametrize("field,log_n,rounds", [(1, 12, 6), (0, 10, 9), (1, 3, 2)])
+def test_stacked_fold_commit_matches_oracle(orc, sp1, perms_bb, field, log_n, rounds):
+    from zorch_gb300.coding import BitReversedReedSolomon
+    from zorch_gb300.commit import SingleMatrixCommitmentScheme
+    from zorch_gb300.jagged import StackedFoldCommit
+
+    gpu, cpu = sp1 if field == 1 else perms_bb
+    shift = None if field == 1 else 31
+    n = 1 << log_n
+    code = BitReversedReedSolomon(n // 4, 4, field, coset_shift=shift)
+    cw = rand_mont(orc, field, (n, 4), 40 + log_n)
+    betas = rand_mont(orc, field, (rounds, 4), 41 + log_n)
+    sf = StackedFoldCommit(SingleMatrixCommitmentScheme(gpu), code)
+    layers, final = sf.run_replay(dev(cw).reshape(n, 4), dev(betas).reshape(rounds, 4))
+    sh = code.level_shift_mont(0)
+    raw, bound, olayers, ofinal = orc.sp1_stacked_fold_chain(cpu, field, cw, betas, sh)
+    assert np.array_equal(to_host(final), ofinal)
+    for r, layer in enumerate(layers):
+        assert np.array_equal(to_host(layer.raw_root), raw[r]), r
+        assert np.array_equal(to_host(layer.bound_root), bound[r]), r
+        want_flat = np.concatenate([lv.reshape(-1) for lv in olayers[r][1]])
+        assert np.array_equal(to_host(layer.digest_layers.flat).reshape(-1), want_flat), r
+    pos = np.random.default_rng(5).integers(0, n, 16).astype(np.int32)
+    opened = sf.open_layers(layers, torch.tensor(pos, device="cuda"))
+    for r, (rows, proofs) in enumerate(opened):
+        leaves, dl = olayers[r]
+        idx = pos >> (r + 1)
+        wr, wp = orc.merkle_open(leaves, leaves.shape[0], 1, 8, 0, dl, idx)
+        assert np.array_equal(to_host(rows), wr) and np.array_equal(to_host(proofs), wp), r
+
+
+def test_sp1_query_positions_use_canonical_bits(orc, sp1):
+    from zorch_gb300.jagged import sample_query_positions
+    from zorch_gb300.transcript import DuplexTranscript
+
+    gpu, cpu = sp1
+    t = DuplexTranscript.new(gpu)
+    vals = rand_mont(orc, 1, 13, 3)
+    t = t.observe(dev(vals))
+    _, pos = sample_query_positions(t, 1 << 20, 52)
+    ot = orc.Transcript(cpu)
+    ot.observe(vals)
+    raw = ot.sample(52)
+    assert np.array_equal(to_host(pos).astype(np.uint32),
+                          orc.from_mont(1, raw) & np.uint32((1 << 20) - 1))

@@ -29,7 +29,7 @@ class ZcError(RuntimeError):
 class LdeJob(C.Structure):
     _fields_ = [("coeffs", C.c_void_p), ("out", C.c_void_p), ("batch", C.c_int64),
                 ("log_k", C.c_int32), ("log_blowup", C.c_int32), ("shift_mont", C.c_uint32),
-                ("tile_log", C.c_int32)]
+                ("tile_log", C.c_int32), ("bit_reversed", C.c_int32)]
 
 
 class Leaves(C.Structure):
@@ -68,10 +68,15 @@ def _declare(lib: C.CDLL) -> None:
         "zc_rs_encode_workspace_bytes": (sz, [i64, C.c_int, C.c_int]),
         "zc_rs_encode": (st, [st, vp, i64, C.c_int, C.c_int, u32, u32, vp, vp, sz, vp]),
         "zc_rs_encode_noalloc": (st, [st, vp, i64, C.c_int, C.c_int, u32, u32, vp, vp]),
+        "zc_rs_encode_bitrev": (st, [st, vp, i64, C.c_int, C.c_int, u32, u32, vp, vp, sz, vp]),
         "zc_merkle_commit": (st, [vp, Leaves, vp, vp]),
         "zc_merkle_open": (st, [Leaves, vp, vp, i32, vp, vp, vp, vp]),
         "zc_fri_fold": (st, [st, vp, i64, C.c_int, vp, C.c_int, u32, u32, vp, vp]),
         "zc_fri_fold_commit": (st, [vp, vp, i64, C.c_int, vp, C.c_int, u32, u32, vp, vp, vp]),
+        "zc_fri_fold_bitrev": (st, [st, vp, i64, C.c_int, vp, C.c_int, u32, u32, vp, vp]),
+        "zc_fri_fold_commit_bitrev": (st, [vp, vp, i64, C.c_int, vp, C.c_int, u32, u32, vp, vp,
+                                           vp]),
+        "zc_smcs_bind_root": (st, [vp, vp, u32, u32, vp, vp]),
         "zc_duplex_hop": (st, [vp, vp, vp, vp, vp, vp, vp, i64, i32, vp, vp, vp, vp, vp, vp, vp]),
         "zc_duplex_hop_host": (st, [vp, vp, vp, vp, vp, vp, vp, i64, i32, vp, vp, vp, vp, vp, vp]),
         "zc_duplex_step": (st, [vp, vp, vp, i64, i32, vp, vp, i64, vp]),

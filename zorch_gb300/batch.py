@@ -32,11 +32,13 @@ _TILE_CANDIDATES = (13, 14, 15)
 @dataclass
 class MatrixJob:
     """One matrix to commit: columns [w, h] (Montgomery), blowup 2^log_blowup,
-    coset shift (canonical) or None."""
+    coset shift (canonical) or None; `bit_reversed` codewords are laid out as
+    BitReversedReedSolomon.encode lays them (zorch/coding/reed_solomon.py:476-478)."""
 
     columns: torch.Tensor
     log_blowup: int
     shift: int | None = 31
+    bit_reversed: bool = False
 
     @property
     def width(self) -> int:
@@ -130,7 +132,8 @@ class BatchCommitter:
             h = j.height
             tl = self.tile_override or (self.tuner.tile_log(j.log_n, j.width) if self.tuner else 0)
             arr[i] = _lib.LdeJob(ptr(j.columns), ptr(o), j.width, h.bit_length() - 1,
-                                 j.log_blowup, self.field.mont(j.shift) if j.shift else 0, tl)
+                                 j.log_blowup, self.field.mont(j.shift) if j.shift else 0, tl,
+                                 int(j.bit_reversed))
         return arr
 
     def encode(self, jobs: list[MatrixJob], outs: list[torch.Tensor] | None = None,

@@ -41,7 +41,8 @@ def _deps() -> list[Path]:
 
 def build(force: bool = False, verbose: bool = False, extra: list[str] | None = None) -> Path:
     """Compile libzc.so; `extra` (or the ZC_NVCC_FLAGS environment variable)
-    adds nvcc flags, e.g. -DZC_MU_SHIFT. A change of flags forces a rebuild."""
+    adds nvcc flags (e.g. -DNAME=VALUE, -maxrregcount=N). A change of flags
+    forces a rebuild."""
     extra = list(extra or []) + os.environ.get("ZC_NVCC_FLAGS", "").split()
     stamp = OUT_DIR / "flags.txt"
     flags_id = " ".join(extra)

@@ -1,8 +1,10 @@
-"""Reed-Solomon code over BabyBear / KoalaBear on the GPU (drop-in for
-zorch/coding/reed_solomon.py:71-426).
+"""Reed-Solomon codes over BabyBear / KoalaBear on the GPU (drop-in for
+zorch/coding/reed_solomon.py:71-540).
 
-`encode` is the coset low-degree extension (zc_rs_encode), `fold` the natural
-order conjugate-pair FRI fold (zc_fri_fold). Tensors are torch.int32 CUDA
+`ReedSolomon.encode` is the coset low-degree extension (zc_rs_encode), `fold`
+the natural-order conjugate-pair FRI fold (zc_fri_fold);
+`BitReversedReedSolomon` is the same code with codewords in bit-reversed order
+(zc_rs_encode_bitrev, zc_fri_fold_bitrev). Tensors are torch.int32 CUDA
 tensors of Montgomery words; the coset shift and generator are canonical ints
 (e.g. coset_shift=31, generator=31 for BabyBear).
 """
@@ -24,8 +26,10 @@ def _log2(x: int) -> int:
 
 
 def rs_encode(field: Field, message: torch.Tensor, log_blowup: int, shift_mont: int = 0,
-              generator: int = 0, out: torch.Tensor | None = None) -> torch.Tensor:
-    """zc_rs_encode over the last axis of `message` (any leading batch shape)."""
+              generator: int = 0, out: torch.Tensor | None = None, *,
+              bit_reversed: bool = False) -> torch.Tensor:
+    """zc_rs_encode (zc_rs_encode_bitrev) over the last axis of `message` (any
+    leading batch shape)."""
     k = message.shape[-1]
     if not _is_pow2(k):
         raise ValueError(f"message_len must be a power of two, got {k}")
@@ -36,9 +40,9 @@ def rs_encode(field: Field, message: torch.Tensor, log_blowup: int, shift_mont: 
     L = _lib.lib()
     ws_bytes = L.zc_rs_encode_workspace_bytes(batch, _log2(k), log_blowup)
     ws = torch.empty(max(ws_bytes // 4, 1), dtype=torch.int32, device=message.device)
-    _lib.check(L.zc_rs_encode(field.id, ptr(message.contiguous()), batch, _log2(k), log_blowup,
-                              shift_mont, generator, ptr(out), ptr(ws), ws_bytes,
-                              stream_handle()), "rs_encode")
+    fn = L.zc_rs_encode_bitrev if bit_reversed else L.zc_rs_encode
+    _lib.check(fn(field.id, ptr(message.contiguous()), batch, _log2(k), log_blowup, shift_mont,
+                  generator, ptr(out), ptr(ws), ws_bytes, stream_handle()), "rs_encode")
     return out
 
 
@@ -191,3 +195,95 @@ class ReedSolomon:
 
     def check_final(self, final: torch.Tensor, claim: torch.Tensor) -> bool:
         return bool((final == claim).all())
+
+
+def bit_reverse_indices(positions: torch.Tensor, n: int) -> torch.Tensor:
+    """Each index reversed over log2(n) bits (zorch/coding/reed_solomon.py:429-437)."""
+    bits = _log2(n)
+    rev = torch.zeros_like(positions)
+    for b in range(bits):
+        rev |= ((positions >> b) & 1) << (bits - 1 - b)
+    return rev
+
+
+class BitReversedReedSolomon:
+    """Reed-Solomon with codewords in bit-reversed evaluation order
+    (zorch/coding/reed_solomon.py:440-540): the pair (f(x), f(-x)) of a fold
+    sits at (2p, 2p+1), and folding a bit-reversed layer yields the next
+    layer, again bit-reversed. The fold math is ReedSolomon's."""
+
+    def __init__(self, message_len: int, blowup: int, field=BABYBEAR, *,
+                 coset_shift: int | None = None) -> None:
+        self._natural = ReedSolomon(message_len, blowup, field, coset_shift=coset_shift)
+        self.message_len = message_len
+        self.blowup = blowup
+        self.block_len = self._natural.block_len
+        self.field = self._natural.field
+        self.coset_shift = coset_shift
+
+    def __eq__(self, other) -> bool:
+        return isinstance(other, BitReversedReedSolomon) and self._natural == other._natural
+
+    def __hash__(self) -> int:
+        return hash((BitReversedReedSolomon, self._natural))
+
+    @property
+    def log_blowup(self) -> int:
+        return self._natural.log_blowup
+
+    def encode(self, message: torch.Tensor, out: torch.Tensor | None = None) -> torch.Tensor:
+        """Coset LDE of the last axis in bit-reversed order (:476-478)."""
+        if message.shape[-1] != self.message_len:
+            raise ValueError(f"message last axis must be {self.message_len}, "
+                             f"got {message.shape[-1]}")
+        return rs_encode(self.field, message, self.log_blowup, self._natural._shift_mont, 0, out,
+                         bit_reversed=True)
+
+    def domain(self) -> torch.Tensor:
+        """The points `encode` evaluates on, in codeword (bit-reversed) order."""
+        d = self._natural.domain()
+        return d.index_select(0, bit_reverse_indices(
+            torch.arange(d.shape[0], device=d.device), d.shape[0]))
+
+    def fold(self, codeword: torch.Tensor, beta: torch.Tensor,
+             out: torch.Tensor | None = None) -> torch.Tensor:
+        """Adjacent-pair fold (:484-492); base layers [n], EF4 layers [n, 4]."""
+        n = codeword.shape[0]
+        if n < 2:
+            raise ValueError(f"fold requires a codeword of length >= 2, got {n}")
+        ef_in = codeword.dim() == 2
+        ef_beta = beta.numel() == 4
+        if out is None:
+            shape = (n // 2, 4) if (ef_in or ef_beta) else (n // 2,)
+            out = torch.empty(shape, dtype=torch.int32, device=codeword.device)
+        level = self._natural.level_of(n)
+        _lib.check(_lib.lib().zc_fri_fold_bitrev(
+            self.field.id, ptr(codeword.contiguous()), n, int(ef_in), ptr(beta.contiguous()),
+            int(ef_beta), self._natural.level_shift_mont(level), 0, ptr(out), stream_handle()),
+            "fri_fold_bitrev")
+        return out
+
+    def level_shift_mont(self, level: int) -> int:
+        return self._natural.level_shift_mont(level)
+
+    def level_of(self, n: int) -> int:
+        return self._natural.level_of(n)
+
+    def pair_indices(self, positions: torch.Tensor, level: int):
+        """The pair landing at `positions` is adjacent (:508-510)."""
+        return positions * 2, positions * 2 + 1
+
+    def pair_leaves(self, codeword: torch.Tensor) -> torch.Tensor:
+        """Leaf p = (codeword[2p], codeword[2p+1]) in base limbs: a view (:512-515)."""
+        return codeword.reshape(codeword.shape[0] // 2, -1)
+
+    def layer_positions(self, positions: torch.Tensor, num_rounds: int) -> list[torch.Tensor]:
+        """Each fold halves the index, a_i = q >> (i+1) (:517-524)."""
+        out, q = [], positions
+        for _ in range(num_rounds):
+            q = q >> 1
+            out.append(q)
+        return out
+
+    def check_final(self, final: torch.Tensor, claim: torch.Tensor) -> bool:
+        return self._natural.check_final(final, claim)

@@ -245,3 +245,84 @@ def koalabear16_params(fixture: dict) -> Poseidon2:
     return Poseidon2.from_params(KOALABEAR, fixture["alpha"], fixture["external_initial"],
                                  fixture["external_terminal"], fixture["internal_rc"],
                                  fixture["internal_diag"], fixture.get("internal_j_scale", 1))
+
+
+class VerifyCode:
+    """SMCS verifier return codes (zorch/commit/smcs.py:31-44)."""
+
+    OK = 0
+    WRONG_HEIGHT = 2
+    INDEX_OUT_OF_BOUNDS = 3
+    ROOT_MISMATCH = 4
+
+
+class SingleMatrixCommitmentScheme:
+    """SP1's single-matrix commitment over the Merkle tree (zorch/commit/smcs.py:47-228):
+    a Merkle root over the rows (or, `column_major=True`, the columns) of one
+    power-of-two-height base-field matrix, bound to the matrix shape by SP1's
+    domain separator commit = compress([root, sponge([log_height, width])])."""
+
+    def __init__(self, perm: Poseidon2) -> None:
+        self.perm = perm
+        self._tree = MerkleTree(perm)
+        self._tree_column_major = MerkleTree(perm, column_major=True)
+        self.digest_elems = 8
+
+    def commit(self, matrix: torch.Tensor, *,
+               column_major: bool = False) -> tuple[torch.Tensor, DigestLayers]:
+        """(commitment (8,), digest layers) (zorch/commit/smcs.py:69-106); a
+        column-major [width, height] matrix commits as its transpose would."""
+        tree = self._tree_column_major if column_major else self._tree
+        raw_root, layers = tree.commit(matrix)
+        height, width = matrix.shape[::-1] if column_major else matrix.shape
+        return self.bind_root(raw_root, height.bit_length() - 1, width), layers
+
+    def commit_layout(self, lv: _lib.Leaves, width: int,
+                      out: torch.Tensor | None = None) -> tuple[torch.Tensor, DigestLayers]:
+        """commit over an explicit leaf layout (zc_leaves)."""
+        raw_root, layers = self._tree.commit_layout(lv, out=out)
+        return self.bind_root(raw_root, lv.num_leaves.bit_length() - 1, width), layers
+
+    def bind_root(self, raw_root: torch.Tensor, log_height: int, width: int,
+                  out: torch.Tensor | None = None) -> torch.Tensor:
+        """compress([raw_root, sponge([log_height, width])]) on the device
+        (zorch/commit/smcs.py:118-140)."""
+        if out is None:
+            out = torch.empty(8, dtype=torch.int32, device=raw_root.device)
+        _lib.check(_lib.lib().zc_smcs_bind_root(self.perm.handle, ptr(raw_root.contiguous()),
+                                                log_height, width, ptr(out), stream_handle()),
+                   "smcs_bind_root")
+        return out
+
+    def bind_root_host(self, raw_root, log_height: int, width: int) -> np.ndarray:
+        """bind_root on the host (for verifiers)."""
+        f = self.perm.field
+        params = self.perm.hash_host(np.array([f.mont(log_height), f.mont(width)], np.uint32))
+        return self.perm.compress_host(np.asarray(raw_root, np.uint32).reshape(-1), params)
+
+    def open_batch(self, indices: torch.Tensor, matrix: torch.Tensor,
+                   layers: DigestLayers) -> tuple[torch.Tensor, torch.Tensor]:
+        """(rows [Q, width], proofs [log_height, Q, 8]) (zorch/commit/smcs.py:158-183):
+        `matrix` is the committed row-major [height, width] matrix."""
+        op = self._tree.open_rows(matrix, layers, indices)
+        return op.row, op.path
+
+    def verify_batch(self, commitment, dims: tuple[int, int], index: int, row, proof) -> int:
+        """One opened row against a commitment, on the host
+        (zorch/commit/smcs.py:185-228): a VerifyCode."""
+        height, width = dims
+        log_height = height.bit_length() - 1
+        proof = np.asarray(proof.detach().cpu() if torch.is_tensor(proof) else proof)
+        proof = proof.view(np.uint32).reshape(-1, 8)
+        if proof.shape[0] != log_height:
+            return VerifyCode.WRONG_HEIGHT
+        if not 0 <= int(index) < height:
+            return VerifyCode.INDEX_OUT_OF_BOUNDS
+        row = torch.as_tensor(np.asarray(
+            row.detach().cpu() if torch.is_tensor(row) else row).view(np.int32))
+        raw = self._tree.reconstruct_root(int(index), Opening(row, torch.as_tensor(
+            proof.view(np.int32))))
+        bound = self.bind_root_host(raw, log_height, width)
+        want = np.asarray(commitment.detach().cpu() if torch.is_tensor(commitment)
+                          else commitment).view(np.uint32).reshape(-1)
+        return VerifyCode.OK if np.array_equal(bound, want) else VerifyCode.ROOT_MISMATCH

@@ -29,6 +29,9 @@ inline int ilog2(int64_t x) {
   return l;
 }
 
+// log2 of a power of two, on the device.
+__device__ __forceinline__ int ilog2_dev(int64_t x) { return 63 - __clzll((long long)x); }
+
 // Digest-layer layout of an arity-2 tree over L leaves: level l (leaf digests
 // = level 0, root = level log2 L) starts at node offset 2L - (2L >> l).
 __host__ __device__ __forceinline__ int64_t level_offset(int64_t L, int l) {

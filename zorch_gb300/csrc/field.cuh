@@ -21,14 +21,10 @@ constexpr uint32_t mont_of(uint32_t p, uint64_t x) {
   return (uint32_t)(((x % p) << 32) % p);
 }
 
-template <uint32_t P_, uint32_t GEN_, uint32_t W_, int TWO_ADICITY_, int ID_, int MU_S_>
+template <uint32_t P_, uint32_t GEN_, uint32_t W_, int TWO_ADICITY_, int ID_>
 struct Mont31 {
   static constexpr uint32_t P = P_;
   static constexpr uint32_t MU = inv_mod_2_32(P_);  // p^-1 mod 2^32
-  // p^-1 mod 2^32 = 2^31 + 2^MU_S + 1 for both primes, so lo * MU is two
-  // shifts and an add (integer ALU pipe instead of the multiplier)
-  static constexpr int MU_S = MU_S_;
-  static_assert(MU == (1u << 31) + (1u << MU_S_) + 1u, "p^-1 mod 2^32 shape");
   static constexpr uint32_t ONE = (uint32_t)((((uint64_t)1) << 32) % P_);
   static constexpr uint32_t R2 = (uint32_t)(((uint64_t)ONE * ONE) % P_);
   static constexpr uint32_t GEN = GEN_;  // multiplicative generator, canonical
@@ -40,9 +36,9 @@ struct Mont31 {
 };
 
 // BabyBear p = 2^31 - 2^27 + 1, generator 31, EF4 = F[x]/(x^4 - 11).
-using BabyBear = Mont31<2013265921u, 31u, 11u, 27, 0, 27>;
+using BabyBear = Mont31<2013265921u, 31u, 11u, 27, 0>;
 // KoalaBear p = 2^31 - 2^24 + 1, generator 3, EF4 = F[x]/(x^4 - 3).
-using KoalaBear = Mont31<2130706433u, 3u, 3u, 24, 1, 24>;
+using KoalaBear = Mont31<2130706433u, 3u, 3u, 24, 1>;
 
 // Montgomery product: (a*b - m*p) / 2^32 with m = (a*b) * p^-1 mod 2^32; the low
 // words cancel exactly, so only the high halves are subtracted.
@@ -50,11 +46,7 @@ template <class F>
 ZC_HD uint32_t mmul(uint32_t a, uint32_t b) {
   uint64_t t = (uint64_t)a * b;
   uint32_t lo = (uint32_t)t, hi = (uint32_t)(t >> 32);
-#if defined(__CUDA_ARCH__) && defined(ZC_MU_SHIFT)
-  uint32_t m = lo + (lo << F::MU_S) + (lo << 31);
-#else
   uint32_t m = lo * F::MU;
-#endif
 #ifdef __CUDA_ARCH__
   uint32_t mp = __umulhi(m, F::P);
 #else

@@ -195,6 +195,64 @@ ZC_HD void p2_compress(const uint32_t* l, const uint32_t* r, uint32_t* out,
   for (int i = 0; i < 8; i++) out[i] = s[i];
 }
 
+// ------------------------------------------------------------- quads ----
+// The same permutation spread over a quad of lanes (lanes 4g .. 4g+3 of a
+// warp): lane q of the quad holds state words 4q .. 4q+3, i.e. one M4 block.
+// The M4 products are lane-local; the external layer's lane-class sums and the
+// internal layer's full sum are butterflies over lane ^ 1 and lane ^ 2, which
+// stay inside the quad. One thread's permutation is a dependency chain of
+// ~7000 instructions; the quad's is about a quarter of that, so the latency-
+// bound parts of a commit (the narrow top levels of a tree, the transcript)
+// use quads. Constants come from a P2Params in shared memory, so the built-in
+// instance uses its generic (Montgomery-diagonal) form here. Every lane of the
+// warp must make the call (full-warp shuffles), active quad or not.
+template <class F>
+__device__ __forceinline__ uint32_t quad_sum(uint32_t v) {
+  v = madd<F>(v, __shfl_xor_sync(0xffffffffu, v, 1));
+  return madd<F>(v, __shfl_xor_sync(0xffffffffu, v, 2));
+}
+
+template <class F>
+__device__ __forceinline__ void quad_ext_linear(uint32_t* x) {
+  const uint32_t t01 = madd<F>(x[0], x[1]), t23 = madd<F>(x[2], x[3]);
+  const uint32_t t0123 = madd<F>(t01, t23);
+  const uint32_t t01123 = madd<F>(t0123, x[1]), t01233 = madd<F>(t0123, x[3]);
+  const uint32_t y3 = madd<F>(t01233, madd<F>(x[0], x[0]));
+  const uint32_t y1 = madd<F>(t01123, madd<F>(x[2], x[2]));
+  const uint32_t y0 = madd<F>(t01123, t01);
+  const uint32_t y2 = madd<F>(t01233, t23);
+  x[0] = madd<F>(y0, quad_sum<F>(y0));
+  x[1] = madd<F>(y1, quad_sum<F>(y1));
+  x[2] = madd<F>(y2, quad_sum<F>(y2));
+  x[3] = madd<F>(y3, quad_sum<F>(y3));
+}
+
+template <class F>
+__device__ __forceinline__ void p2_permute_quad(uint32_t* x, int q, const RtParams<F>& k) {
+  quad_ext_linear<F>(x);
+#pragma unroll 1
+  for (int r = 0; r < k.rf_half(); r++) {
+#pragma unroll
+    for (int j = 0; j < 4; j++) x[j] = k.sbox(madd<F>(x[j], k.ei(r, 4 * q + j)));
+    quad_ext_linear<F>(x);
+  }
+#pragma unroll 1
+  for (int r = 0; r < k.rp(); r++) {
+    const uint32_t s0 = k.sbox(madd<F>(x[0], k.ir(r)));
+    x[0] = q == 0 ? s0 : x[0];
+    const uint32_t sum =
+        k.jsum(quad_sum<F>(madd<F>(madd<F>(x[0], x[1]), madd<F>(x[2], x[3]))));
+#pragma unroll
+    for (int j = 0; j < 4; j++) x[j] = madd<F>(sum, mmul<F>(k.dg(4 * q + j), x[j]));
+  }
+#pragma unroll 1
+  for (int r = 0; r < k.rf_half(); r++) {
+#pragma unroll
+    for (int j = 0; j < 4; j++) x[j] = k.sbox(madd<F>(x[j], k.et(r, 4 * q + j)));
+    quad_ext_linear<F>(x);
+  }
+}
+
 // Stage run-time params into shared memory (whole block participates).
 __device__ __forceinline__ void stage_params(P2Params* dst, const P2Params* src) {
   const uint32_t* s = reinterpret_cast<const uint32_t*>(src);

@@ -61,15 +61,18 @@ struct Duplex {
 // _observe_body (zorch/transcript.py:637-748): the stream in_buf[0:in_pos] ++
 // values is absorbed a full rate block at a time (overwrite sponge[0:8],
 // permute); the tail stays pending; a fresh output iff no tail remains.
-template <class K>
-ZC_HD void duplex_observe(Duplex& t, const uint32_t* v, int64_t m, const K& k) {
+// `perm(s)` permutes the 16-word sponge in place: one thread on the host, a
+// quad of lanes on the device (QuadPerm).
+#pragma nv_exec_check_disable
+template <class Perm>
+ZC_HD void duplex_observe(Duplex& t, const uint32_t* v, int64_t m, const Perm& perm) {
   if (m <= 0) return;
   int pos = t.in_pos & 7;  // a corrupt caller state cannot index past the buffer
   for (int64_t i = 0; i < m; i++) {
     t.in_buf[pos++] = v[i];
     if (pos == 8) {
       for (int j = 0; j < 8; j++) t.sponge[j] = t.in_buf[j];
-      p2_permute(t.sponge, k);
+      perm(t.sponge);
       pos = 0;
     }
   }
@@ -86,14 +89,15 @@ ZC_HD void duplex_observe(Duplex& t, const uint32_t* v, int64_t m, const K& k) {
 
 // _sample_one (zorch/transcript.py:370-387) n times; _duplexing (:299-313)
 // merges the pending prefix over sponge[0:in_pos] (:154-163) and permutes.
-template <class K>
-ZC_HD void duplex_sample(Duplex& t, int n, uint32_t* out, const K& k) {
+#pragma nv_exec_check_disable
+template <class Perm>
+ZC_HD void duplex_sample(Duplex& t, int n, uint32_t* out, const Perm& perm) {
   t.in_pos &= 7;
   if (t.out_pos < 0 || t.out_pos > 8) t.out_pos = 0;
   for (int i = 0; i < n; i++) {
     if (t.in_pos > 0 || t.out_pos == 0) {
       for (int j = 0; j < t.in_pos; j++) t.sponge[j] = t.in_buf[j];
-      p2_permute(t.sponge, k);
+      perm(t.sponge);
       for (int j = 0; j < 8; j++) {
         t.in_buf[j] = 0;
         t.out_buf[j] = t.sponge[j];
@@ -107,33 +111,63 @@ ZC_HD void duplex_sample(Duplex& t, int n, uint32_t* out, const K& k) {
 }
 
 template <class K>
-__global__ void k_duplex_step(const P2Params* rt, uint32_t* state, const uint32_t* values,
-                              int64_t m, int n, uint32_t* out, int32_t* positions,
-                              int64_t block_len) {
+struct HostPerm {
+  const K& k;
+  void operator()(uint32_t* s) const { p2_permute(s, k); }
+};
+
+// Every lane of the (single) warp holds the same Duplex state and runs the same
+// control flow; a permutation runs on each quad (all quads compute the same
+// result) and is gathered back into every lane's copy.
+template <class F>
+struct QuadPerm {
+  RtParams<F> k;
+  __device__ void operator()(uint32_t* s) const {
+    const int lane = threadIdx.x & 31, q = lane & 3;
+    uint32_t x[4];
+#pragma unroll
+    for (int j = 0; j < 4; j++) x[j] = s[4 * q + j];
+    p2_permute_quad(x, q, k);
+#pragma unroll
+    for (int qq = 0; qq < 4; qq++)
+#pragma unroll
+      for (int j = 0; j < 4; j++) s[4 * qq + j] = __shfl_sync(0xffffffffu, x[j], (lane & ~3) | qq);
+  }
+};
+
+// One warp; lane 0 writes the results.
+template <class K>
+__global__ void __launch_bounds__(32) k_duplex_step(const P2Params* rt, uint32_t* state,
+                                                    const uint32_t* values, int64_t m, int n,
+                                                    uint32_t* out, int32_t* positions,
+                                                    int64_t block_len) {
   __shared__ P2Params s_rt;
-  K k = KIn<K>::make(rt, &s_rt);
-  if (threadIdx.x != 0) return;
+  KIn<K>::make(rt, &s_rt);
+  const QuadPerm<typename K::F> perm{KIn<K>::quad(rt, &s_rt)};
   Duplex t;
   memcpy(&t, state, sizeof(Duplex));
-  duplex_observe(t, values, m, k);
+  duplex_observe(t, values, m, perm);
   for (int i = 0; i < n; i++) {
     uint32_t w;
-    duplex_sample(t, 1, &w, k);
-    if (out) out[i] = w;
-    if (positions) positions[i] = (int32_t)(w % (uint32_t)block_len);
+    duplex_sample(t, 1, &w, perm);
+    if (threadIdx.x == 0) {
+      if (out) out[i] = w;
+      if (positions) positions[i] = (int32_t)(w % (uint32_t)block_len);
+    }
   }
-  memcpy(state, &t, sizeof(Duplex));
+  __syncwarp();
+  if (threadIdx.x == 0) memcpy(state, &t, sizeof(Duplex));
 }
 
 template <class K>
-__global__ void k_duplex_hop(const P2Params* rt, const uint32_t* in_buf, const uint32_t* out_buf,
-                             const uint32_t* sponge, const uint32_t* in_pos,
-                             const uint32_t* out_pos, const uint32_t* values, int64_t m, int n,
-                             uint32_t* in_buf_o, uint32_t* out_buf_o, uint32_t* sponge_o,
-                             uint32_t* in_pos_o, uint32_t* out_pos_o, uint32_t* chal) {
+__global__ void __launch_bounds__(32) k_duplex_hop(
+    const P2Params* rt, const uint32_t* in_buf, const uint32_t* out_buf, const uint32_t* sponge,
+    const uint32_t* in_pos, const uint32_t* out_pos, const uint32_t* values, int64_t m, int n,
+    uint32_t* in_buf_o, uint32_t* out_buf_o, uint32_t* sponge_o, uint32_t* in_pos_o,
+    uint32_t* out_pos_o, uint32_t* chal) {
   __shared__ P2Params s_rt;
-  K k = KIn<K>::make(rt, &s_rt);
-  if (threadIdx.x != 0) return;
+  KIn<K>::make(rt, &s_rt);
+  const QuadPerm<typename K::F> perm{KIn<K>::quad(rt, &s_rt)};
   Duplex t;
   for (int j = 0; j < 8; j++) {
     t.in_buf[j] = in_buf[j];
@@ -142,8 +176,15 @@ __global__ void k_duplex_hop(const P2Params* rt, const uint32_t* in_buf, const u
   for (int j = 0; j < 16; j++) t.sponge[j] = sponge[j];
   t.in_pos = (int32_t)in_pos[0];
   t.out_pos = (int32_t)out_pos[0];
-  duplex_observe(t, values, m, k);
-  for (int i = 0; i < n; i++) duplex_sample(t, 1, chal + i, k);
+  duplex_observe(t, values, m, perm);
+  for (int i = 0; i < n; i++) {
+    uint32_t w;
+    duplex_sample(t, 1, &w, perm);
+    if (threadIdx.x == 0) chal[i] = w;
+  }
+  // inputs may alias outputs: every lane has read them by now
+  __syncwarp();
+  if (threadIdx.x != 0) return;
   for (int j = 0; j < 8; j++) {
     in_buf_o[j] = t.in_buf[j];
     out_buf_o[j] = t.out_buf[j];
@@ -413,13 +454,15 @@ zc_status zc_duplex_hop_host(const zc_poseidon2* p, const uint32_t* in_buf,
   t.out_pos = (int32_t)out_pos[0];
   if (t.in_pos < 0 || t.in_pos >= 8 || t.out_pos < 0 || t.out_pos > 8) return ZC_BAD_ARG;
   if (p->field == ZC_FIELD_BABYBEAR) {
-    RtParams<BabyBear> k{&p->host};
-    duplex_observe(t, values, m, k);
-    duplex_sample(t, n, challenges, k);
+    const RtParams<BabyBear> k{&p->host};
+    const HostPerm<RtParams<BabyBear>> perm{k};
+    duplex_observe(t, values, m, perm);
+    duplex_sample(t, n, challenges, perm);
   } else {
-    RtParams<KoalaBear> k{&p->host};
-    duplex_observe(t, values, m, k);
-    duplex_sample(t, n, challenges, k);
+    const RtParams<KoalaBear> k{&p->host};
+    const HostPerm<RtParams<KoalaBear>> perm{k};
+    duplex_observe(t, values, m, perm);
+    duplex_sample(t, n, challenges, perm);
   }
   memcpy(in_buf_o, t.in_buf, 32);
   memcpy(out_buf_o, t.out_buf, 32);

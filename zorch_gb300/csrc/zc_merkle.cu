@@ -10,6 +10,8 @@
 // openings, zorch/commit/merkle.py:187-202) without reading a level back.
 #include <string.h>
 
+#include <type_traits>
+
 #include "internal.cuh"
 
 namespace zc {
@@ -101,9 +103,18 @@ struct FoldMath {
   }
 };
 
-// Leaf p of the next layer's pair tree: (g[p], g[p + n/4]), computed from the
-// current layer f (n elements) and written to g on the way.
-template <class F, int LI, int LB>
+__device__ __forceinline__ int64_t brev64(int64_t i, int bits) {
+  return bits ? (int64_t)(__brevll((unsigned long long)i) >> (64 - bits)) : 0;
+}
+
+// Leaf p of the next layer's pair tree, computed from the current layer f (n
+// elements) and written to g on the way. Natural order (BR = false): the leaf
+// is (g[p], g[p + n/4]), g[j] folded from (f[j], f[j + n/2]) at x_j = shift w^j.
+// Bit-reversed order (BR = true, BitReversedReedSolomon.fold,
+// zorch/coding/reed_solomon.py:484-492, 532-540): the leaf is (g[2p], g[2p+1]),
+// g[i] folded from (f[2i], f[2i+1]) at x_i = shift w^brev(i) (i read over
+// log2(n/2) bits); brev(2p+1) = brev(2p) + n/4, so x_{2p+1} = x_{2p} w^(n/4).
+template <class F, int LI, int LB, bool BR = false>
 struct FoldLeaf {
   using M = FoldMath<F, LI, LB>;
   static constexpr int LO = M::LO;
@@ -120,18 +131,28 @@ struct FoldLeaf {
     uint32_t bt[4];
 #pragma unroll
     for (int e = 0; e < LB; e++) bt[e] = __ldg(beta + e);
-    uint32_t x0 = mmul<F>(inv2s, mpow<F>(winv, (uint64_t)p));
-    uint32_t x1 = mmul<F>(x0, w4inv);
     uint32_t o0[4], o1[4];
-    M::fold(f, half, p, x0, bt, o0);
-    M::fold(f, half, p + quarter, x1, bt, o1);
+    int64_t i0, i1;
+    if (BR) {
+      const uint32_t x0 = mmul<F>(inv2s, mpow<F>(winv, (uint64_t)brev64(2 * p, ilog2_dev(half))));
+      M::fold(f + 4 * p * LI, 1, 0, x0, bt, o0);
+      M::fold(f + (4 * p + 2) * LI, 1, 0, mmul<F>(x0, w4inv), bt, o1);
+      i0 = 2 * p;
+      i1 = 2 * p + 1;
+    } else {
+      const uint32_t x0 = mmul<F>(inv2s, mpow<F>(winv, (uint64_t)p));
+      M::fold(f, half, p, x0, bt, o0);
+      M::fold(f, half, p + quarter, mmul<F>(x0, w4inv), bt, o1);
+      i0 = p;
+      i1 = p + quarter;
+    }
     uint32_t s[16];
 #pragma unroll
     for (int j = 0; j < 16; j++) s[j] = 0;
 #pragma unroll
     for (int e = 0; e < LO; e++) {
-      g[p * LO + e] = o0[e];
-      g[(p + quarter) * LO + e] = o1[e];
+      g[i0 * LO + e] = o0[e];
+      g[i1 * LO + e] = o1[e];
       s[e] = o0[e];
       s[LO + e] = o1[e];
     }
@@ -141,39 +162,82 @@ struct FoldLeaf {
   }
 };
 
+// Threads per CTA for a subtree of T first-level nodes: T/2 quads, so every
+// level above the first is one round of quad permutations; at least a warp.
+inline int subtree_threads(int T) { return 2 * T > 32 ? 2 * T : 32; }
+
+// Lanes q = 0, 1 of a quad hold output words 4q .. 4q+3 (16-byte aligned).
+__device__ __forceinline__ void quad_store(uint32_t* dst8, int q, const uint32_t* x) {
+  reinterpret_cast<uint4*>(dst8)[q] = make_uint4(x[0], x[1], x[2], x[3]);
+}
+
+// One subtree of T first-level nodes per CTA (blockDim = subtree_threads(T)):
+// the first level is T leaf digests (one thread each; for NodeLeaf, quads
+// compressing stored children), then every level up to the subtree root is
+// compressed by quads out of ping-pong shared-memory slots, each level written
+// to `layers`.
 template <class K, class Leaf>
-__global__ void __launch_bounds__(kMaxT) k_subtree(Leaf leaf, uint32_t* layers, int64_t L,
-                                                   int l0, const P2Params* rt) {
+__global__ void __launch_bounds__(2 * kMaxT) k_subtree(Leaf leaf, uint32_t* layers, int64_t L,
+                                                       int l0, int T, const P2Params* rt) {
   __shared__ P2Params s_rt;
-  __shared__ uint32_t sm[8 * kMaxT];  // [word][node]: conflict-free digest slots
+  __shared__ uint32_t sm[2][8 * kMaxT];  // [word][node] digest slots
   K k = KIn<K>::make(rt, &s_rt);
-  const int T = blockDim.x, t = threadIdx.x;
-  const int64_t p = (int64_t)blockIdx.x * T + t;
-  uint32_t d[8];
-  leaf.digest(p, d, k);
-  store_digest(layers + 8 * (level_offset(L, l0) + p), d);
+  const RtParams<typename K::F> kq = KIn<K>::quad(rt, &s_rt);
+  const int t = threadIdx.x, q = t & 3, qi = t >> 2, Q = blockDim.x >> 2;
+  const int64_t base = (int64_t)blockIdx.x * T;
+  uint32_t* lay0 = layers + 8 * (level_offset(L, l0) + base);
+  // A warp whose 8 quads are all past the level's width skips the round (a
+  // warp-uniform branch: the quad shuffles need every lane of a running warp).
+  const int warp_q0 = (t >> 5) * 8;
+  if constexpr (std::is_same<Leaf, NodeLeaf>::value) {
+    for (int r = 0; r < T; r += Q) {
+      const int node = r + qi;
+      if (r + warp_q0 >= T) continue;
+      uint32_t x[4] = {0, 0, 0, 0};
+      if (node < T) {
+        const uint4 v = reinterpret_cast<const uint4*>(leaf.in + 16 * (base + node))[q];
+        x[0] = v.x, x[1] = v.y, x[2] = v.z, x[3] = v.w;
+      }
+      p2_permute_quad(x, q, kq);
+      if (node < T && q < 2) {
+        quad_store(lay0 + 8 * node, q, x);
 #pragma unroll
-  for (int i = 0; i < 8; i++) sm[i * kMaxT + t] = d[i];
-  int lvl = l0, width = T;
+        for (int j = 0; j < 4; j++) sm[0][(4 * q + j) * kMaxT + node] = x[j];
+      }
+    }
+  } else {
+    if (t < T) {
+      uint32_t d[8];
+      leaf.digest(base + t, d, k);
+      store_digest(lay0 + 8 * t, d);
+#pragma unroll
+      for (int i = 0; i < 8; i++) sm[0][i * kMaxT + t] = d[i];
+    }
+  }
+  int cur = 0, lvl = l0, width = T;
   while (width > 1) {
     __syncthreads();
     width >>= 1;
     lvl++;
-    uint32_t a[8], b[8];
-    if (t < width) {
+    uint32_t* lay = layers + 8 * (level_offset(L, lvl) + (int64_t)blockIdx.x * width);
+    for (int r = 0; r < width; r += Q) {
+      const int node = r + qi;
+      if (r + warp_q0 >= width) continue;
+      // quad state = child(2 node) || child(2 node + 1); lane q: words 4q .. 4q+3
+      const int child = 2 * node + (q >> 1), w0 = 4 * (q & 1);
+      uint32_t x[4] = {0, 0, 0, 0};
+      if (node < width) {
 #pragma unroll
-      for (int i = 0; i < 8; i++) {
-        a[i] = sm[i * kMaxT + 2 * t];
-        b[i] = sm[i * kMaxT + 2 * t + 1];
+        for (int j = 0; j < 4; j++) x[j] = sm[cur][(w0 + j) * kMaxT + child];
+      }
+      p2_permute_quad(x, q, kq);
+      if (node < width && q < 2) {
+        quad_store(lay + 8 * node, q, x);
+#pragma unroll
+        for (int j = 0; j < 4; j++) sm[cur ^ 1][(4 * q + j) * kMaxT + node] = x[j];
       }
     }
-    __syncthreads();
-    if (t < width) {
-      p2_compress(a, b, d, k);
-      store_digest(layers + 8 * (level_offset(L, lvl) + (int64_t)blockIdx.x * width + t), d);
-#pragma unroll
-      for (int i = 0; i < 8; i++) sm[i * kMaxT + t] = d[i];
-    }
+    cur ^= 1;
   }
 }
 
@@ -213,7 +277,8 @@ zc_status finish_tree(uint32_t* layers, int64_t L, int l_done, const P2Params* r
       continue;
     }
     const int T = parents < kMaxT ? (int)parents : kMaxT;
-    k_subtree<K, NodeLeaf><<<(unsigned)(parents / T), T, 0, st>>>(nl, layers, L, l + 1, rt);
+    k_subtree<K, NodeLeaf><<<(unsigned)(parents / T), subtree_threads(T), 0, st>>>(
+        nl, layers, L, l + 1, T, rt);
     ZC_TRY(launch_check());
     l += 1 + ilog2(T);
   }
@@ -229,7 +294,8 @@ zc_status commit_tree(const Leaf& leaf, uint32_t* layers, int64_t L, const P2Par
     return finish_tree<K>(layers, L, 0, rt, st);
   }
   const int T0 = L < kMaxT ? (int)L : kMaxT;
-  k_subtree<K, Leaf><<<(unsigned)(L / T0), T0, 0, st>>>(leaf, layers, L, 0, rt);
+  k_subtree<K, Leaf><<<(unsigned)(L / T0), subtree_threads(T0), 0, st>>>(leaf, layers, L, 0, T0,
+                                                                         rt);
   ZC_TRY(launch_check());
   return finish_tree<K>(layers, L, ilog2(T0), rt, st);
 }
@@ -255,7 +321,7 @@ __global__ void k_open(zc_leaves lv, const uint32_t* layers, const int32_t* idx,
   }
 }
 
-template <class F, int LI, int LB>
+template <class F, int LI, int LB, bool BR>
 __global__ void k_fold(const uint32_t* f, int64_t n, const uint32_t* beta, uint32_t inv2s,
                        uint32_t winv, uint32_t* g) {
   using M = FoldMath<F, LI, LB>;
@@ -266,7 +332,11 @@ __global__ void k_fold(const uint32_t* f, int64_t n, const uint32_t* beta, uint3
 #pragma unroll
   for (int e = 0; e < LB; e++) bt[e] = __ldg(beta + e);
   uint32_t out[4];
-  M::fold(f, half, j, mmul<F>(inv2s, mpow<F>(winv, (uint64_t)j)), bt, out);
+  if (BR)  // pair (f[2j], f[2j+1]) at x_j = shift w^brev(j)
+    M::fold(f + 2 * j * LI, 1, 0,
+            mmul<F>(inv2s, mpow<F>(winv, (uint64_t)brev64(j, ilog2_dev(half)))), bt, out);
+  else
+    M::fold(f, half, j, mmul<F>(inv2s, mpow<F>(winv, (uint64_t)j)), bt, out);
 #pragma unroll
   for (int e = 0; e < M::LO; e++) g[j * M::LO + e] = out[e];
 }
@@ -291,27 +361,60 @@ zc_status fold_scalars(int64_t n, uint32_t shift_mont, uint32_t generator, FoldS
   return ZC_OK;
 }
 
-template <class F, int LI, int LB>
+template <class F, int LI, int LB, bool BR>
 zc_status fold_launch(const uint32_t* cw, int64_t n, const uint32_t* beta, uint32_t shift_mont,
                       uint32_t generator, uint32_t* out, cudaStream_t st) {
   FoldScalars<F> fs;
   ZC_TRY(fold_scalars<F>(n, shift_mont, generator, &fs));
   const int64_t half = n >> 1;
   const int B = 256;
-  k_fold<F, LI, LB><<<(unsigned)((half + B - 1) / B), B, 0, st>>>(cw, n, beta, fs.inv2s, fs.winv,
-                                                                  out);
+  k_fold<F, LI, LB, BR><<<(unsigned)((half + B - 1) / B), B, 0, st>>>(cw, n, beta, fs.inv2s,
+                                                                      fs.winv, out);
   return launch_check();
 }
 
-template <class K, int LI, int LB>
+template <class K, int LI, int LB, bool BR>
 zc_status fold_commit_launch(const uint32_t* cw, int64_t n, const uint32_t* beta,
                              uint32_t shift_mont, uint32_t generator, uint32_t* out,
                              uint32_t* layers, const P2Params* rt, cudaStream_t st) {
   using F = typename K::F;
   FoldScalars<F> fs;
   ZC_TRY(fold_scalars<F>(n, shift_mont, generator, &fs));
-  FoldLeaf<F, LI, LB> leaf{cw, out, beta, n, fs.inv2s, fs.winv, fs.w4inv};
+  FoldLeaf<F, LI, LB, BR> leaf{cw, out, beta, n, fs.inv2s, fs.winv, fs.w4inv};
   return commit_tree<K>(leaf, layers, n >> 2, rt, st);
+}
+
+// compress([raw_root, sponge([log_height, width])]) on one warp's quads.
+template <class K>
+__global__ void __launch_bounds__(32) k_bind_root(const P2Params* rt, const uint32_t* raw_root,
+                                                  uint32_t log_height, uint32_t width,
+                                                  uint32_t* out) {
+  using F = typename K::F;
+  __shared__ P2Params s_rt;
+  KIn<K>::make(rt, &s_rt);
+  const RtParams<F> kq = KIn<K>::quad(rt, &s_rt);
+  const int lane = threadIdx.x & 31, q = lane & 3;
+  // sponge: state = [log_height, width, 0 ...] (one absorb block), permute
+  uint32_t x[4] = {0, 0, 0, 0};
+  if (q == 0) {
+    x[0] = to_mont<F>(log_height);
+    x[1] = to_mont<F>(width);
+  }
+  p2_permute_quad(x, q, kq);
+  // compress: state = raw_root || params (params = words 0..7, lanes q = 0, 1)
+  uint32_t y[4];
+  const uint32_t from2 = __shfl_sync(0xffffffffu, x[0], (lane & ~3) | (q & 1)),
+                 from2b = __shfl_sync(0xffffffffu, x[1], (lane & ~3) | (q & 1)),
+                 from2c = __shfl_sync(0xffffffffu, x[2], (lane & ~3) | (q & 1)),
+                 from2d = __shfl_sync(0xffffffffu, x[3], (lane & ~3) | (q & 1));
+  if (q < 2) {
+#pragma unroll
+    for (int j = 0; j < 4; j++) y[j] = raw_root[4 * q + j];
+  } else {
+    y[0] = from2, y[1] = from2b, y[2] = from2c, y[3] = from2d;
+  }
+  p2_permute_quad(y, q, kq);
+  if (lane < 2) quad_store(out, q, y);
 }
 
 // ------------------------------------------------------------ batched ----
@@ -387,38 +490,46 @@ __global__ void __launch_bounds__(kMaxT) k_tree_batch(const __grid_constant__ Tr
   }
 }
 
-// One CTA per tree: level `top` (<= 256 nodes, already stored) to the root.
+// One CTA per tree: level `top` (<= 256 nodes, already stored) to the root,
+// each level one round of quad permutations (2 * kMaxT threads = 128 quads).
 template <class K>
-__global__ void __launch_bounds__(kMaxT) k_tree_top(const __grid_constant__ TreeBatch B,
-                                                    const P2Params* rt) {
+__global__ void __launch_bounds__(2 * kMaxT) k_tree_top(const __grid_constant__ TreeBatch B,
+                                                        const P2Params* rt) {
   __shared__ P2Params s_rt;
-  __shared__ uint32_t sm[8 * kMaxT];
-  K k = KIn<K>::make(rt, &s_rt);
+  __shared__ uint32_t sm[2][8 * kMaxT];
+  KIn<K>::make(rt, &s_rt);
+  const RtParams<typename K::F> kq = KIn<K>::quad(rt, &s_rt);
   const TreeJobDev& J = B.job[blockIdx.x];
   int lvl = J.top;
   int width = (int)(J.L >> lvl);
   const uint32_t* src = J.layers + 8 * level_offset(J.L, lvl);
-  for (int i = threadIdx.x; i < width * 8; i += blockDim.x) sm[(i & 7) * kMaxT + (i >> 3)] = src[i];
-  const int t = threadIdx.x;
+  for (int i = threadIdx.x; i < width * 8; i += blockDim.x)
+    sm[0][(i & 7) * kMaxT + (i >> 3)] = src[i];
+  const int q = threadIdx.x & 3, qi = threadIdx.x >> 2, Q = blockDim.x >> 2;
+  const int warp_q0 = (threadIdx.x >> 5) * 8;
+  int cur = 0;
   while (width > 1) {
     __syncthreads();
     width >>= 1;
     lvl++;
-    uint32_t a[8], b[8], d[8];
-    if (t < width) {
+    uint32_t* lay = J.layers + 8 * level_offset(J.L, lvl);
+    for (int r = 0; r < width; r += Q) {
+      const int node = r + qi;
+      if (r + warp_q0 >= width) continue;  // whole warp idle this round
+      const int child = 2 * node + (q >> 1), w0 = 4 * (q & 1);
+      uint32_t x[4] = {0, 0, 0, 0};
+      if (node < width) {
 #pragma unroll
-      for (int i = 0; i < 8; i++) {
-        a[i] = sm[i * kMaxT + 2 * t];
-        b[i] = sm[i * kMaxT + 2 * t + 1];
+        for (int j = 0; j < 4; j++) x[j] = sm[cur][(w0 + j) * kMaxT + child];
+      }
+      p2_permute_quad(x, q, kq);
+      if (node < width && q < 2) {
+        quad_store(lay + 8 * node, q, x);
+#pragma unroll
+        for (int j = 0; j < 4; j++) sm[cur ^ 1][(4 * q + j) * kMaxT + node] = x[j];
       }
     }
-    __syncthreads();
-    if (t < width) {
-      p2_compress(a, b, d, k);
-      store_digest(J.layers + 8 * (level_offset(J.L, lvl) + t), d);
-#pragma unroll
-      for (int i = 0; i < 8; i++) sm[i * kMaxT + t] = d[i];
-    }
+    cur ^= 1;
   }
 }
 
@@ -466,7 +577,7 @@ zc_status tree_batch_wave(const zc_merkle_job* jobs, int n, unsigned long long* 
       k_tree_batch<K, 1><<<(unsigned)grid, kMaxT, 0, st>>>(B, ctr + l, rt);
     ZC_TRY(launch_check());
   }
-  k_tree_top<K><<<n, kMaxT / 2, 0, st>>>(B, rt);
+  k_tree_top<K><<<n, 2 * kMaxT, 0, st>>>(B, rt);
   return launch_check();
 }
 
@@ -523,6 +634,36 @@ __global__ void k_fill_uniform(uint32_t* out, int64_t n, uint64_t seed, uint32_t
     out[i] = (uint32_t)(splitmix64(seed * 0x100000001B3ull + (uint64_t)i) % p);
 }
 
+template <bool BR>
+zc_status fri_fold_any(zc_field field, const uint32_t* cw, int64_t n, int ef_in,
+                       const uint32_t* beta, int ef_beta, uint32_t shift_mont, uint32_t generator,
+                       uint32_t* out, cudaStream_t st) {
+  return with_field(field, [&](auto f) {
+    using F = decltype(f);
+    if (ef_in && ef_beta)
+      return fold_launch<F, 4, 4, BR>(cw, n, beta, shift_mont, generator, out, st);
+    if (ef_in) return fold_launch<F, 4, 1, BR>(cw, n, beta, shift_mont, generator, out, st);
+    if (ef_beta) return fold_launch<F, 1, 4, BR>(cw, n, beta, shift_mont, generator, out, st);
+    return fold_launch<F, 1, 1, BR>(cw, n, beta, shift_mont, generator, out, st);
+  });
+}
+
+template <bool BR>
+zc_status fold_commit_any(const zc_poseidon2* p, const uint32_t* cw, int64_t n, int ef_in,
+                          const uint32_t* beta, int ef_beta, uint32_t shift_mont,
+                          uint32_t generator, uint32_t* out, uint32_t* layers, cudaStream_t st) {
+  return with_perm(p, [&](auto k, const P2Params* rt) {
+    using K = decltype(k);
+    if (ef_in && ef_beta)
+      return fold_commit_launch<K, 4, 4, BR>(cw, n, beta, shift_mont, generator, out, layers, rt, st);
+    if (ef_in)
+      return fold_commit_launch<K, 4, 1, BR>(cw, n, beta, shift_mont, generator, out, layers, rt, st);
+    if (ef_beta)
+      return fold_commit_launch<K, 1, 4, BR>(cw, n, beta, shift_mont, generator, out, layers, rt, st);
+    return fold_commit_launch<K, 1, 1, BR>(cw, n, beta, shift_mont, generator, out, layers, rt, st);
+  });
+}
+
 }  // namespace zc
 
 using namespace zc;
@@ -565,14 +706,20 @@ zc_status zc_fri_fold(zc_field field, const uint32_t* cw, int64_t n, int ef_in,
     set_error("fri_fold requires a power-of-two codeword of length >= 2");
     return ZC_NOT_POW2;
   }
-  cudaStream_t st = (cudaStream_t)stream;
-  return with_field(field, [&](auto f) {
-    using F = decltype(f);
-    if (ef_in && ef_beta) return fold_launch<F, 4, 4>(cw, n, beta, shift_mont, generator, out, st);
-    if (ef_in) return fold_launch<F, 4, 1>(cw, n, beta, shift_mont, generator, out, st);
-    if (ef_beta) return fold_launch<F, 1, 4>(cw, n, beta, shift_mont, generator, out, st);
-    return fold_launch<F, 1, 1>(cw, n, beta, shift_mont, generator, out, st);
-  });
+  return fri_fold_any<false>(field, cw, n, ef_in, beta, ef_beta, shift_mont, generator, out,
+                             (cudaStream_t)stream);
+}
+
+zc_status zc_fri_fold_bitrev(zc_field field, const uint32_t* cw, int64_t n, int ef_in,
+                             const uint32_t* beta, int ef_beta, uint32_t shift_mont,
+                             uint32_t generator, uint32_t* out, void* stream) {
+  if (!cw || !beta || !out) return ZC_BAD_ARG;
+  if (!is_pow2(n) || n < 2) {
+    set_error("fri_fold requires a power-of-two codeword of length >= 2");
+    return ZC_NOT_POW2;
+  }
+  return fri_fold_any<true>(field, cw, n, ef_in, beta, ef_beta, shift_mont, generator, out,
+                            (cudaStream_t)stream);
 }
 
 zc_status zc_fri_fold_commit(const zc_poseidon2* p, const uint32_t* cw, int64_t n, int ef_in,
@@ -585,16 +732,32 @@ zc_status zc_fri_fold_commit(const zc_poseidon2* p, const uint32_t* cw, int64_t 
     return ZC_NOT_POW2;
   }
   if ((uintptr_t)next_layers % 16) return ZC_BAD_ARG;
+  return fold_commit_any<false>(p, cw, n, ef_in, beta, ef_beta, shift_mont, generator, out,
+                                next_layers, (cudaStream_t)stream);
+}
+
+zc_status zc_fri_fold_commit_bitrev(const zc_poseidon2* p, const uint32_t* cw, int64_t n,
+                                    int ef_in, const uint32_t* beta, int ef_beta,
+                                    uint32_t shift_mont, uint32_t generator, uint32_t* out,
+                                    uint32_t* next_layers, void* stream) {
+  if (!cw || !beta || !out || !next_layers) return ZC_BAD_ARG;
+  if (!is_pow2(n) || n < 4) {
+    set_error("fri_fold_commit requires a power-of-two codeword of length >= 4");
+    return ZC_NOT_POW2;
+  }
+  if ((uintptr_t)next_layers % 16) return ZC_BAD_ARG;
+  return fold_commit_any<true>(p, cw, n, ef_in, beta, ef_beta, shift_mont, generator, out,
+                               next_layers, (cudaStream_t)stream);
+}
+
+zc_status zc_smcs_bind_root(const zc_poseidon2* p, const uint32_t* raw_root, uint32_t log_height,
+                            uint32_t width, uint32_t* out, void* stream) {
+  if (!raw_root || !out || ((uintptr_t)out % 16)) return ZC_BAD_ARG;
   cudaStream_t st = (cudaStream_t)stream;
   return with_perm(p, [&](auto k, const P2Params* rt) {
     using K = decltype(k);
-    if (ef_in && ef_beta)
-      return fold_commit_launch<K, 4, 4>(cw, n, beta, shift_mont, generator, out, next_layers, rt, st);
-    if (ef_in)
-      return fold_commit_launch<K, 4, 1>(cw, n, beta, shift_mont, generator, out, next_layers, rt, st);
-    if (ef_beta)
-      return fold_commit_launch<K, 1, 4>(cw, n, beta, shift_mont, generator, out, next_layers, rt, st);
-    return fold_commit_launch<K, 1, 1>(cw, n, beta, shift_mont, generator, out, next_layers, rt, st);
+    k_bind_root<K><<<1, 32, 0, st>>>(rt, raw_root, log_height, width, out);
+    return launch_check();
   });
 }
 

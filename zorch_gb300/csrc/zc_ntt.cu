@@ -13,9 +13,16 @@
 //    per CTA), multiplies by w_k^(i1*t2) and writes a [b][k2][k1] intermediate
 //    to the caller's workspace; pass 2 runs the k1-point NTTs along its rows
 //    for all b cosets of a t2 tile and writes contiguous b*TT runs of out.
-// In shared memory the transform is an iterative radix-2 DIT whose input is
-// stored bit-reversed as it is loaded (the bit reversal folded into the load),
-// processed 4 stages per register pass (16 elements per thread).
+// In shared memory the transform is a radix-2 decimation-in-frequency NTT
+// (natural order in, bit-reversed order out), processed in balanced register
+// passes of up to 4 stages.
+//
+// Bit-reversed codewords (BitReversedReedSolomon.encode,
+// zorch/coding/reed_solomon.py:476-478) cost nothing extra: with n = b*k and
+// j = b*t + s, brev_n(j) = brev_b(s)*k + brev_k(t), and with t = t2 + k2*t1 in
+// the four-step split brev_k(t) = brev_k2(t2)*k1 + brev_k1(t1) -- the second
+// term is exactly the position in the DIF output row. So each transformed row
+// lands as one contiguous run of the bit-reversed codeword.
 #include <string.h>
 
 #include <mutex>
@@ -158,7 +165,7 @@ constexpr int kThreads = 512;
 // Layout: work[b][rs] | tw[k/2] | hp[k] | wl[128] | wh[128].
 template <class F>
 __device__ void lde_small_body(const uint32_t* x, uint32_t* out, int log_k, int log_b,
-                               uint32_t h, int64_t c, uint32_t* sm) {
+                               uint32_t h, int64_t c, uint32_t* sm, int brev_out) {
   const int k = 1 << log_k, b = 1 << log_b, log_n = log_k + log_b;
   const int rs = row_stride(k);
   uint32_t* work = sm;
@@ -184,6 +191,13 @@ __device__ void lde_small_body(const uint32_t* x, uint32_t* out, int log_k, int 
   __syncthreads();
   smem_ntt_dif<F>(work, log_b, log_k, rs, tw);
   uint32_t* oc = out + (c << log_n);
+  if (brev_out) {  // out[brev_b(s) k + p] = row s, position p
+    for (int idx = threadIdx.x; idx < (b << log_k); idx += blockDim.x) {
+      const int s = brev(idx >> log_k, log_b), p = idx & (k - 1);
+      oc[idx] = work[s * rs + pad(p)];
+    }
+    return;
+  }
   for (int idx = threadIdx.x; idx < (b << log_k); idx += blockDim.x) {
     const int t = idx >> log_b, s = idx & (b - 1);
     oc[idx] = work[s * rs + pad(brev(t, log_k))];
@@ -192,9 +206,10 @@ __device__ void lde_small_body(const uint32_t* x, uint32_t* out, int log_k, int 
 
 template <class F>
 __global__ void __launch_bounds__(kThreads) k_lde_small(const uint32_t* x, uint32_t* out,
-                                                        int log_k, int log_b, uint32_t h) {
+                                                        int log_k, int log_b, uint32_t h,
+                                                        int brev_out) {
   extern __shared__ uint32_t sm[];
-  lde_small_body<F>(x, out, log_k, log_b, h, blockIdx.x, sm);
+  lde_small_body<F>(x, out, log_k, log_b, h, blockIdx.x, sm, brev_out);
 }
 
 // Pass 1 item (coset s, i1 tile, column c): the k2-point DIF NTTs down the
@@ -249,11 +264,13 @@ constexpr int kTwLoLog = 6;  // pass-2 twiddle tables: w^(t2 i1) = lo[i1 & 63] *
 // Pass 2 item (t2 tile, column c): rows (s, t2) for all b cosets and TT
 // values of t2; each row is multiplied by w_k^(t2 i1), transformed by a
 // k1-point DIF NTT, and written to out[b (t2 + k2 t1) + s] (t1 = bit-reversed
-// position) in contiguous runs of b*TT words.
+// position) in contiguous runs of b*TT words -- or, for a bit-reversed
+// codeword, row (s, t2) to the k1 contiguous words at brev_b(s) k + brev_k2(t2) k1.
 // Layout: work[b*TT][rs] | tw[k1/2] | lo[TT][64] | hi[TT][k1/64].
 template <class F>
 __device__ void lde_pass2_body(const uint32_t* z, uint32_t* out, int log_k1, int log_k2,
-                               int log_b, int log_tt, int tile, int64_t c, uint32_t* sm) {
+                               int log_b, int log_tt, int tile, int64_t c, uint32_t* sm,
+                               int brev_out) {
   const int k1 = 1 << log_k1, TT = 1 << log_tt;
   const int log_k = log_k1 + log_k2, log_n = log_k + log_b;
   const int log_rows = log_b + log_tt;
@@ -286,6 +303,15 @@ __device__ void lde_pass2_body(const uint32_t* z, uint32_t* out, int log_k1, int
   __syncthreads();
   smem_ntt_dif<F>(work, log_rows, log_k1, rs, tw);
   uint32_t* oc = out + (c << log_n);
+  if (brev_out) {
+    for (int idx = threadIdx.x; idx < (1 << (log_rows + log_k1)); idx += blockDim.x) {
+      const int p = idx & (k1 - 1), row = idx >> log_k1;
+      const int s = row >> log_tt, dt = row & (TT - 1);
+      oc[((int64_t)brev(s, log_b) << log_k) + ((int64_t)brev(t2_0 + dt, log_k2) << log_k1) + p] =
+          work[row * rs + pad(p)];
+    }
+    return;
+  }
   for (int idx = threadIdx.x; idx < (1 << (log_rows + log_k1)); idx += blockDim.x) {
     const int s = idx & ((1 << log_b) - 1), dt = (idx >> log_b) & (TT - 1);
     const int p = idx >> (log_b + log_tt);
@@ -297,9 +323,9 @@ __device__ void lde_pass2_body(const uint32_t* z, uint32_t* out, int log_k1, int
 template <class F>
 __global__ void __launch_bounds__(kThreads) k_lde_pass2(const uint32_t* z, uint32_t* out,
                                                         int log_k1, int log_k2, int log_b,
-                                                        int log_tt) {
+                                                        int log_tt, int brev_out) {
   extern __shared__ uint32_t sm[];
-  lde_pass2_body<F>(z, out, log_k1, log_k2, log_b, log_tt, blockIdx.x, blockIdx.y, sm);
+  lde_pass2_body<F>(z, out, log_k1, log_k2, log_b, log_tt, blockIdx.x, blockIdx.y, sm, brev_out);
 }
 
 struct LdePlan {
@@ -341,7 +367,8 @@ inline LdePlan plan_lde(int log_k, int log_b, int tile_log = 0) {
 
 template <class F>
 zc_status lde_launch(const uint32_t* x, int64_t batch, int log_k, int log_b, uint32_t h,
-                     uint32_t* out, void* ws, size_t ws_bytes, cudaStream_t st) {
+                     uint32_t* out, void* ws, size_t ws_bytes, cudaStream_t st,
+                     int brev_out = 0) {
   const LdePlan p = plan_lde(log_k, log_b);
   const int log_n = log_k + log_b;
   const size_t smem_cap = 227 * 1024;
@@ -356,7 +383,7 @@ zc_status lde_launch(const uint32_t* x, int64_t batch, int log_k, int log_b, uin
     for (int64_t c0 = 0; c0 < batch; c0 += 0x7fffffff) {
       const int64_t cols = batch - c0 < 0x7fffffff ? batch - c0 : 0x7fffffff;
       k_lde_small<F><<<(unsigned)cols, kThreads, p.smem_small, st>>>(
-          x + (c0 << log_k), out + (c0 << log_n), log_k, log_b, h);
+          x + (c0 << log_k), out + (c0 << log_n), log_k, log_b, h, brev_out);
       ZC_TRY(launch_check());
     }
     return ZC_OK;
@@ -383,7 +410,7 @@ zc_status lde_launch(const uint32_t* x, int64_t batch, int log_k, int log_b, uin
     ZC_TRY(launch_check());
     dim3 g2(1u << (p.log_k2 - p.log_tt), (unsigned)cols);
     k_lde_pass2<F><<<g2, kThreads, p.smem2, st>>>(z, out + (c0 << log_n), p.log_k1, p.log_k2,
-                                                  log_b, p.log_tt);
+                                                  log_b, p.log_tt, brev_out);
     ZC_TRY(launch_check());
   }
   return ZC_OK;
@@ -403,7 +430,7 @@ struct LdeJobDev {
   uint32_t* z;
   int64_t batch;
   uint32_t h;
-  int8_t log_k, log_b, log_k1, log_k2, log_ti, log_tt, small, pad_;
+  int8_t log_k, log_b, log_k1, log_k2, log_ti, log_tt, small, brev_out;
 };
 
 struct LdeBatch {
@@ -438,7 +465,7 @@ __global__ void __launch_bounds__(kThreads) k_lde_batch(const __grid_constant__ 
     const LdeJobDev& J = B.job[j];
     const int64_t local = it - B.prefix[j];
     if (B.phase == 0 && J.small) {
-      lde_small_body<F>(J.x, J.out, J.log_k, J.log_b, J.h, local, sm);
+      lde_small_body<F>(J.x, J.out, J.log_k, J.log_b, J.h, local, sm, J.brev_out);
     } else if (B.phase == 0) {
       const int b = 1 << J.log_b;
       const int64_t per_col = (int64_t)b << (J.log_k1 - J.log_ti);
@@ -450,7 +477,7 @@ __global__ void __launch_bounds__(kThreads) k_lde_batch(const __grid_constant__ 
       const int64_t tiles = (int64_t)1 << (J.log_k2 - J.log_tt);
       const int64_t c = local / tiles;
       lde_pass2_body<F>(J.z, J.out, J.log_k1, J.log_k2, J.log_b, J.log_tt,
-                        (int)(local - c * tiles), c, sm);
+                        (int)(local - c * tiles), c, sm, J.brev_out);
     }
     __syncthreads();  // the item's shared memory is free again
   }
@@ -488,6 +515,7 @@ zc_status lde_batch_wave(const zc_lde_job* jobs, int n, uint32_t* zbase, unsigne
     d.log_ti = (int8_t)p.log_ti;
     d.log_tt = (int8_t)p.log_tt;
     d.small = p.small ? 1 : 0;
+    d.brev_out = j.bit_reversed ? 1 : 0;
     d.z = p.small ? nullptr : z;
     if (!p.small) z += ((size_t)j.batch) << (j.log_k + j.log_blowup);
     B.prefix[i] = totA;
@@ -542,7 +570,8 @@ zc_status lde_batch_launch(const zc_lde_job* jobs, int njobs, void* ws, size_t w
     if (zi > zcap) {
       const zc_lde_job& j = jobs[i];
       ZC_TRY(lde_launch<F>(j.coeffs, j.batch, j.log_k, j.log_blowup,
-                           j.shift_mont ? j.shift_mont : F::ONE, j.out, zbase, zcap, st));
+                           j.shift_mont ? j.shift_mont : F::ONE, j.out, zbase, zcap, st,
+                           j.bit_reversed ? 1 : 0));
       i++;
       continue;
     }
@@ -608,9 +637,9 @@ size_t zc_rs_encode_workspace_bytes(int64_t batch, int log_k, int log_blowup) {
   return cols * col;
 }
 
-zc_status zc_rs_encode(zc_field field, const uint32_t* coeffs, int64_t batch, int log_k,
-                       int log_blowup, uint32_t shift_mont, uint32_t generator, uint32_t* out,
-                       void* workspace, size_t workspace_bytes, void* stream) {
+static zc_status rs_encode(zc_field field, const uint32_t* coeffs, int64_t batch, int log_k,
+                           int log_blowup, uint32_t shift_mont, uint32_t generator, uint32_t* out,
+                           void* workspace, size_t workspace_bytes, void* stream, int brev_out) {
   if (!coeffs || !out || batch < 0 || log_k < 0 || log_blowup < 0) return ZC_BAD_ARG;
   if (batch == 0) return ZC_OK;
   return with_field(field, [&](auto f) -> zc_status {
@@ -626,8 +655,23 @@ zc_status zc_rs_encode(zc_field field, const uint32_t* coeffs, int64_t batch, in
     ZC_TRY(ensure_init());
     const uint32_t h = shift_mont ? shift_mont : F::ONE;
     return lde_launch<F>(coeffs, batch, log_k, log_blowup, h, out, workspace, workspace_bytes,
-                         (cudaStream_t)stream);
+                         (cudaStream_t)stream, brev_out);
   });
+}
+
+zc_status zc_rs_encode(zc_field field, const uint32_t* coeffs, int64_t batch, int log_k,
+                       int log_blowup, uint32_t shift_mont, uint32_t generator, uint32_t* out,
+                       void* workspace, size_t workspace_bytes, void* stream) {
+  return rs_encode(field, coeffs, batch, log_k, log_blowup, shift_mont, generator, out,
+                   workspace, workspace_bytes, stream, 0);
+}
+
+zc_status zc_rs_encode_bitrev(zc_field field, const uint32_t* coeffs, int64_t batch, int log_k,
+                              int log_blowup, uint32_t shift_mont, uint32_t generator,
+                              uint32_t* out, void* workspace, size_t workspace_bytes,
+                              void* stream) {
+  return rs_encode(field, coeffs, batch, log_k, log_blowup, shift_mont, generator, out,
+                   workspace, workspace_bytes, stream, 1);
 }
 
 zc_status zc_rs_encode_noalloc(zc_field field, const uint32_t* coeffs, int64_t batch, int log_k,
