@@ -627,6 +627,115 @@ void orc_rlc_columns(int field, const uint32_t* cw, int64_t n, int w, const uint
   free(st);
 }
 
+/* ------------------------------------------------------------ sumcheck ---- */
+static void ef4_add(const fld* F, const uint32_t* a, const uint32_t* b, uint32_t* c) {
+  for (int e = 0; e < 4; e++) c[e] = fadd(F, a[e], b[e]);
+}
+static void ef4_sub(const fld* F, const uint32_t* a, const uint32_t* b, uint32_t* c) {
+  for (int e = 0; e < 4; e++) c[e] = fsub(F, a[e], b[e]);
+}
+
+/* a^(p^4 - 2) = a^-1 in EF4 (a != 0). */
+void orc_ef4_inv(int field, const uint32_t* a, uint32_t* out) {
+  const fld* F = FLD(field);
+  unsigned __int128 e = (unsigned __int128)F->p * F->p;
+  e = e * F->p * F->p - 2;
+  uint32_t r[4] = {F->one, 0, 0, 0}, b[4];
+  memcpy(b, a, 16);
+  while (e) {
+    if (e & 1) ef4_mul(F, r, b, r);
+    ef4_mul(F, b, b, b);
+    e >>= 1;
+  }
+  memcpy(out, r, 16);
+}
+
+/* expand_eq_to_hypercube(z, 1) (zorch/poly/eq.py:92-130, expand_hypercube_step
+ * :55-62): eq(w, z) for w in {0,1}^m, z[0] on the most significant index bit;
+ * each step splits an entry s into (s - s z_j, s z_j) at (2i, 2i+1). */
+void orc_eq_expand(int field, const uint32_t* z, int m, uint32_t* out) {
+  const fld* F = FLD(field);
+  out[0] = F->one;
+  out[1] = out[2] = out[3] = 0;
+  for (int j = 0; j < m; j++) {
+    for (int64_t i = ((int64_t)1 << j) - 1; i >= 0; i--) {
+      uint32_t s[4], hi[4], lo[4];
+      memcpy(s, out + 4 * i, 16);
+      ef4_mul(F, s, z + 4 * j, hi);
+      ef4_sub(F, s, hi, lo);
+      memcpy(out + 4 * (2 * i), lo, 16);
+      memcpy(out + 4 * (2 * i + 1), hi, 16);
+    }
+  }
+}
+
+/* eval_mle (zorch/poly/multilinear.py:92-98) of w base columns [w][2^m] at
+ * the EF4 point z: out[c] = sum_i eq(i, z) cols[c][i]. */
+void orc_eval_mle_base(int field, const uint32_t* cols, int w, int m, const uint32_t* z,
+                       uint32_t* out) {
+  const fld* F = FLD(field);
+  const int64_t S = (int64_t)1 << m;
+  uint32_t* eq = (uint32_t*)malloc(sizeof(uint32_t) * 4 * (size_t)S);
+  orc_eq_expand(field, z, m, eq);
+#pragma omp parallel for num_threads(orc_get_threads()) schedule(static)
+  for (int c = 0; c < w; c++) {
+    uint32_t acc[4] = {0, 0, 0, 0};
+    for (int64_t i = 0; i < S; i++)
+      for (int e = 0; e < 4; e++)
+        acc[e] = fadd(F, acc[e], fmul(F, eq[4 * i + e], cols[(int64_t)c * S + i]));
+    memcpy(out + 4 * c, acc, 16);
+  }
+  free(eq);
+}
+
+/* eval_mle of one EF4 MLE [2^m] at the EF4 point z (m = 0: mle[0]). */
+void orc_eval_mle_ef4(int field, const uint32_t* mle, int m, const uint32_t* z, uint32_t* out) {
+  const fld* F = FLD(field);
+  const int64_t M = (int64_t)1 << m;
+  uint32_t* eq = (uint32_t*)malloc(sizeof(uint32_t) * 4 * (size_t)M);
+  orc_eq_expand(field, z, m, eq);
+  uint32_t acc[4] = {0, 0, 0, 0};
+  for (int64_t i = 0; i < M; i++) {
+    uint32_t t[4];
+    ef4_mul(F, eq + 4 * i, mle + 4 * i, t);
+    ef4_add(F, acc, t, acc);
+  }
+  memcpy(out, acc, 16);
+  free(eq);
+}
+
+/* mle_fold (zorch/poly/multilinear.py:101-109): out[i] = mle[2i] + beta mle[2i+1],
+ * EF4 entries, beta EF4 (a base beta as [b, 0, 0, 0]). */
+void orc_mle_fold(int field, const uint32_t* mle, int64_t M, const uint32_t* beta,
+                  uint32_t* out) {
+  const fld* F = FLD(field);
+  for (int64_t i = 0; i < M / 2; i++) {
+    uint32_t t[4];
+    ef4_mul(F, beta, mle + 4 * (2 * i + 1), t);
+    ef4_add(F, mle + 4 * (2 * i), t, out + 4 * i);
+  }
+}
+
+/* batch_staggered (zorch/pcs/basefold/batching.py:66-80) of one matrix's w
+ * base columns [w][n] with partial_lagrange weights over nbv EF4 challenges,
+ * the matrix taking weights offset .. offset+w-1; accumulate adds onto out. */
+void orc_rlc_columns_ex(int field, const uint32_t* cw, int64_t n, int w, const uint32_t* chal,
+                        int nbv, int offset, int accumulate, uint32_t* out) {
+  const fld* F = FLD(field);
+  uint32_t* wt = (uint32_t*)malloc(sizeof(uint32_t) * 4 * ((size_t)1 << nbv));
+  orc_eq_expand(field, chal, nbv, wt);
+#pragma omp parallel for num_threads(orc_get_threads()) schedule(static)
+  for (int64_t j = 0; j < n; j++) {
+    uint32_t r[4] = {0, 0, 0, 0};
+    if (accumulate) memcpy(r, out + 4 * j, 16);
+    for (int c = 0; c < w; c++)
+      for (int e = 0; e < 4; e++)
+        r[e] = fadd(F, r[e], fmul(F, wt[4 * (offset + c) + e], cw[(int64_t)c * n + j]));
+    memcpy(out + 4 * j, r, 16);
+  }
+  free(wt);
+}
+
 /* ----------------------------------------------------------- transcript ---- */
 /* DuplexTranscript (zorch/transcript.py:239-481), width 16, rate 8. */
 void orc_duplex_init(orc_duplex* t) { memset(t, 0, sizeof(*t)); }

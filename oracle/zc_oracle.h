@@ -114,6 +114,16 @@ int orc_fri_fold_bitrev(int field, const uint32_t* cw, int64_t n, int ef_in,
 void orc_smcs_bind_root(const orc_p2* p, const uint32_t* raw_root, uint32_t log_height,
                         uint32_t width, uint32_t* out8);
 
+/* Basefold sumcheck pieces (EF4 values are 4 Montgomery limbs c0..c3). */
+void orc_ef4_inv(int field, const uint32_t* a, uint32_t* out);
+void orc_eq_expand(int field, const uint32_t* z, int m, uint32_t* out);
+void orc_eval_mle_base(int field, const uint32_t* cols, int w, int m, const uint32_t* z,
+                       uint32_t* out);
+void orc_eval_mle_ef4(int field, const uint32_t* mle, int m, const uint32_t* z, uint32_t* out);
+void orc_mle_fold(int field, const uint32_t* mle, int64_t M, const uint32_t* beta, uint32_t* out);
+void orc_rlc_columns_ex(int field, const uint32_t* cw, int64_t n, int w, const uint32_t* chal,
+                        int nbv, int offset, int accumulate, uint32_t* out);
+
 /* Duplex transcript (overwrite mode, rate 8, width 16) */
 void orc_duplex_init(orc_duplex* t);
 void orc_duplex_observe(const orc_p2* p, orc_duplex* t, const uint32_t* v, int64_t m);

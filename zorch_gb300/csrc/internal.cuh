@@ -19,10 +19,10 @@ struct KIn;
 template <>
 struct KIn<Bb16Builtin> {
   __device__ static Bb16Builtin make(const P2Params*, P2Params*) { return {}; }
-  // The quad permutation reads P2Params from shared memory: stage them.
-  __device__ static RtParams<BabyBear> quad(const P2Params* g, P2Params* s) {
+  // The half-warp permutation reads P2Params from shared memory: stage them.
+  __device__ static const P2Params* half(const P2Params* g, P2Params* s) {
     stage_params(s, g);
-    return RtParams<BabyBear>{s};
+    return s;
   }
 };
 template <class F>
@@ -32,7 +32,7 @@ struct KIn<RtParams<F>> {
     return RtParams<F>{s};
   }
   // Already staged by make (same shared copy).
-  __device__ static RtParams<F> quad(const P2Params*, P2Params* s) { return RtParams<F>{s}; }
+  __device__ static const P2Params* half(const P2Params*, P2Params* s) { return s; }
 };
 
 // Calls fn(K{}, device_params) with the provider matching the handle.

@@ -195,61 +195,104 @@ ZC_HD void p2_compress(const uint32_t* l, const uint32_t* r, uint32_t* out,
   for (int i = 0; i < 8; i++) out[i] = s[i];
 }
 
-// ------------------------------------------------------------- quads ----
-// The same permutation spread over a quad of lanes (lanes 4g .. 4g+3 of a
-// warp): lane q of the quad holds state words 4q .. 4q+3, i.e. one M4 block.
-// The M4 products are lane-local; the external layer's lane-class sums and the
-// internal layer's full sum are butterflies over lane ^ 1 and lane ^ 2, which
-// stay inside the quad. One thread's permutation is a dependency chain of
-// ~7000 instructions; the quad's is about a quarter of that, so the latency-
-// bound parts of a commit (the narrow top levels of a tree, the transcript)
-// use quads. Constants come from a P2Params in shared memory, so the built-in
-// instance uses its generic (Montgomery-diagonal) form here. Every lane of the
-// warp must make the call (full-warp shuffles), active quad or not.
-template <class F>
-__device__ __forceinline__ uint32_t quad_sum(uint32_t v) {
-  v = madd<F>(v, __shfl_xor_sync(0xffffffffu, v, 1));
-  return madd<F>(v, __shfl_xor_sync(0xffffffffu, v, 2));
+// ------------------------------------------------------------- halves ---
+// The same permutation on a half-warp (lanes 16h .. 16h+15): lane l of the
+// half holds state word l. One thread's permutation is a dependency chain of
+// ~7000 instructions (~9.4 us at 2.07 GHz, measured); on a half-warp each lane
+// runs one S-box per round and the linear layers are butterflies of shuffles,
+// which brings a permutation to ~3 us. The latency-bound parts of a commit --
+// the narrow top levels of a tree and the transcript -- use halves.
+//  - external layer: y_j = s_b + x_j + 2 x_{j+1} is M4 = circ(2,3,1,1) on the
+//    4-word block b (s_b = block sum, j + 1 mod 4), then y += the sum of y over
+//    the lane class (xor 4, xor 8);
+//  - partial round: the sum of lanes 1..15 is reduced while lane 0 runs its
+//    S-box, and lane 0's new word is broadcast and added afterwards.
+// Constants come from a P2Params in shared memory. Every lane of the warp must
+// make the call (full-warp shuffles), active half or not.
+constexpr unsigned kFullMask = 0xffffffffu;
+
+template <class F, int ALPHA>
+__device__ __forceinline__ uint32_t half_sbox(uint32_t x, uint32_t alpha) {
+  if (ALPHA == 3) return mmul<F>(mmul<F>(x, x), x);
+  if (ALPHA == 5) {
+    const uint32_t x2 = mmul<F>(x, x);
+    return mmul<F>(mmul<F>(x2, x2), x);
+  }
+  if (ALPHA == 7) {
+    const uint32_t x2 = mmul<F>(x, x);
+    return mmul<F>(mmul<F>(x2, x), mmul<F>(x2, x2));
+  }
+  return mpow<F>(x, alpha);
 }
 
 template <class F>
-__device__ __forceinline__ void quad_ext_linear(uint32_t* x) {
-  const uint32_t t01 = madd<F>(x[0], x[1]), t23 = madd<F>(x[2], x[3]);
-  const uint32_t t0123 = madd<F>(t01, t23);
-  const uint32_t t01123 = madd<F>(t0123, x[1]), t01233 = madd<F>(t0123, x[3]);
-  const uint32_t y3 = madd<F>(t01233, madd<F>(x[0], x[0]));
-  const uint32_t y1 = madd<F>(t01123, madd<F>(x[2], x[2]));
-  const uint32_t y0 = madd<F>(t01123, t01);
-  const uint32_t y2 = madd<F>(t01233, t23);
-  x[0] = madd<F>(y0, quad_sum<F>(y0));
-  x[1] = madd<F>(y1, quad_sum<F>(y1));
-  x[2] = madd<F>(y2, quad_sum<F>(y2));
-  x[3] = madd<F>(y3, quad_sum<F>(y3));
+__device__ __forceinline__ uint32_t half_sum16(uint32_t v) {
+  v = madd<F>(v, __shfl_xor_sync(kFullMask, v, 1));
+  v = madd<F>(v, __shfl_xor_sync(kFullMask, v, 2));
+  v = madd<F>(v, __shfl_xor_sync(kFullMask, v, 4));
+  return madd<F>(v, __shfl_xor_sync(kFullMask, v, 8));
 }
 
 template <class F>
-__device__ __forceinline__ void p2_permute_quad(uint32_t* x, int q, const RtParams<F>& k) {
-  quad_ext_linear<F>(x);
+__device__ __forceinline__ uint32_t half_ext_linear(uint32_t x) {
+  const int lane = threadIdx.x & 31;
+  const uint32_t nxt = __shfl_sync(kFullMask, x, (lane & ~3) | ((lane + 1) & 3));
+  uint32_t s = madd<F>(x, __shfl_xor_sync(kFullMask, x, 1));
+  s = madd<F>(s, __shfl_xor_sync(kFullMask, s, 2));
+  const uint32_t y = madd<F>(madd<F>(s, x), madd<F>(nxt, nxt));
+  uint32_t c = madd<F>(y, __shfl_xor_sync(kFullMask, y, 4));
+  c = madd<F>(c, __shfl_xor_sync(kFullMask, c, 8));
+  return madd<F>(y, c);
+}
+
+// The rounds are rolled loops (constants read from shared memory one round
+// ahead): a permutation runs only a few times per launch here, so its code
+// is fetched cold, and a short loop body costs far fewer instruction-cache
+// misses than unrolled rounds.
+template <class F, int ALPHA>
+__device__ __forceinline__ uint32_t half_permute_a(uint32_t x, const P2Params* p) {
+  const int l = threadIdx.x & 15;
+  const int rfh = (int)p->rounds_f_half, rp = (int)p->rounds_p;
+  const uint32_t alpha = p->alpha, dg = p->diag[l], js = p->j_scale;
+  const bool jone = p->j_is_one != 0;
+  x = half_ext_linear<F>(x);
+  uint32_t c = rfh > 0 ? p->ext_init[0][l] : p->int_rc[0];
 #pragma unroll 1
-  for (int r = 0; r < k.rf_half(); r++) {
-#pragma unroll
-    for (int j = 0; j < 4; j++) x[j] = k.sbox(madd<F>(x[j], k.ei(r, 4 * q + j)));
-    quad_ext_linear<F>(x);
+  for (int r = 0; r < rfh; r++) {
+    const uint32_t c_next = r + 1 < rfh ? p->ext_init[r + 1][l] : p->int_rc[0];
+    x = half_ext_linear<F>(half_sbox<F, ALPHA>(madd<F>(x, c), alpha));
+    c = c_next;
   }
 #pragma unroll 1
-  for (int r = 0; r < k.rp(); r++) {
-    const uint32_t s0 = k.sbox(madd<F>(x[0], k.ir(r)));
-    x[0] = q == 0 ? s0 : x[0];
-    const uint32_t sum =
-        k.jsum(quad_sum<F>(madd<F>(madd<F>(x[0], x[1]), madd<F>(x[2], x[3]))));
-#pragma unroll
-    for (int j = 0; j < 4; j++) x[j] = madd<F>(sum, mmul<F>(k.dg(4 * q + j), x[j]));
+  for (int r = 0; r < rp; r++) {
+    const uint32_t c_next = r + 1 < rp ? p->int_rc[r + 1] : p->ext_term[0][l];
+    const uint32_t s0 = half_sbox<F, ALPHA>(madd<F>(x, c), alpha);  // lane 0's is used
+    const uint32_t rest = half_sum16<F>(l == 0 ? 0u : x);           // lanes 1..15
+    const uint32_t dx = mmul<F>(dg, l == 0 ? s0 : x);
+    uint32_t sum = madd<F>(rest, __shfl_sync(kFullMask, s0, threadIdx.x & 16));
+    if (!jone) sum = mmul<F>(sum, js);
+    x = madd<F>(sum, dx);
+    c = c_next;
   }
+  if (rp == 0) c = p->ext_term[0][l];
 #pragma unroll 1
-  for (int r = 0; r < k.rf_half(); r++) {
-#pragma unroll
-    for (int j = 0; j < 4; j++) x[j] = k.sbox(madd<F>(x[j], k.et(r, 4 * q + j)));
-    quad_ext_linear<F>(x);
+  for (int r = 0; r < rfh; r++) {
+    const uint32_t c_next = p->ext_term[r + 1 < rfh ? r + 1 : r][l];
+    x = half_ext_linear<F>(half_sbox<F, ALPHA>(madd<F>(x, c), alpha));
+    c = c_next;
+  }
+  return x;
+}
+
+// Lane l (of the caller's half-warp) passes state word l and gets word l of
+// the permuted state back. `p` points to shared memory.
+template <class F>
+__device__ __forceinline__ uint32_t p2_permute_half(uint32_t x, const P2Params* p) {
+  switch (p->alpha) {
+    case 3: return half_permute_a<F, 3>(x, p);
+    case 5: return half_permute_a<F, 5>(x, p);
+    case 7: return half_permute_a<F, 7>(x, p);
+    default: return half_permute_a<F, 0>(x, p);
   }
 }
 

@@ -62,7 +62,7 @@ struct Duplex {
 // values is absorbed a full rate block at a time (overwrite sponge[0:8],
 // permute); the tail stays pending; a fresh output iff no tail remains.
 // `perm(s)` permutes the 16-word sponge in place: one thread on the host, a
-// quad of lanes on the device (QuadPerm).
+// half-warp on the device (HalfPerm).
 #pragma nv_exec_check_disable
 template <class Perm>
 ZC_HD void duplex_observe(Duplex& t, const uint32_t* v, int64_t m, const Perm& perm) {
@@ -117,21 +117,19 @@ struct HostPerm {
 };
 
 // Every lane of the (single) warp holds the same Duplex state and runs the same
-// control flow; a permutation runs on each quad (all quads compute the same
+// control flow; a permutation runs on each half-warp (both compute the same
 // result) and is gathered back into every lane's copy.
 template <class F>
-struct QuadPerm {
-  RtParams<F> k;
+struct HalfPerm {
+  const P2Params* p;  // shared memory
   __device__ void operator()(uint32_t* s) const {
-    const int lane = threadIdx.x & 31, q = lane & 3;
-    uint32_t x[4];
+    const int lane = threadIdx.x & 31;
+    uint32_t x = 0;
 #pragma unroll
-    for (int j = 0; j < 4; j++) x[j] = s[4 * q + j];
-    p2_permute_quad(x, q, k);
+    for (int j = 0; j < 16; j++) x = (lane & 15) == j ? s[j] : x;
+    x = p2_permute_half<F>(x, p);
 #pragma unroll
-    for (int qq = 0; qq < 4; qq++)
-#pragma unroll
-      for (int j = 0; j < 4; j++) s[4 * qq + j] = __shfl_sync(0xffffffffu, x[j], (lane & ~3) | qq);
+    for (int j = 0; j < 16; j++) s[j] = __shfl_sync(kFullMask, x, (lane & 16) | j);
   }
 };
 
@@ -143,7 +141,7 @@ __global__ void __launch_bounds__(32) k_duplex_step(const P2Params* rt, uint32_t
                                                     int64_t block_len) {
   __shared__ P2Params s_rt;
   KIn<K>::make(rt, &s_rt);
-  const QuadPerm<typename K::F> perm{KIn<K>::quad(rt, &s_rt)};
+  const HalfPerm<typename K::F> perm{KIn<K>::half(rt, &s_rt)};
   Duplex t;
   memcpy(&t, state, sizeof(Duplex));
   duplex_observe(t, values, m, perm);
@@ -167,7 +165,7 @@ __global__ void __launch_bounds__(32) k_duplex_hop(
     uint32_t* out_pos_o, uint32_t* chal) {
   __shared__ P2Params s_rt;
   KIn<K>::make(rt, &s_rt);
-  const QuadPerm<typename K::F> perm{KIn<K>::quad(rt, &s_rt)};
+  const HalfPerm<typename K::F> perm{KIn<K>::half(rt, &s_rt)};
   Duplex t;
   for (int j = 0; j < 8; j++) {
     t.in_buf[j] = in_buf[j];

@@ -162,47 +162,68 @@ struct FoldLeaf {
   }
 };
 
-// Threads per CTA for a subtree of T first-level nodes: T/2 quads, so every
-// level above the first is one round of quad permutations; at least a warp.
-inline int subtree_threads(int T) { return 2 * T > 32 ? 2 * T : 32; }
+// Nodes per subtree CTA at its first level, and its threads: 8 per node, so
+// each level above the first is one round of half-warp permutations (T/2
+// halves); at least a warp.
+constexpr int kSubT = 128;
+inline int subtree_threads(int T) { return 8 * T > 32 ? 8 * T : 32; }
 
-// Lanes q = 0, 1 of a quad hold output words 4q .. 4q+3 (16-byte aligned).
-__device__ __forceinline__ void quad_store(uint32_t* dst8, int q, const uint32_t* x) {
-  reinterpret_cast<uint4*>(dst8)[q] = make_uint4(x[0], x[1], x[2], x[3]);
+// Half-warp permutation of the caller's field (lane l passes state word l).
+template <class F>
+__device__ __forceinline__ uint32_t half_perm(uint32_t x, const P2Params* hp) {
+  return p2_permute_half<F>(x, hp);
+}
+
+// One level of a subtree: parent i (< width) = compress(children 2i, 2i+1)
+// read from the [word][node] slots `src` (row stride `stride`), written to the
+// `dst` slots and to the tree's level at `lay`. Half-warp h takes nodes
+// h, h + H, ... (H halves); a warp with no node in a round skips it (a
+// warp-uniform branch: the shuffles need every lane of a running warp).
+template <class F>
+__device__ __forceinline__ void subtree_level(const uint32_t* src, uint32_t* dst, int stride,
+                                              uint32_t* lay, int width, const P2Params* hp) {
+  const int t = threadIdx.x, l = t & 15, H = blockDim.x >> 4;
+  const int child_off = l >> 3, word = l & 7;
+  for (int r = 0; r < width; r += H) {
+    if (r + 2 * (t >> 5) >= width) continue;
+    const int node = r + (t >> 4);
+    const bool on = node < width;
+    uint32_t x = on ? src[word * stride + 2 * node + child_off] : 0u;
+    x = half_perm<F>(x, hp);
+    if (on && l < 8) {
+      lay[8 * node + l] = x;
+      dst[l * stride + node] = x;
+    }
+  }
 }
 
 // One subtree of T first-level nodes per CTA (blockDim = subtree_threads(T)):
-// the first level is T leaf digests (one thread each; for NodeLeaf, quads
+// the first level is T leaf digests (one thread each; for NodeLeaf, half-warps
 // compressing stored children), then every level up to the subtree root is
-// compressed by quads out of ping-pong shared-memory slots, each level written
-// to `layers`.
+// compressed by half-warps out of ping-pong shared-memory slots, each level
+// written to `layers`.
 template <class K, class Leaf>
-__global__ void __launch_bounds__(2 * kMaxT) k_subtree(Leaf leaf, uint32_t* layers, int64_t L,
+__global__ void __launch_bounds__(8 * kSubT) k_subtree(Leaf leaf, uint32_t* layers, int64_t L,
                                                        int l0, int T, const P2Params* rt) {
+  using F = typename K::F;
   __shared__ P2Params s_rt;
-  __shared__ uint32_t sm[2][8 * kMaxT];  // [word][node] digest slots
+  __shared__ uint32_t sm[2][8 * kSubT];  // [word][node] digest slots
   K k = KIn<K>::make(rt, &s_rt);
-  const RtParams<typename K::F> kq = KIn<K>::quad(rt, &s_rt);
-  const int t = threadIdx.x, q = t & 3, qi = t >> 2, Q = blockDim.x >> 2;
+  const P2Params* hp = KIn<K>::half(rt, &s_rt);
+  const int t = threadIdx.x;
   const int64_t base = (int64_t)blockIdx.x * T;
   uint32_t* lay0 = layers + 8 * (level_offset(L, l0) + base);
-  // A warp whose 8 quads are all past the level's width skips the round (a
-  // warp-uniform branch: the quad shuffles need every lane of a running warp).
-  const int warp_q0 = (t >> 5) * 8;
   if constexpr (std::is_same<Leaf, NodeLeaf>::value) {
-    for (int r = 0; r < T; r += Q) {
-      const int node = r + qi;
-      if (r + warp_q0 >= T) continue;
-      uint32_t x[4] = {0, 0, 0, 0};
-      if (node < T) {
-        const uint4 v = reinterpret_cast<const uint4*>(leaf.in + 16 * (base + node))[q];
-        x[0] = v.x, x[1] = v.y, x[2] = v.z, x[3] = v.w;
-      }
-      p2_permute_quad(x, q, kq);
-      if (node < T && q < 2) {
-        quad_store(lay0 + 8 * node, q, x);
-#pragma unroll
-        for (int j = 0; j < 4; j++) sm[0][(4 * q + j) * kMaxT + node] = x[j];
+    const int l = t & 15, H = blockDim.x >> 4;
+    for (int r = 0; r < T; r += H) {
+      if (r + 2 * (t >> 5) >= T) continue;
+      const int node = r + (t >> 4);
+      const bool on = node < T;
+      uint32_t x = on ? leaf.in[16 * (base + node) + l] : 0u;
+      x = half_perm<F>(x, hp);
+      if (on && l < 8) {
+        lay0[8 * node + l] = x;
+        sm[0][l * kSubT + node] = x;
       }
     }
   } else {
@@ -211,7 +232,7 @@ __global__ void __launch_bounds__(2 * kMaxT) k_subtree(Leaf leaf, uint32_t* laye
       leaf.digest(base + t, d, k);
       store_digest(lay0 + 8 * t, d);
 #pragma unroll
-      for (int i = 0; i < 8; i++) sm[0][i * kMaxT + t] = d[i];
+      for (int i = 0; i < 8; i++) sm[0][i * kSubT + t] = d[i];
     }
   }
   int cur = 0, lvl = l0, width = T;
@@ -219,24 +240,8 @@ __global__ void __launch_bounds__(2 * kMaxT) k_subtree(Leaf leaf, uint32_t* laye
     __syncthreads();
     width >>= 1;
     lvl++;
-    uint32_t* lay = layers + 8 * (level_offset(L, lvl) + (int64_t)blockIdx.x * width);
-    for (int r = 0; r < width; r += Q) {
-      const int node = r + qi;
-      if (r + warp_q0 >= width) continue;
-      // quad state = child(2 node) || child(2 node + 1); lane q: words 4q .. 4q+3
-      const int child = 2 * node + (q >> 1), w0 = 4 * (q & 1);
-      uint32_t x[4] = {0, 0, 0, 0};
-      if (node < width) {
-#pragma unroll
-        for (int j = 0; j < 4; j++) x[j] = sm[cur][(w0 + j) * kMaxT + child];
-      }
-      p2_permute_quad(x, q, kq);
-      if (node < width && q < 2) {
-        quad_store(lay + 8 * node, q, x);
-#pragma unroll
-        for (int j = 0; j < 4; j++) sm[cur ^ 1][(4 * q + j) * kMaxT + node] = x[j];
-      }
-    }
+    subtree_level<F>(sm[cur], sm[cur ^ 1], kSubT,
+                     layers + 8 * (level_offset(L, lvl) + (int64_t)blockIdx.x * width), width, hp);
     cur ^= 1;
   }
 }
@@ -256,9 +261,10 @@ __global__ void __launch_bounds__(kMaxT) k_leaf(Leaf leaf, uint32_t* out, int64_
 }
 
 // Levels with more than this many nodes run one thread per node (k_leaf with
-// NodeLeaf, fully occupied); the small top of the tree runs as fused CTA
-// subtrees (k_subtree with NodeLeaf), log2(T)+1 levels per launch.
-constexpr int64_t kLevelWiseMin = 1 << 15;
+// NodeLeaf, fully occupied, throughput-bound); the narrow top of the tree is
+// latency-bound and runs as fused CTA subtrees of half-warp permutations
+// (k_subtree with NodeLeaf), log2(T)+1 levels per launch.
+constexpr int64_t kLevelWiseMin = 1 << 13;
 
 // Launches the levels above `l_done` (all levels <= l_done already stored).
 template <class K>
@@ -276,7 +282,7 @@ zc_status finish_tree(uint32_t* layers, int64_t L, int l_done, const P2Params* r
       l += 1;
       continue;
     }
-    const int T = parents < kMaxT ? (int)parents : kMaxT;
+    const int T = parents < kSubT ? (int)parents : kSubT;
     k_subtree<K, NodeLeaf><<<(unsigned)(parents / T), subtree_threads(T), 0, st>>>(
         nl, layers, L, l + 1, T, rt);
     ZC_TRY(launch_check());
@@ -293,7 +299,7 @@ zc_status commit_tree(const Leaf& leaf, uint32_t* layers, int64_t L, const P2Par
     ZC_TRY(launch_check());
     return finish_tree<K>(layers, L, 0, rt, st);
   }
-  const int T0 = L < kMaxT ? (int)L : kMaxT;
+  const int T0 = L < kSubT ? (int)L : kSubT;
   k_subtree<K, Leaf><<<(unsigned)(L / T0), subtree_threads(T0), 0, st>>>(leaf, layers, L, 0, T0,
                                                                          rt);
   ZC_TRY(launch_check());
@@ -384,7 +390,8 @@ zc_status fold_commit_launch(const uint32_t* cw, int64_t n, const uint32_t* beta
   return commit_tree<K>(leaf, layers, n >> 2, rt, st);
 }
 
-// compress([raw_root, sponge([log_height, width])]) on one warp's quads.
+// compress([raw_root, sponge([log_height, width])]) on one warp (both halves
+// compute the same permutations).
 template <class K>
 __global__ void __launch_bounds__(32) k_bind_root(const P2Params* rt, const uint32_t* raw_root,
                                                   uint32_t log_height, uint32_t width,
@@ -392,29 +399,17 @@ __global__ void __launch_bounds__(32) k_bind_root(const P2Params* rt, const uint
   using F = typename K::F;
   __shared__ P2Params s_rt;
   KIn<K>::make(rt, &s_rt);
-  const RtParams<F> kq = KIn<K>::quad(rt, &s_rt);
-  const int lane = threadIdx.x & 31, q = lane & 3;
+  const P2Params* hp = KIn<K>::half(rt, &s_rt);
+  const int lane = threadIdx.x & 31, l = lane & 15;
   // sponge: state = [log_height, width, 0 ...] (one absorb block), permute
-  uint32_t x[4] = {0, 0, 0, 0};
-  if (q == 0) {
-    x[0] = to_mont<F>(log_height);
-    x[1] = to_mont<F>(width);
-  }
-  p2_permute_quad(x, q, kq);
-  // compress: state = raw_root || params (params = words 0..7, lanes q = 0, 1)
-  uint32_t y[4];
-  const uint32_t from2 = __shfl_sync(0xffffffffu, x[0], (lane & ~3) | (q & 1)),
-                 from2b = __shfl_sync(0xffffffffu, x[1], (lane & ~3) | (q & 1)),
-                 from2c = __shfl_sync(0xffffffffu, x[2], (lane & ~3) | (q & 1)),
-                 from2d = __shfl_sync(0xffffffffu, x[3], (lane & ~3) | (q & 1));
-  if (q < 2) {
-#pragma unroll
-    for (int j = 0; j < 4; j++) y[j] = raw_root[4 * q + j];
-  } else {
-    y[0] = from2, y[1] = from2b, y[2] = from2c, y[3] = from2d;
-  }
-  p2_permute_quad(y, q, kq);
-  if (lane < 2) quad_store(out, q, y);
+  uint32_t x = l == 0 ? to_mont<F>(log_height) : (l == 1 ? to_mont<F>(width) : 0u);
+  x = half_perm<F>(x, hp);
+  // compress: state = raw_root || params (params = words 0..7 of the sponge)
+  const uint32_t par = __shfl_sync(kFullMask, x, (lane & 16) | (l & 7));
+  uint32_t y = l < 8 ? raw_root[l] : par;
+  y = half_perm<F>(y, hp);
+  __syncwarp();  // raw_root may alias out: every lane has read it
+  if (lane < 8) out[lane] = y;
 }
 
 // ------------------------------------------------------------ batched ----
@@ -491,44 +486,28 @@ __global__ void __launch_bounds__(kMaxT) k_tree_batch(const __grid_constant__ Tr
 }
 
 // One CTA per tree: level `top` (<= 256 nodes, already stored) to the root,
-// each level one round of quad permutations (2 * kMaxT threads = 128 quads).
+// each level compressed by half-warps (64 halves: the first level of up to 128
+// parents takes up to two rounds, every later level one).
 template <class K>
-__global__ void __launch_bounds__(2 * kMaxT) k_tree_top(const __grid_constant__ TreeBatch B,
-                                                        const P2Params* rt) {
+__global__ void __launch_bounds__(8 * kSubT) k_tree_top(const __grid_constant__ TreeBatch B,
+                                                       const P2Params* rt) {
+  using F = typename K::F;
+  constexpr int S = 2 * kSubT;  // slot stride: up to 256 nodes
   __shared__ P2Params s_rt;
-  __shared__ uint32_t sm[2][8 * kMaxT];
+  __shared__ uint32_t sm[2][8 * S];
   KIn<K>::make(rt, &s_rt);
-  const RtParams<typename K::F> kq = KIn<K>::quad(rt, &s_rt);
+  const P2Params* hp = KIn<K>::half(rt, &s_rt);
   const TreeJobDev& J = B.job[blockIdx.x];
   int lvl = J.top;
   int width = (int)(J.L >> lvl);
   const uint32_t* src = J.layers + 8 * level_offset(J.L, lvl);
-  for (int i = threadIdx.x; i < width * 8; i += blockDim.x)
-    sm[0][(i & 7) * kMaxT + (i >> 3)] = src[i];
-  const int q = threadIdx.x & 3, qi = threadIdx.x >> 2, Q = blockDim.x >> 2;
-  const int warp_q0 = (threadIdx.x >> 5) * 8;
+  for (int i = threadIdx.x; i < width * 8; i += blockDim.x) sm[0][(i & 7) * S + (i >> 3)] = src[i];
   int cur = 0;
   while (width > 1) {
     __syncthreads();
     width >>= 1;
     lvl++;
-    uint32_t* lay = J.layers + 8 * level_offset(J.L, lvl);
-    for (int r = 0; r < width; r += Q) {
-      const int node = r + qi;
-      if (r + warp_q0 >= width) continue;  // whole warp idle this round
-      const int child = 2 * node + (q >> 1), w0 = 4 * (q & 1);
-      uint32_t x[4] = {0, 0, 0, 0};
-      if (node < width) {
-#pragma unroll
-        for (int j = 0; j < 4; j++) x[j] = sm[cur][(w0 + j) * kMaxT + child];
-      }
-      p2_permute_quad(x, q, kq);
-      if (node < width && q < 2) {
-        quad_store(lay + 8 * node, q, x);
-#pragma unroll
-        for (int j = 0; j < 4; j++) sm[cur ^ 1][(4 * q + j) * kMaxT + node] = x[j];
-      }
-    }
+    subtree_level<F>(sm[cur], sm[cur ^ 1], S, J.layers + 8 * level_offset(J.L, lvl), width, hp);
     cur ^= 1;
   }
 }
@@ -577,7 +556,7 @@ zc_status tree_batch_wave(const zc_merkle_job* jobs, int n, unsigned long long* 
       k_tree_batch<K, 1><<<(unsigned)grid, kMaxT, 0, st>>>(B, ctr + l, rt);
     ZC_TRY(launch_check());
   }
-  k_tree_top<K><<<n, 2 * kMaxT, 0, st>>>(B, rt);
+  k_tree_top<K><<<n, 8 * kSubT, 0, st>>>(B, rt);
   return launch_check();
 }
 
