@@ -239,6 +239,50 @@ zc_status zc_fri_fold_commit_bitrev(const zc_poseidon2* p, const uint32_t* cw, i
 zc_status zc_smcs_bind_root(const zc_poseidon2* p, const uint32_t* raw_root, uint32_t log_height,
                             uint32_t width, uint32_t* out, void* stream);
 
+/* ---- Basefold open: the multilinear side ------------------------------ */
+/* EF4 values are 4 Montgomery words (c0..c3), 16-byte aligned on the device.
+ * Replaces expand_eq_to_hypercube(z, 1) (zorch/poly/eq.py:92-130): out[i] =
+ * eq(i, z) for i < 2^m, z[0] on the most significant index bit; m <= 24.
+ * workspace: zc_eq_expand_workspace_bytes(m) bytes (0 for m <= 12). */
+size_t zc_eq_expand_workspace_bytes(int32_t m);
+zc_status zc_eq_expand(zc_field field, const uint32_t* z, int32_t m, uint32_t* out, void* workspace,
+                       size_t workspace_bytes, void* stream);
+/* Replaces eval_mle(mle, z, axis=0) (zorch/poly/multilinear.py:92-98) on w
+ * base-field columns cols[w][2^m]: out[c] = sum_i eq(i, z) cols[c][i] (EF4). */
+size_t zc_eval_mle_workspace_bytes(int32_t w, int32_t m);
+zc_status zc_eval_mle(zc_field field, const uint32_t* cols, int32_t w, int32_t m,
+                      const uint32_t* z, uint32_t* out, void* workspace, size_t workspace_bytes,
+                      void* stream);
+/* batch_staggered (zorch/pcs/basefold/batching.py:66-80) of one matrix's w base
+ * columns cw[w][n] into the EF4 out[n]: weights eq(., r) over nbv <= 12 EF4
+ * challenges (challenge 0 the most significant index bit), this matrix taking
+ * weights offset .. offset+w-1; accumulate != 0 adds onto out. */
+zc_status zc_rlc_columns_ex(zc_field field, const uint32_t* cw, int64_t n, int32_t w,
+                            const uint32_t* challenges, int32_t nbv, int32_t offset,
+                            int32_t accumulate, uint32_t* out, void* stream);
+/* The same weights applied to w EF4 values (the batched claim): out (one EF4)
+ * = [out +] sum_c weight[offset + c] values[c]. */
+zc_status zc_rlc_values(zc_field field, const uint32_t* values, int32_t w,
+                        const uint32_t* challenges, int32_t nbv, int32_t offset,
+                        int32_t accumulate, uint32_t* out, void* stream);
+/* One interleaved-sumcheck message (SumcheckKernel.message,
+ * zorch/pcs/basefold/kernel.py:52-66): the running MLE mle[2M] (EF4), the eq
+ * table eq[M] of the unbound point prefix, the running claim and 1/z_last:
+ * msg = (s0, s1), s0 = sum_j eq[j] mle[2j], s1 = (claim - s0) / z_last + s0.
+ * workspace: zc_sumcheck_workspace_bytes() bytes. */
+size_t zc_sumcheck_workspace_bytes(void);
+zc_status zc_sumcheck_message(zc_field field, const uint32_t* mle, int64_t M, const uint32_t* eq,
+                              const uint32_t* claim, const uint32_t* zinv, uint32_t* msg,
+                              void* workspace, size_t workspace_bytes, void* stream);
+/* The round's fold (SumcheckKernel.fold, :68-74; mle_fold,
+ * zorch/poly/multilinear.py:101-109; contract_hypercube_step,
+ * zorch/poly/eq.py:65-77): mle_out[j] = mle[2j] + beta mle[2j+1] (j < M),
+ * eq_out[k] = eq[2k] + eq[2k+1] (k < M/2; skipped when eq_out is NULL),
+ * claim = s0 + beta s1; beta has beta_limbs (1 or 4) device words. */
+zc_status zc_sumcheck_fold(zc_field field, const uint32_t* mle, int64_t M, const uint32_t* beta,
+                           int32_t beta_limbs, const uint32_t* msg, uint32_t* mle_out,
+                           const uint32_t* eq, uint32_t* eq_out, uint32_t* claim, void* stream);
+
 /* Staggered partial-Lagrange batching of a committed matrix's w base columns
  * (n words each) into one EF4 codeword [n, 4] (16-byte aligned): weights =
  * eq(., r) over nbv = ceil(log2 w) EF4 challenges (challenges: nbv x 4 words,

@@ -67,6 +67,12 @@ def _load() -> C.CDLL:
         "orc_rs_encode_bitrev": (i32, [i32, _u32p, i64, i32, i32, u32, u32, _u32p]),
         "orc_fri_fold_bitrev": (i32, [i32, _u32p, i64, i32, _u32p, i32, u32, u32, _u32p]),
         "orc_smcs_bind_root": (None, [vp, _u32p, u32, u32, _u32p]),
+        "orc_ef4_inv": (None, [i32, _u32p, _u32p]),
+        "orc_eq_expand": (None, [i32, _u32p, i32, _u32p]),
+        "orc_eval_mle_base": (None, [i32, _u32p, i32, i32, _u32p, _u32p]),
+        "orc_eval_mle_ef4": (None, [i32, _u32p, i32, _u32p, _u32p]),
+        "orc_mle_fold": (None, [i32, _u32p, i64, _u32p, _u32p]),
+        "orc_rlc_columns_ex": (None, [i32, _u32p, i64, i32, _u32p, i32, i32, i32, _u32p]),
         "orc_duplex_init": (None, [vp]),
         "orc_duplex_observe": (None, [vp, vp, _u32p, i64]),
         "orc_duplex_sample": (None, [vp, vp, i32, _u32p]),
@@ -461,3 +467,150 @@ def fri_commit_phase(p2: Poseidon2, field: int, codeword, num_rounds: int, num_q
         ro += row_sizes[r]
         po += path_sizes[r]
     return CommitPhaseProof(roots, betas, final, pos, rl, pl)
+
+
+# ------------------------------------------------------------ basefold open --
+def ef4_mul(field: int, a, b) -> np.ndarray:
+    out = np.zeros(4, np.uint32)
+    LIB.orc_ef4_mul(field, u32(a).reshape(-1), u32(b).reshape(-1), out)
+    return out
+
+
+def ef4_inv(field: int, a) -> np.ndarray:
+    out = np.zeros(4, np.uint32)
+    LIB.orc_ef4_inv(field, u32(a).reshape(-1), out)
+    return out
+
+
+def ef4_add(field: int, a, b) -> np.ndarray:
+    p = MODULUS[field]
+    return ((u32(a).astype(np.uint64) + u32(b).astype(np.uint64)) % p).astype(np.uint32)
+
+
+def ef4_sub(field: int, a, b) -> np.ndarray:
+    p = MODULUS[field]
+    return ((u32(a).astype(np.uint64) + p - u32(b).astype(np.uint64)) % p).astype(np.uint32)
+
+
+def eq_expand(field: int, z) -> np.ndarray:
+    z = u32(z).reshape(-1, 4)
+    out = np.zeros((1 << z.shape[0], 4), np.uint32)
+    LIB.orc_eq_expand(field, z.reshape(-1), z.shape[0], out.reshape(-1))
+    return out
+
+
+def eval_mle_base(field: int, cols, z) -> np.ndarray:
+    """eval_mle of base columns [w, 2^m] at the EF4 point z [m, 4] -> [w, 4]."""
+    cols = u32(cols)
+    z = u32(z).reshape(-1, 4)
+    out = np.zeros((cols.shape[0], 4), np.uint32)
+    LIB.orc_eval_mle_base(field, cols.reshape(-1), cols.shape[0], z.shape[0], z.reshape(-1),
+                          out.reshape(-1))
+    return out
+
+
+def eval_mle_ef4(field: int, mle, z) -> np.ndarray:
+    mle = u32(mle).reshape(-1, 4)
+    z = u32(z).reshape(-1, 4)
+    out = np.zeros(4, np.uint32)
+    LIB.orc_eval_mle_ef4(field, mle.reshape(-1), z.shape[0],
+                         z.reshape(-1) if z.size else np.zeros(4, np.uint32), out)
+    return out
+
+
+def mle_fold(field: int, mle, beta) -> np.ndarray:
+    mle = u32(mle).reshape(-1, 4)
+    b = np.zeros(4, np.uint32)
+    bb = u32(beta).reshape(-1)
+    b[: bb.size] = bb
+    out = np.zeros((mle.shape[0] // 2, 4), np.uint32)
+    LIB.orc_mle_fold(field, mle.reshape(-1), mle.shape[0], b, out.reshape(-1))
+    return out
+
+
+def basefold_open(p2: Poseidon2, field: int, mats, z, log_blowup: int, shift_mont: int,
+                  num_queries: int, t: "Transcript") -> dict:
+    """BasefoldProver.open_batch over committed base-field matrices at the EF4
+    point z, the native wire (zorch/pcs/basefold/prover.py:215-247, 503-547,
+    419-480; kernel zorch/pcs/basefold/kernel.py:52-78; choreography
+    zorch/pcs/fold.py:277-299, 385-389):
+    observe each root -> observe each matrix's eval_mle values -> sample
+    ceil(log2 total width) batch challenges (base, as EF4) -> staggered
+    partial-Lagrange batching of MLEs, codewords and values -> observe the
+    round count (EF4) -> per round: message (s(0), s(1)) observed, pre-fold
+    pair leaves committed and the root observed, beta = one base squeeze, fold
+    codeword / MLE / claim -> observe the final codeword -> query positions
+    (Montgomery bits mod n) -> open every matrix and every fold layer.
+    mats: dicts with cols [w, S], codeword [w, n] (column-major, base) and
+    layers (digest layers of the row leaves)."""
+    z = u32(z).reshape(-1, 4)
+    v = z.shape[0]
+    S = 1 << v
+    n = S << log_blowup
+    one = np.zeros(4, np.uint32)
+    one[0] = to_mont(field, [1])[0]
+    for m in mats:
+        t.observe(m["layers"][-1][0])
+    values = []
+    for m in mats:
+        vals = eval_mle_base(field, m["cols"], z)
+        t.observe(vals.reshape(-1))
+        values.append(vals)
+    total = sum(int(m["cols"].shape[0]) for m in mats)
+    nbv = (total - 1).bit_length() if total > 1 else 0
+    chal = np.zeros((max(nbv, 1), 4), np.uint32)
+    if nbv:
+        chal[:nbv, 0] = t.sample(nbv)
+    mle = np.zeros((S, 4), np.uint32)
+    cw = np.zeros((n, 4), np.uint32)
+    off = 0
+    for m in mats:
+        w = int(m["cols"].shape[0])
+        LIB.orc_rlc_columns_ex(field, u32(m["cols"]).reshape(-1), S, w, chal.reshape(-1), nbv, off,
+                               int(off > 0), mle.reshape(-1))
+        LIB.orc_rlc_columns_ex(field, u32(m["codeword"]).reshape(-1), n, w, chal.reshape(-1), nbv,
+                               off, int(off > 0), cw.reshape(-1))
+        off += w
+    wt = eq_expand(field, chal[:nbv])
+    claim = np.zeros(4, np.uint32)
+    for c, val in enumerate(np.concatenate(values)):
+        claim = ef4_add(field, claim, ef4_mul(field, wt[c], val))
+    vm = np.zeros(4, np.uint32)
+    vm[0] = to_mont(field, [v])[0]
+    t.observe(vm)
+    msgs, roots, betas, layers = [], [], [], []
+    sh = shift_mont
+    for i in range(v):
+        zs = z[: v - i]
+        s0 = eval_mle_ef4(field, mle[0::2], zs[:-1])
+        s1 = ef4_add(field, ef4_mul(field, ef4_sub(field, claim, s0), ef4_inv(field, zs[-1])), s0)
+        msg = np.concatenate([s0, s1])
+        t.observe(msg)
+        N = cw.shape[0]
+        dl = merkle_commit(p2, cw, N // 2, 2, 4, (N // 2) * 4)
+        t.observe(dl[-1][0])
+        beta = t.sample(1)[0]
+        layers.append((cw, dl))
+        msgs.append(msg)
+        roots.append(dl[-1][0])
+        betas.append(beta)
+        cw = fri_fold(field, cw, True, [beta], False, sh)
+        mle = mle_fold(field, mle, [beta])
+        claim = ef4_add(field, s0, ef4_mul(field, np.array([beta, 0, 0, 0], np.uint32), s1))
+        sh = int(LIB.orc_mul(field, sh, sh)) if sh else 0
+    final = cw
+    t.observe(final.reshape(-1))
+    positions = (t.sample(num_queries) % np.uint32(n)).astype(np.int32)
+    comp = []
+    for m in mats:
+        w = int(m["cols"].shape[0])
+        comp.append(merkle_open(m["codeword"], n, w, 1, n, m["layers"], positions))
+    queries = []
+    for i, (lcw, dl) in enumerate(layers):
+        N = lcw.shape[0]
+        a = (positions % (N // 2)).astype(np.int32)
+        queries.append(merkle_open(lcw, N // 2, 2, 4, (N // 2) * 4, dl, a))
+    return {"values": values, "uni_msgs": np.stack(msgs) if msgs else np.zeros((0, 8), np.uint32),
+            "fri_roots": np.stack(roots) if roots else np.zeros((0, 8), np.uint32),
+            "betas": np.array(betas, np.uint32), "final_poly": final, "positions": positions,
+            "component_openings": comp, "query_openings": queries, "final_claim": claim}

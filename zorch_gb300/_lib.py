@@ -77,6 +77,15 @@ def _declare(lib: C.CDLL) -> None:
         "zc_fri_fold_commit_bitrev": (st, [vp, vp, i64, C.c_int, vp, C.c_int, u32, u32, vp, vp,
                                            vp]),
         "zc_smcs_bind_root": (st, [vp, vp, u32, u32, vp, vp]),
+        "zc_eq_expand_workspace_bytes": (sz, [i32]),
+        "zc_eq_expand": (st, [st, vp, i32, vp, vp, sz, vp]),
+        "zc_eval_mle_workspace_bytes": (sz, [i32, i32]),
+        "zc_eval_mle": (st, [st, vp, i32, i32, vp, vp, vp, sz, vp]),
+        "zc_rlc_columns_ex": (st, [st, vp, i64, i32, vp, i32, i32, i32, vp, vp]),
+        "zc_rlc_values": (st, [st, vp, i32, vp, i32, i32, i32, vp, vp]),
+        "zc_sumcheck_workspace_bytes": (sz, []),
+        "zc_sumcheck_message": (st, [st, vp, i64, vp, vp, vp, vp, vp, sz, vp]),
+        "zc_sumcheck_fold": (st, [st, vp, i64, vp, i32, vp, vp, vp, vp, vp, vp]),
         "zc_duplex_hop": (st, [vp, vp, vp, vp, vp, vp, vp, i64, i32, vp, vp, vp, vp, vp, vp, vp]),
         "zc_duplex_hop_host": (st, [vp, vp, vp, vp, vp, vp, vp, i64, i32, vp, vp, vp, vp, vp, vp]),
         "zc_duplex_step": (st, [vp, vp, vp, i64, i32, vp, vp, i64, vp]),

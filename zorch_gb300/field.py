@@ -49,6 +49,43 @@ class Field:
         return pow(g, (self.p - 1) >> log_n, self.p)
 
 
+    # -- EF4 = F[x]/(x^4 - w) on the host, canonical coefficient tuples (c0..c3);
+    # verifier-side scalar arithmetic (a few operations per round or query).
+    def ef_mul(self, a, b) -> tuple:
+        p, w = self.p, self.ef4_w
+        t = [0] * 7
+        for i in range(4):
+            for j in range(4):
+                t[i + j] += a[i] * b[j]
+        return tuple((t[i] + (w * t[i + 4] if i < 3 else 0)) % p for i in range(4))
+
+    def ef_add(self, a, b) -> tuple:
+        return tuple((x + y) % self.p for x, y in zip(a, b))
+
+    def ef_sub(self, a, b) -> tuple:
+        return tuple((x - y) % self.p for x, y in zip(a, b))
+
+    def ef_scale(self, a, s: int) -> tuple:
+        return tuple(x * s % self.p for x in a)
+
+    def ef_inv(self, a) -> tuple:
+        """a^(p^4 - 2)."""
+        e = self.p ** 4 - 2
+        r, b = (1, 0, 0, 0), tuple(a)
+        while e:
+            if e & 1:
+                r = self.ef_mul(r, b)
+            b = self.ef_mul(b, b)
+            e >>= 1
+        return r
+
+    def ef_from_mont(self, words) -> tuple:
+        return tuple(self.canon(int(x)) for x in words)
+
+    def ef_to_mont(self, a) -> list:
+        return [self.mont(x) for x in a]
+
+
 BABYBEAR = Field(_lib.BABYBEAR, "babybear", 2013265921, 31, 27, 11)
 KOALABEAR = Field(_lib.KOALABEAR, "koalabear", 2130706433, 3, 24, 3)
 FIELDS = {BABYBEAR.id: BABYBEAR, KOALABEAR.id: KOALABEAR}

@@ -231,14 +231,49 @@ class FriProver:
 
 @dataclass
 class BasefoldProverData:
+    """zorch/pcs/basefold/prover.py:65-83: digest layers, the codeword (column
+    major [K, block_len]; codeword.T rows are the leaves) and the message
+    columns [K, S] (the reference's mle.T, kept for the open)."""
+
     digest_layers: DigestLayers
-    codeword: torch.Tensor  # [K, block_len]: column-major; codeword.T rows are the leaves
+    codeword: torch.Tensor
     widths: tuple
+    columns: torch.Tensor | None = None
+
+
+@dataclass
+class BasefoldProof:
+    """zorch/pcs/basefold/config.py BasefoldProof: per round the sumcheck
+    message (s(0), s(1)) and the pre-fold pair-leaf root, the cleartext final
+    codeword, every matrix opened at the query positions and every fold layer's
+    pair leaf at its halved position."""
+
+    uni_msgs: torch.Tensor            # [v, 8]: s(0) c0..c3, s(1) c0..c3
+    fri_roots: torch.Tensor           # [v, 8]
+    final_poly: torch.Tensor          # [blowup, 4]
+    component_openings: list[Opening]
+    query_openings: list[Opening]
+    positions: torch.Tensor           # [Q]
+
+    def to_bytes(self) -> bytes:
+        """Mont-u32 little endian in pytree flatten order: messages, roots,
+        final poly, component then query openings (row, path)."""
+        parts = [self.uni_msgs.reshape(-1), self.fri_roots.reshape(-1),
+                 self.final_poly.reshape(-1)]
+        for op in list(self.component_openings) + list(self.query_openings):
+            parts += [op.row.reshape(-1), op.path.reshape(-1)]
+        return to_host(torch.cat(parts)).astype("<u4").tobytes()
+
+
+def _ceil_log2(x: int) -> int:
+    return (x - 1).bit_length() if x > 1 else 0
 
 
 class BasefoldProver:
-    """Basefold matrix commit (zorch/pcs/basefold/prover.py:190-193, 437-455):
-    one batched LDE over the [K, S] columns, leaves = codeword rows."""
+    """Basefold PCS prover (zorch/pcs/basefold/prover.py:160-247, 419-547):
+    the matrix commit (one batched LDE over the [K, S] columns, leaves =
+    codeword rows) and the native batch open (staggered batching of the
+    matrices, interleaved sumcheck + pre-fold pair commits, queries)."""
 
     def __init__(self, code: ReedSolomon, tree: MerkleTree, num_queries: int = 4) -> None:
         self.code = code
@@ -250,15 +285,239 @@ class BasefoldProver:
         cw = self.code.encode(columns)
         K, n = cw.shape
         _, layers = self.tree.commit_layout(leaves_layout(cw, n, K, 1, n), cw.device)
-        return layers.root, BasefoldProverData(layers, cw, (K,))
+        return layers.root, BasefoldProverData(layers, cw, (K,), columns.contiguous())
+
+    def open_batch(self, rounds: Sequence[BasefoldProverData], z: torch.Tensor,
+                   transcript: DuplexTranscript):
+        """Batch-open the committed matrices at the shared EF4 point z [v, 4]
+        (Montgomery words on the device; _open_batch_body,
+        zorch/pcs/basefold/prover.py:503-547, and _fold_and_query, :419-480):
+        returns (values: per matrix [w, 4], proof, transcript). The whole open
+        runs on the device; the only host work is 1/z per coordinate."""
+        from .field import from_mont_np
+        if not rounds:
+            raise ValueError("BaseFold opens at least one committed matrix, got none")
+        if z.dim() != 2 or z.shape[1] != 4 or z.shape[0] < 1:
+            raise ValueError("the opening point is EF4 [num_vars >= 1, 4]")
+        code, tree, f = self.code, self.tree, self.code.field
+        v = z.shape[0]
+        S = 1 << v
+        if code.message_len != S:
+            raise ValueError(f"point dimension {v} doesn't match MLE height {code.message_len}")
+        for pd in rounds:
+            if pd.columns is None or pd.columns.shape[1] != S:
+                raise ValueError("prover data without its [K, S] message columns")
+        dev = z.device
+        L = _lib.lib()
+        st = stream_handle()
+        zc = z.contiguous()
+        t = transcript._copy()
+        for pd in rounds:
+            t.observe_(pd.digest_layers.root)
+        values = []
+        for pd in rounds:
+            w = pd.columns.shape[0]
+            out = torch.empty((w, 4), dtype=torch.int32, device=dev)
+            nb = L.zc_eval_mle_workspace_bytes(w, v)
+            ws = torch.empty((nb + 15) // 4, dtype=torch.int32, device=dev)
+            _lib.check(L.zc_eval_mle(f.id, ptr(pd.columns), w, v, ptr(zc), ptr(out), ptr(ws), nb,
+                                     st), "eval_mle")
+            t.observe_(out.reshape(-1))
+            values.append(out)
+        total = sum(int(pd.columns.shape[0]) for pd in rounds)
+        nbv = _ceil_log2(total)
+        chal = torch.zeros((max(nbv, 1), 4), dtype=torch.int32, device=dev)
+        if nbv:
+            chal[:nbv, 0] = t.sample_(nbv)
+        n = code.block_len
+        mle = torch.empty((S, 4), dtype=torch.int32, device=dev)
+        cw = torch.empty((n, 4), dtype=torch.int32, device=dev)
+        claim = torch.empty(4, dtype=torch.int32, device=dev)
+        off = 0
+        for pd, vals in zip(rounds, values):
+            w = pd.columns.shape[0]
+            acc = int(off > 0)
+            _lib.check(L.zc_rlc_columns_ex(f.id, ptr(pd.columns), S, w, ptr(chal), nbv, off, acc,
+                                           ptr(mle), st), "rlc mle")
+            _lib.check(L.zc_rlc_columns_ex(f.id, ptr(pd.codeword), n, w, ptr(chal), nbv, off, acc,
+                                           ptr(cw), st), "rlc codeword")
+            _lib.check(L.zc_rlc_values(f.id, ptr(vals), w, ptr(chal), nbv, off, acc, ptr(claim),
+                                       st), "rlc values")
+            off += w
+        t.observe_(torch.tensor([f.mont(v), 0, 0, 0], dtype=torch.int32, device=dev))
+        # 1/z per coordinate (statement data, on the host)
+        zh = from_mont_np(f, to_host(zc))
+        zinv = torch.tensor(np.array([f.ef_to_mont(f.ef_inv(tuple(int(x) for x in row)))
+                                      for row in zh], np.uint32).view(np.int32), device=dev)
+        eq = torch.empty((max(S // 2, 1), 4), dtype=torch.int32, device=dev)
+        nb = L.zc_eq_expand_workspace_bytes(v - 1)
+        ews = torch.empty(max((nb + 15) // 4, 4), dtype=torch.int32, device=dev)
+        _lib.check(L.zc_eq_expand(f.id, ptr(zc), v - 1, ptr(eq), ptr(ews), nb, st), "eq_expand")
+        scb = L.zc_sumcheck_workspace_bytes()
+        scws = torch.empty(scb // 4, dtype=torch.int32, device=dev)
+        msgs = torch.empty((v, 8), dtype=torch.int32, device=dev)
+        rnd = PreFoldPairCommitRound(code, tree, 1)
+        layers: list[CommittedLayer] = []
+        pending = None
+        for i in range(v):
+            M = S >> (i + 1)
+            _lib.check(L.zc_sumcheck_message(f.id, ptr(mle), M, ptr(eq), ptr(claim),
+                                             ptr(zinv[v - 1 - i]), ptr(msgs[i]), ptr(scws), scb,
+                                             st), "sumcheck_message")
+            t.observe_(msgs[i])
+            layer = pending if pending is not None else rnd.commit_layer(cw)
+            beta = t.observe_and_sample_(layer.root, 1)
+            if i < v - 1 and cw.shape[0] >= 4:
+                cw_next, pending = rnd.fold_commit(cw, beta, i)
+            else:
+                cw_next, pending = code.fold(cw, beta), None
+            mle_next = torch.empty((M, 4), dtype=torch.int32, device=dev)
+            eq_next = torch.empty((M // 2, 4), dtype=torch.int32, device=dev) if M >= 2 else None
+            _lib.check(L.zc_sumcheck_fold(f.id, ptr(mle), M, ptr(beta), 1, ptr(msgs[i]),
+                                          ptr(mle_next), ptr(eq) if eq_next is not None else None,
+                                          ptr(eq_next) if eq_next is not None else None,
+                                          ptr(claim), st), "sumcheck_fold")
+            layers.append(layer)
+            mle, eq, cw = mle_next, eq_next, cw_next
+        final = cw
+        positions = t.sample_positions_(n, self.num_queries, values=final)
+        comp = [self.open_rows(pd, positions, check=False) for pd in rounds]
+        queries = []
+        q = positions
+        for i, layer in enumerate(layers):
+            q = torch.remainder(q, n >> (i + 1))
+            queries.append(open_layer(tree, layer, q))
+        proof = BasefoldProof(msgs, torch.stack([ly.root for ly in layers]), final, comp,
+                              queries, positions)
+        return values, proof, t
 
     def commit(self, polys: Sequence[torch.Tensor]):
         return self.commit_columns(torch.stack(list(polys), dim=0))
 
-    def open_rows(self, data: BasefoldProverData, indices: torch.Tensor) -> Opening:
+    def open_rows(self, data: BasefoldProverData, indices: torch.Tensor,
+                  check: bool = True) -> Opening:
         K, n = data.codeword.shape
         return self.tree.open_layout(leaves_layout(data.codeword, n, K, 1, n),
-                                     data.digest_layers, indices, K)
+                                     data.digest_layers, indices, K, check=check)
+
+
+class BasefoldVerifier:
+    """The native Basefold batch verifier on the host
+    (zorch/pcs/basefold/verifier.py:429-540): replays the transcript, checks
+    every sumcheck round against the running claim, the final codeword
+    against the reduced claim, every Merkle opening against its root, the
+    batched component rows against fold layer 0, and the fold chain down to
+    the final codeword. Returns a boolean verdict, never raises on a bad proof."""
+
+    def __init__(self, code: ReedSolomon, tree: MerkleTree, num_queries: int = 4) -> None:
+        self.code = code
+        self.tree = tree
+        self.num_queries = num_queries
+
+    def verify(self, commitments, z, values, proof: BasefoldProof) -> bool:
+        from .field import from_mont_np
+        from .transcript import HostDuplexTranscript
+        f, code, tree = self.code.field, self.code, self.tree
+        host = lambda x: to_host(x) if torch.is_tensor(x) else np.asarray(x, np.uint32)  # noqa: E731
+        ef = lambda words: f.ef_from_mont(words)  # noqa: E731
+        zc = [ef(r) for r in host(z).reshape(-1, 4)]
+        v = len(zc)
+        n = code.block_len
+        msgs = host(proof.uni_msgs).reshape(-1, 8)
+        roots = host(proof.fri_roots).reshape(-1, 8)
+        if msgs.shape[0] != v or roots.shape[0] != v or code.message_len != 1 << v:
+            return False
+        t = HostDuplexTranscript(tree.perm)
+        for c in commitments:
+            t = t.observe(host(c).reshape(-1))
+        vals = [host(x).reshape(-1, 4) for x in values]
+        for x in vals:
+            t = t.observe(x.reshape(-1))
+        total = sum(x.shape[0] for x in vals)
+        nbv = _ceil_log2(total)
+        chal = []
+        if nbv:
+            t, s = t.sample(nbv)
+            chal = [f.canon(int(x)) for x in s]
+
+        def weight(idx: int) -> tuple:
+            w = (1, 0, 0, 0)
+            for j, r in enumerate(chal):
+                bit = (idx >> (nbv - 1 - j)) & 1
+                w = f.ef_scale(w, r) if bit else f.ef_scale(w, (1 - r) % f.p)
+            return w
+
+        wts = [weight(c) for c in range(total)]
+        claim = (0, 0, 0, 0)
+        for c, x in enumerate(np.concatenate(vals)):
+            claim = f.ef_add(claim, f.ef_mul(wts[c], ef(x)))
+        t = t.observe(np.array([f.mont(v), 0, 0, 0], np.uint32))
+        ok = True
+        betas = []
+        for i in range(v):
+            s0, s1 = ef(msgs[i, :4]), ef(msgs[i, 4:])
+            zl = zc[v - 1 - i]
+            one_minus = f.ef_sub((1, 0, 0, 0), zl)
+            ok &= claim == f.ef_add(f.ef_mul(one_minus, s0), f.ef_mul(zl, s1))
+            t = t.observe(msgs[i])
+            t, b = t.observe_and_sample(roots[i], 1)
+            beta = f.canon(int(b[0]))
+            betas.append(beta)
+            claim = f.ef_add(s0, f.ef_scale(s1, beta))
+        final = host(proof.final_poly).reshape(-1, 4)
+        ok &= final.shape[0] == n >> v and all(ef(x) == claim for x in final)
+        t = t.observe(final.reshape(-1))
+        t, raw = t.sample(self.num_queries)
+        positions = [int(x) % n for x in raw]
+        if [int(x) for x in host(proof.positions).view(np.int32)] != positions:
+            return False
+        # Merkle openings
+        for pos_i, q in enumerate(positions):
+            for r, (c, op) in enumerate(zip(commitments, proof.component_openings)):
+                row = Opening(op.row[pos_i], op.path[:, pos_i])
+                ok &= tree.verify(c if torch.is_tensor(c) else torch.tensor(c), q, row)
+            a = q
+            for i, op in enumerate(proof.query_openings):
+                a = a % (n >> (i + 1))
+                ok &= tree.verify(torch.as_tensor(roots[i].view(np.int32)), a,
+                                  Opening(op.row[pos_i], op.path[:, pos_i]))
+        if not ok:
+            return False
+        # batched component rows == fold layer 0's leg at the position
+        shift = code.coset_shift
+        for pos_i, q in enumerate(positions):
+            comp = (0, 0, 0, 0)
+            off = 0
+            for op in proof.component_openings:
+                row = host(op.row)[pos_i]
+                for c, x in enumerate(row):
+                    comp = f.ef_add(comp, f.ef_scale(wts[off + c], f.canon(int(x))))
+                off += len(row)
+            leaf0 = host(proof.query_openings[0].row)[pos_i].reshape(2, 4)
+            a0 = q % (n >> 1)
+            ok &= comp == ef(leaf0[0] if q == a0 else leaf0[1])
+            # fold chain
+            a = q
+            for i in range(v):
+                ni = n >> i
+                a = q % (ni >> 1)
+                leaf = host(proof.query_openings[i].row)[pos_i].reshape(2, 4)
+                lo, hi = ef(leaf[0]), ef(leaf[1])
+                sh = pow(shift, 1 << i, f.p) if shift is not None else 1
+                x = sh * pow(f.root_of_unity((ni).bit_length() - 1, code.generator or None), a,
+                             f.p) % f.p
+                inv2x = pow(2 * x % f.p, f.p - 2, f.p)
+                inv2 = pow(2, f.p - 2, f.p)
+                folded = f.ef_add(f.ef_scale(f.ef_add(lo, hi), inv2),
+                                  f.ef_scale(f.ef_sub(lo, hi), betas[i] * inv2x % f.p))
+                if i + 1 < v:
+                    a_next = q % (ni >> 2)
+                    nxt = host(proof.query_openings[i + 1].row)[pos_i].reshape(2, 4)
+                    expected = ef(nxt[0] if a == a_next else nxt[1])
+                else:
+                    expected = ef(final[a])
+                ok &= folded == expected
+        return bool(ok)
 
 
 class GraphedFriCommitPhase:
