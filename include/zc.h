@@ -217,6 +217,15 @@ zc_status zc_fri_fold_commit(const zc_poseidon2* p, const uint32_t* cw, int64_t 
                              uint32_t generator, uint32_t* out, uint32_t* next_layers,
                              void* stream);
 
+/* Replaces ReedSolomon.fold_group (zorch/coding/reed_solomon.py:357-381;
+ * fri_fold_k :551-586): the k-ary fold, k = 2^log_k (log_k 1..4), of a
+ * natural-order layer of n elements. Group p < n/k is
+ * (cw[p], cw[p + n/k], ..., cw[p + (k-1) n/k]) on the points
+ * shift_mont * w_n^(p + m n/k); out[p] is its degree-(k-1) interpolant at
+ * beta. Limb conventions as zc_fri_fold. */
+zc_status zc_fri_fold_k(zc_field field, const uint32_t* cw, int64_t n, int ef_in,
+                        const uint32_t* beta, int ef_beta, int log_k, uint32_t shift_mont,
+                        uint32_t generator, uint32_t* out, void* stream);
 /* Replaces BitReversedReedSolomon.fold (zorch/coding/reed_solomon.py:484-492,
  * 532-540) on a bit-reversed layer: out[p] folds the adjacent pair
  * (cw[2p], cw[2p+1]) at x_p = shift_mont * w_n^brev(p) (p read over

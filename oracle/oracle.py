@@ -67,6 +67,7 @@ def _load() -> C.CDLL:
         "orc_rs_encode_bitrev": (i32, [i32, _u32p, i64, i32, i32, u32, u32, _u32p]),
         "orc_fri_fold_bitrev": (i32, [i32, _u32p, i64, i32, _u32p, i32, u32, u32, _u32p]),
         "orc_smcs_bind_root": (None, [vp, _u32p, u32, u32, _u32p]),
+        "orc_fri_fold_k": (i32, [i32, _u32p, i64, i32, _u32p, i32, i32, u32, u32, _u32p]),
         "orc_ef4_inv": (None, [i32, _u32p, _u32p]),
         "orc_eq_expand": (None, [i32, _u32p, i32, _u32p]),
         "orc_eval_mle_base": (None, [i32, _u32p, i32, i32, _u32p, _u32p]),
@@ -339,6 +340,22 @@ def fri_fold_bitrev(field, cw, ef_in: bool, beta, ef_beta: bool, shift_mont=0, g
                                  shift_mont, generator, out.reshape(-1))
     if rc:
         raise ValueError("fri_fold_bitrev needs a power-of-two length >= 2")
+    return out
+
+
+def fri_fold_k(field, cw, ef_in: bool, beta, ef_beta: bool, log_k: int, shift_mont=0,
+               generator=0):
+    """ReedSolomon.fold_group (zorch/coding/reed_solomon.py:357-381)."""
+    cw = u32(cw)
+    n = cw.shape[0]
+    lo = 4 if (ef_in or ef_beta) else 1
+    out = np.zeros((n >> log_k, lo) if lo == 4 else (n >> log_k,), np.uint32)
+    b = np.zeros(4, np.uint32)
+    b[: (4 if ef_beta else 1)] = u32(beta).reshape(-1)[: (4 if ef_beta else 1)]
+    rc = LIB.orc_fri_fold_k(field, cw.reshape(-1), n, int(ef_in), b, int(ef_beta), log_k,
+                            shift_mont, generator, out.reshape(-1))
+    if rc:
+        raise ValueError("fri_fold_k needs a power-of-two length >= k")
     return out
 
 

@@ -582,6 +582,56 @@ int orc_fri_fold_bitrev(int field, const uint32_t* cw, int64_t n, int ef_in, con
   return 0;
 }
 
+/* k-ary fold (ReedSolomon.fold_group, zorch/coding/reed_solomon.py:357-381,
+ * fri_fold_k points= path :551-586, compute_lagrange_basis
+ * zorch/poly/univariate.py:56-65): group p < n/k is
+ * (cw[p], cw[p + n/k], ..., cw[p + (k-1)n/k]) on the points
+ * x_m = shift w_n^(p + m n/k); out[p] = sum_m g_m L_m(beta), L_m the Lagrange
+ * basis of the group's points. Values and beta EF4 or base; x base. */
+int orc_fri_fold_k(int field, const uint32_t* cw, int64_t n, int ef_in, const uint32_t* beta,
+                   int ef_beta, int log_k, uint32_t shift_mont, uint32_t generator,
+                   uint32_t* out) {
+  const fld* F = FLD(field);
+  const int k = 1 << log_k;
+  if (!is_pow2(n) || n < k || log_k < 1 || log_k > 6) return 2;
+  int log_n = 0;
+  while (((int64_t)1 << log_n) < n) log_n++;
+  const int li = ef_in ? 4 : 1, lb = ef_beta ? 4 : 1, lo = (ef_in || ef_beta) ? 4 : 1;
+  const int64_t sub = n / k;
+  const uint32_t w = root_of_unity(F, log_n, generator);
+  const uint32_t sh = shift_mont ? shift_mont : F->one;
+  uint32_t bt[4] = {0, 0, 0, 0};
+  for (int e = 0; e < lb; e++) bt[e] = beta[e];
+#pragma omp parallel for num_threads(orc_get_threads()) schedule(static)
+  for (int64_t p = 0; p < sub; p++) {
+    uint32_t x[64];
+    for (int m = 0; m < k; m++) x[m] = fmul(F, sh, fpow(F, w, (uint64_t)(p + m * sub)));
+    uint32_t acc[4] = {0, 0, 0, 0};
+    for (int m = 0; m < k; m++) {
+      /* L_m(beta) = prod_{j != m} (beta - x_j) / (x_m - x_j) */
+      uint32_t num[4] = {F->one, 0, 0, 0};
+      uint32_t den = F->one;
+      for (int j = 0; j < k; j++) {
+        if (j == m) continue;
+        uint32_t d[4];
+        memcpy(d, bt, 16);
+        d[0] = fsub(F, d[0], x[j]);
+        ef4_mul(F, num, d, num);
+        den = fmul(F, den, fsub(F, x[m], x[j]));
+      }
+      const uint32_t dinv = finv(F, den);
+      for (int e = 0; e < 4; e++) num[e] = fmul(F, num[e], dinv);
+      uint32_t g[4] = {0, 0, 0, 0};
+      for (int e = 0; e < li; e++) g[e] = cw[(p + m * sub) * li + e];
+      uint32_t t[4];
+      ef4_mul(F, g, num, t);
+      for (int e = 0; e < 4; e++) acc[e] = fadd(F, acc[e], t[e]);
+    }
+    for (int e = 0; e < lo; e++) out[p * lo + e] = acc[e];
+  }
+  return 0;
+}
+
 /* SingleMatrixCommitmentScheme.bind_root (zorch/commit/smcs.py:118-140):
  * compress([raw_root, sponge([log_height, width])]), the two shape words as
  * field elements. */

@@ -110,6 +110,11 @@ int orc_fri_fold_bitrev(int field, const uint32_t* cw, int64_t n, int ef_in,
                         const uint32_t* beta, int ef_beta, uint32_t shift_mont,
                         uint32_t generator, uint32_t* out);
 
+/* k-ary Lagrange fold of a natural-order layer (k = 2^log_k <= 64). */
+int orc_fri_fold_k(int field, const uint32_t* cw, int64_t n, int ef_in, const uint32_t* beta,
+                   int ef_beta, int log_k, uint32_t shift_mont, uint32_t generator,
+                   uint32_t* out);
+
 /* SP1 single-matrix commitment domain separator. */
 void orc_smcs_bind_root(const orc_p2* p, const uint32_t* raw_root, uint32_t log_height,
                         uint32_t width, uint32_t* out8);

@@ -74,6 +74,7 @@ def _declare(lib: C.CDLL) -> None:
         "zc_fri_fold": (st, [st, vp, i64, C.c_int, vp, C.c_int, u32, u32, vp, vp]),
         "zc_fri_fold_commit": (st, [vp, vp, i64, C.c_int, vp, C.c_int, u32, u32, vp, vp, vp]),
         "zc_fri_fold_bitrev": (st, [st, vp, i64, C.c_int, vp, C.c_int, u32, u32, vp, vp]),
+        "zc_fri_fold_k": (st, [st, vp, i64, C.c_int, vp, C.c_int, C.c_int, u32, u32, vp, vp]),
         "zc_fri_fold_commit_bitrev": (st, [vp, vp, i64, C.c_int, vp, C.c_int, u32, u32, vp, vp,
                                            vp]),
         "zc_smcs_bind_root": (st, [vp, vp, u32, u32, vp, vp]),

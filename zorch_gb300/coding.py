@@ -11,6 +11,7 @@ tensors of Montgomery words; the coset shift and generator are canonical ints
 
 from __future__ import annotations
 
+import numpy as np
 import torch
 
 from . import _lib
@@ -92,8 +93,8 @@ class ReedSolomon:
             raise ValueError(f"blowup must be a power of two, got {blowup}")
         if not _is_pow2(fold_factor) or fold_factor < 2:
             raise ValueError(f"fold_factor must be a power of two >= 2, got {fold_factor}")
-        if fold_factor != 2:
-            raise NotImplementedError("only the binary (arity-2) fold is built")
+        if fold_factor > 16:
+            raise NotImplementedError("k-ary folds are built for fold_factor <= 16")
         self.field = field_of(field)
         if generator not in (None, 0, self.field.generator):
             raise NotImplementedError("only the field's canonical generator is built")
@@ -195,6 +196,85 @@ class ReedSolomon:
 
     def check_final(self, final: torch.Tensor, claim: torch.Tensor) -> bool:
         return bool((final == claim).all())
+
+    # -- KFoldableCode: the k-ary fold (zorch/coding/reed_solomon.py:340-426) --
+    @property
+    def log_fold_factor(self) -> int:
+        return _log2(self.fold_factor)
+
+    def group_level_shift_mont(self, level: int) -> int:
+        """coset_shift^(k^level) (:418-426)."""
+        return self.level_shift_mont(self.log_fold_factor * level)
+
+    def group_level_of(self, n: int) -> int:
+        return _log2(self.block_len // n) // self.log_fold_factor
+
+    def fold_group(self, codeword: torch.Tensor, beta: torch.Tensor,
+                   out: torch.Tensor | None = None) -> torch.Tensor:
+        """k-ary fold of a natural-order layer (:357-381): n -> n/k."""
+        k = self.fold_factor
+        n = codeword.shape[0]
+        if n < k:
+            raise ValueError(f"fold_group requires a codeword length >= fold_factor {k}, got {n}")
+        ef_in = codeword.dim() == 2
+        ef_beta = beta.numel() == 4
+        if out is None:
+            shape = (n // k, 4) if (ef_in or ef_beta) else (n // k,)
+            out = torch.empty(shape, dtype=torch.int32, device=codeword.device)
+        level = self.group_level_of(n)
+        _lib.check(_lib.lib().zc_fri_fold_k(
+            self.field.id, ptr(codeword.contiguous()), n, int(ef_in), ptr(beta.contiguous()),
+            int(ef_beta), self.log_fold_factor, self.group_level_shift_mont(level),
+            self.generator or 0, ptr(out), stream_handle()), "fri_fold_k")
+        return out
+
+    def group_leaves(self, codeword: torch.Tensor) -> torch.Tensor:
+        """Leaf p = (cw[p], cw[p + n/k], ..., cw[p + (k-1)n/k]) in base limbs
+        (materialised; the commit round addresses it in place)."""
+        k = self.fold_factor
+        n = codeword.shape[0]
+        return codeword.reshape(k, n // k, -1).transpose(0, 1).reshape(n // k, -1)
+
+    def group_indices(self, positions: torch.Tensor, level: int) -> tuple:
+        sub = self.block_len >> (self.log_fold_factor * (level + 1))
+        return tuple(positions + m * sub for m in range(self.fold_factor))
+
+    def group_layer_positions(self, positions: torch.Tensor, num_rounds: int) -> list:
+        """a_i = q_i mod (n / k^{i+1}) (:395-406)."""
+        out, q = [], positions
+        for i in range(num_rounds):
+            q = torch.remainder(q, self.block_len >> (self.log_fold_factor * (i + 1)))
+            out.append(q)
+        return out
+
+    def fold_group_values(self, group, beta, positions, level: int) -> list:
+        """Host-side k-ary fold of opened groups (the verifier's path, :383-393):
+        `group` [Q, k] (or [Q, k, 4]) Montgomery words, `beta` 1 or 4 words,
+        `positions` [Q]; returns canonical EF4 tuples."""
+        f = self.field
+        g = np.asarray(group).reshape(len(positions), self.fold_factor, -1)
+        b = [int(x) for x in np.asarray(beta).reshape(-1)]
+        bt = f.ef_from_mont((b + [0, 0, 0])[:4])
+        n = self.block_len >> (self.log_fold_factor * level)
+        w = f.root_of_unity(_log2(n), self.generator or None)
+        sh = f.canon(self.group_level_shift_mont(level)) if self.coset_shift is not None else 1
+        out = []
+        for qi, p in enumerate(int(x) for x in np.asarray(positions).reshape(-1)):
+            xs = [sh * pow(w, p + m * (n // self.fold_factor), f.p) % f.p
+                  for m in range(self.fold_factor)]
+            acc = (0, 0, 0, 0)
+            for m in range(self.fold_factor):
+                num, den = (1, 0, 0, 0), 1
+                for j in range(self.fold_factor):
+                    if j != m:
+                        num = f.ef_mul(num, f.ef_sub(bt, (xs[j], 0, 0, 0)))
+                        den = den * (xs[m] - xs[j]) % f.p
+                lm = f.ef_scale(num, pow(den, f.p - 2, f.p))
+                words = [int(x) for x in g[qi, m]]
+                val = f.ef_from_mont(words + [0] * (4 - len(words)))
+                acc = f.ef_add(acc, f.ef_mul(val, lm))
+            out.append(acc)
+        return out
 
 
 def bit_reverse_indices(positions: torch.Tensor, n: int) -> torch.Tensor:

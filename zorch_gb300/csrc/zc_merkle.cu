@@ -347,6 +347,66 @@ __global__ void k_fold(const uint32_t* f, int64_t n, const uint32_t* beta, uint3
   for (int e = 0; e < M::LO; e++) g[j * M::LO + e] = out[e];
 }
 
+// k-ary fold (ReedSolomon.fold_group, zorch/coding/reed_solomon.py:357-381) by
+// the coset form of fri_fold_k (:551-586): group p < n/K is
+// (f[p], f[p + n/K], ..., f[p + (K-1) n/K]) on the points x0 w_K^m, x0 =
+// shift w_n^p, so its interpolant is Q(Y) = P(x0 Y) = sum_j c_j Y^j with
+// c = (1/K) sum_m g_m w_K^(-jm), and out[p] = Q(beta / x0) (Horner). The
+// interpolant is unique, so this equals the Lagrange form of the reference.
+template <class F, int LI, int LB, int K>
+__global__ void k_fold_k(const uint32_t* f, int64_t n, const uint32_t* beta, uint32_t shinv,
+                         uint32_t winv, uint32_t wkinv, uint32_t kinv, uint32_t* g) {
+  constexpr int LO = (LI == 4 || LB == 4) ? 4 : 1;
+  const int64_t sub = n / K;
+  const int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= sub) return;
+  ef4 v[K];
+#pragma unroll
+  for (int m = 0; m < K; m++) {
+    v[m] = ef4{{0, 0, 0, 0}};
+#pragma unroll
+    for (int e = 0; e < LI; e++) v[m].c[e] = __ldg(f + (p + m * sub) * LI + e);
+  }
+  uint32_t wk[K];  // w_K^(-j)
+  wk[0] = F::ONE;
+#pragma unroll
+  for (int j = 1; j < K; j++) wk[j] = mmul<F>(wk[j - 1], wkinv);
+  const uint32_t x0inv = mmul<F>(shinv, mpow<F>(winv, (uint64_t)p));
+  ef4 u{{0, 0, 0, 0}};
+#pragma unroll
+  for (int e = 0; e < LB; e++) u.c[e] = mmul<F>(__ldg(beta + e), x0inv);
+  ef4 acc{{0, 0, 0, 0}};
+#pragma unroll
+  for (int j = K - 1; j >= 0; j--) {
+    ef4 c{{0, 0, 0, 0}};
+#pragma unroll
+    for (int m = 0; m < K; m++) c = ef_add<F>(c, ef_scale<F>(v[m], wk[(j * m) & (K - 1)]));
+    c = ef_scale<F>(c, kinv);
+    acc = ef_add<F>(LB == 4 ? ef_mul<F>(acc, u) : ef_scale<F>(acc, u.c[0]), c);
+  }
+#pragma unroll
+  for (int e = 0; e < LO; e++) g[p * LO + e] = acc.c[e];
+}
+
+template <class F, int LI, int LB>
+zc_status fold_k_launch(const uint32_t* cw, int64_t n, const uint32_t* beta, int log_k,
+                        uint32_t shift_mont, uint32_t* out, cudaStream_t st) {
+  const int log_n = ilog2(n);
+  const uint32_t winv = minv<F>(root_of_unity<F>(log_n, 0));
+  const uint32_t wkinv = mpow<F>(winv, (uint64_t)(n >> log_k));
+  const uint32_t shinv = minv<F>(shift_mont ? shift_mont : F::ONE);
+  const uint32_t kinv = minv<F>(to_mont<F>(1u << log_k));
+  const int64_t sub = n >> log_k;
+  const unsigned grid = (unsigned)((sub + 127) / 128);
+  switch (log_k) {
+    case 1: k_fold_k<F, LI, LB, 2><<<grid, 128, 0, st>>>(cw, n, beta, shinv, winv, wkinv, kinv, out); break;
+    case 2: k_fold_k<F, LI, LB, 4><<<grid, 128, 0, st>>>(cw, n, beta, shinv, winv, wkinv, kinv, out); break;
+    case 3: k_fold_k<F, LI, LB, 8><<<grid, 128, 0, st>>>(cw, n, beta, shinv, winv, wkinv, kinv, out); break;
+    default: k_fold_k<F, LI, LB, 16><<<grid, 128, 0, st>>>(cw, n, beta, shinv, winv, wkinv, kinv, out); break;
+  }
+  return launch_check();
+}
+
 template <class F>
 struct FoldScalars {
   uint32_t inv2s, winv, w4inv;
@@ -687,6 +747,29 @@ zc_status zc_fri_fold(zc_field field, const uint32_t* cw, int64_t n, int ef_in,
   }
   return fri_fold_any<false>(field, cw, n, ef_in, beta, ef_beta, shift_mont, generator, out,
                              (cudaStream_t)stream);
+}
+
+zc_status zc_fri_fold_k(zc_field field, const uint32_t* cw, int64_t n, int ef_in,
+                        const uint32_t* beta, int ef_beta, int log_k, uint32_t shift_mont,
+                        uint32_t generator, uint32_t* out, void* stream) {
+  if (!cw || !beta || !out || log_k < 1 || log_k > 4) return ZC_BAD_ARG;
+  if (!is_pow2(n) || n < ((int64_t)1 << log_k)) {
+    set_error("fold_group requires a power-of-two codeword of length >= fold_factor");
+    return ZC_NOT_POW2;
+  }
+  if (generator != 0 && generator != (field == ZC_FIELD_BABYBEAR ? BabyBear::GEN : KoalaBear::GEN)) {
+    set_error("only the field's canonical generator is built");
+    return ZC_UNSUPPORTED;
+  }
+  cudaStream_t st = (cudaStream_t)stream;
+  return with_field(field, [&](auto f) {
+    using F = decltype(f);
+    if (ilog2(n) > F::TWO_ADICITY) return ZC_BAD_SHAPE;
+    if (ef_in && ef_beta) return fold_k_launch<F, 4, 4>(cw, n, beta, log_k, shift_mont, out, st);
+    if (ef_in) return fold_k_launch<F, 4, 1>(cw, n, beta, log_k, shift_mont, out, st);
+    if (ef_beta) return fold_k_launch<F, 1, 4>(cw, n, beta, log_k, shift_mont, out, st);
+    return fold_k_launch<F, 1, 1>(cw, n, beta, log_k, shift_mont, out, st);
+  });
 }
 
 zc_status zc_fri_fold_bitrev(zc_field field, const uint32_t* cw, int64_t n, int ef_in,

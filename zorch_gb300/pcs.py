@@ -117,6 +117,73 @@ class PreFoldPairCommitRound:
         return out, CommittedLayer(out, DigestLayers(flat, L))
 
 
+def group_layout(layer: torch.Tensor, k: int) -> _lib.Leaves:
+    """k-group leaves of a natural-order layer in place: leaf p =
+    (cw[p], cw[p + n/k], ..., cw[p + (k-1)n/k]) in base limbs."""
+    n = layer.shape[0]
+    limbs = limbs_of(layer)
+    return leaves_layout(layer, n // k, k, limbs, (n // k) * limbs)
+
+
+@dataclass
+class PreFoldKGroupCommitRound:
+    """commit the k-group leaves -> observe(root) -> sample beta -> k-ary fold
+    (zorch/pcs/fold.py:118-139): one leaf is one k-th-root coset, so one path
+    opens all k legs the fold consumes."""
+
+    code: ReedSolomon
+    tree: MerkleTree
+
+    def __call__(self, state: FoldState, t: DuplexTranscript):
+        cw = state.codeword
+        k = self.code.fold_factor
+        _, layers = self.tree.commit_layout(group_layout(cw, k), cw.device)
+        layer = CommittedLayer(cw, layers)
+        t = t._copy()
+        beta = t.observe_and_sample_(layer.root, 1)
+        out = self.code.fold_group(cw, beta)
+        return FoldState(out, state.layers + (layer,)), t, layer.root
+
+
+def open_group_layer(tree: MerkleTree, layer: CommittedLayer, indices: torch.Tensor,
+                     k: int) -> Opening:
+    """open_rows over a layer's k-group leaves."""
+    return tree.open_layout(group_layout(layer.codeword, k), layer.digest_layers, indices,
+                            k * layer.limbs, check=False)
+
+
+def verify_group_fold_chain(code: ReedSolomon, query_openings, betas, leaf_indices,
+                            final_poly) -> bool:
+    """Each opened k-group folds to the next layer's opened leg, the last to the
+    final poly (zorch/pcs/fold.py:471-505), on the host."""
+    f = code.field
+    k = code.fold_factor
+    final = to_host(final_poly) if torch.is_tensor(final_poly) else np.asarray(final_poly)
+    final = final.reshape(final.shape[0], -1)
+    ok = True
+    nr = len(query_openings)
+    host = lambda x: to_host(x) if torch.is_tensor(x) else np.asarray(x, np.uint32)  # noqa: E731
+    for i in range(nr):
+        rows = host(query_openings[i].row)
+        pos = [int(x) for x in host(leaf_indices[i]).view(np.int32)]
+        folded = code.fold_group_values(rows, host(betas[i]), pos, i)
+        if i + 1 < nr:
+            nxt_pos = torch.as_tensor(host(leaf_indices[i + 1]).view(np.int32))
+            members = [host(m).view(np.int32) for m in code.group_indices(nxt_pos, i + 1)]
+            nxt = host(query_openings[i + 1].row).reshape(len(pos), k, -1)
+            for qi, p in enumerate(pos):
+                legs = [m for m in range(k) if int(members[m][qi]) == p]
+                if len(legs) != 1:
+                    return False
+                words = [int(x) for x in nxt[qi, legs[0]]]
+                ok &= folded[qi] == f.ef_from_mont(words + [0] * (4 - len(words)))
+        else:
+            for qi, p in enumerate(pos):
+                words = [int(x) for x in final[p]]
+                ok &= folded[qi] == f.ef_from_mont(words + [0] * (4 - len(words)))
+    return bool(ok)
+
+
 def fold_rounds(rnd, state, transcript, rounds: int):
     """Run `rnd` exactly `rounds` times (zorch/prove.py:26-37)."""
     msgs = []
