@@ -540,10 +540,12 @@ def main():
             r.host = r.resident.cpu().pin_memory()
         torch.cuda.synchronize()
         served(host_fed=True)
+        h_runs = max(1, min(args.steps, 3))
         h0 = time.perf_counter()
-        h_res, _ = served(host_fed=True)
+        for _ in range(h_runs):
+            h_res, _ = served(host_fed=True)
         torch.cuda.synchronize()
-        h_dt = max_over_ranks(time.perf_counter() - h0, device)
+        h_dt = max_over_ranks(time.perf_counter() - h0, device) / h_runs
         value = elements * args.steps * world / sv_s
         e2e_value = elements * world / h_dt
         plain_value = elements / p_dt

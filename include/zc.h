@@ -179,6 +179,15 @@ zc_status zc_rs_encode_batch(zc_field field, const zc_lde_job* jobs, int32_t njo
  * power of two. */
 zc_status zc_merkle_commit(const zc_poseidon2* p, zc_leaves leaves, uint32_t* layers,
                            void* stream);
+/* Replaces StridedMerkleTree.commit (zorch/commit/strided_merkle.py:100-152):
+ * the leaves are the num_leaves rows of `leaves`; query-layer node y
+ * (s = num_leaves / rows_per_query of them) is the binary tree over rows
+ * y, y + s, ..., y + (rows_per_query - 1) s; layers: (2s-1)*8 words, the
+ * query layer first (the strided levels below it are not stored), root last.
+ * rows_per_query a power of two <= 128. Opening paths come from zc_merkle_open
+ * over s leaves with an empty row layout. */
+zc_status zc_strided_merkle_commit(const zc_poseidon2* p, zc_leaves leaves, int32_t rows_per_query,
+                                   uint32_t* layers, void* stream);
 /* Replaces open_rows / MerkleTree.open (zorch/pcs/fold.py:142-149,
  * zorch/commit/merkle.py:204-235): rows [q, w], paths [depth][q][8] leaf first.
  * Out-of-range indices are clamped on the device and reported as ZC_OOB_INDEX

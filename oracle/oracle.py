@@ -68,6 +68,7 @@ def _load() -> C.CDLL:
         "orc_fri_fold_bitrev": (i32, [i32, _u32p, i64, i32, _u32p, i32, u32, u32, _u32p]),
         "orc_smcs_bind_root": (None, [vp, _u32p, u32, u32, _u32p]),
         "orc_fri_fold_k": (i32, [i32, _u32p, i64, i32, _u32p, i32, i32, u32, u32, _u32p]),
+        "orc_strided_merkle_commit": (i32, [vp, _u32p, i64, i32, i32, i64, i32, _u32p]),
         "orc_ef4_inv": (None, [i32, _u32p, _u32p]),
         "orc_eq_expand": (None, [i32, _u32p, i32, _u32p]),
         "orc_eval_mle_base": (None, [i32, _u32p, i32, i32, _u32p, _u32p]),
@@ -218,6 +219,27 @@ def merkle_commit(p2: Poseidon2, base: np.ndarray, num_leaves: int, groups: int,
     out, off, n = [], 0, num_leaves
     while True:
         out.append(layers[8 * off: 8 * (off + n)].reshape(n, 8))
+        if n == 1:
+            break
+        off += n
+        n //= 2
+    return out
+
+
+def strided_merkle_commit(p2: Poseidon2, matrix: np.ndarray, rows_per_query: int):
+    """StridedMerkleTree.commit of a row-major [height, w] matrix
+    (zorch/commit/strided_merkle.py:100-152): stored layers from the query
+    layer (height / rows_per_query nodes) to the root."""
+    m = u32(matrix)
+    h, w = m.shape
+    s = h // rows_per_query
+    flat = np.zeros((2 * s - 1) * 8, np.uint32)
+    rc = LIB.orc_strided_merkle_commit(p2.ptr, m.reshape(-1), h, 1, w, 0, rows_per_query, flat)
+    if rc:
+        raise ValueError("strided commit needs power-of-two height and rows_per_query <= height")
+    out, off, n = [], 0, s
+    while True:
+        out.append(flat[8 * off: 8 * (off + n)].reshape(n, 8))
         if n == 1:
             break
         off += n

@@ -370,6 +370,51 @@ int orc_merkle_open(const uint32_t* base, int64_t L, int groups, int g, int64_t 
   return 0;
 }
 
+/* StridedMerkleTree.commit (zorch/commit/strided_merkle.py:100-152): leaf
+ * hashes of all `height` rows, then log2(rpq) query-strided levels
+ * next[x s + y] = compress(prev[2x s + y], prev[(2x+1) s + y]) (s = height /
+ * rpq, not stored), then the plain binary tree over the s query-layer nodes.
+ * layers: (2s-1)*8 words, query layer first. */
+int orc_strided_merkle_commit(const orc_p2* P, const uint32_t* base, int64_t height, int groups,
+                              int g, int64_t gstride, int rpq, uint32_t* layers) {
+  if (!is_pow2(height) || !is_pow2(rpq) || rpq > height) return 2;
+  const int w = groups * g;
+  const int64_t s = height / rpq;
+  uint32_t* cur = (uint32_t*)malloc(sizeof(uint32_t) * 8 * (size_t)height);
+#pragma omp parallel num_threads(orc_get_threads())
+  {
+    uint32_t* row = (uint32_t*)malloc(sizeof(uint32_t) * (size_t)(w > 0 ? w : 1));
+#pragma omp for schedule(static)
+    for (int64_t p = 0; p < height; p++) {
+      gather_leaf(base, p, groups, g, gstride, row);
+      orc_sponge_hash(P, row, w, cur + 8 * p);
+    }
+    free(row);
+  }
+  int64_t m = height;
+  while (m > s) {
+    uint32_t* nxt = (uint32_t*)malloc(sizeof(uint32_t) * 8 * (size_t)(m / 2));
+    for (int64_t x = 0; x < m / (2 * s); x++)
+      for (int64_t y = 0; y < s; y++)
+        orc_compress(P, cur + 8 * ((2 * x) * s + y), cur + 8 * ((2 * x + 1) * s + y),
+                     nxt + 8 * (x * s + y));
+    free(cur);
+    cur = nxt;
+    m /= 2;
+  }
+  memcpy(layers, cur, sizeof(uint32_t) * 8 * (size_t)s);
+  free(cur);
+  int64_t off = 0, n = s;
+  while (n > 1) {
+    const uint32_t* a = layers + 8 * off;
+    uint32_t* b = layers + 8 * (off + n);
+    for (int64_t i = 0; i < n / 2; i++) orc_compress(P, a + 16 * i, a + 16 * i + 8, b + 8 * i);
+    off += n;
+    n /= 2;
+  }
+  return 0;
+}
+
 /* ------------------------------------------------------------------ NTT ---- */
 static void ntt_inplace(const fld* F, uint32_t* a, int log_n, uint32_t omega) {
   const int64_t n = (int64_t)1 << log_n;

@@ -83,6 +83,10 @@ int orc_merkle_open(const uint32_t* base, int64_t num_leaves, int groups, int g,
                     int64_t gstride, const uint32_t* layers, const int32_t* idx,
                     int q, uint32_t* rows, uint32_t* paths);
 
+/* Query-strided Merkle tree (rows_per_query rows per query-layer node). */
+int orc_strided_merkle_commit(const orc_p2* p, const uint32_t* base, int64_t height, int groups,
+                              int g, int64_t gstride, int rpq, uint32_t* layers);
+
 /* Reed-Solomon coset LDE, natural order in and out. */
 int orc_rs_encode(int field, const uint32_t* coeffs, int64_t batch, int log_k,
                   int log_blowup, uint32_t shift_mont, uint32_t generator,

@@ -71,6 +71,7 @@ def _declare(lib: C.CDLL) -> None:
         "zc_rs_encode_bitrev": (st, [st, vp, i64, C.c_int, C.c_int, u32, u32, vp, vp, sz, vp]),
         "zc_merkle_commit": (st, [vp, Leaves, vp, vp]),
         "zc_merkle_open": (st, [Leaves, vp, vp, i32, vp, vp, vp, vp]),
+        "zc_strided_merkle_commit": (st, [vp, Leaves, i32, vp, vp]),
         "zc_fri_fold": (st, [st, vp, i64, C.c_int, vp, C.c_int, u32, u32, vp, vp]),
         "zc_fri_fold_commit": (st, [vp, vp, i64, C.c_int, vp, C.c_int, u32, u32, vp, vp, vp]),
         "zc_fri_fold_bitrev": (st, [st, vp, i64, C.c_int, vp, C.c_int, u32, u32, vp, vp]),

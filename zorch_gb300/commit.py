@@ -326,3 +326,95 @@ class SingleMatrixCommitmentScheme:
         want = np.asarray(commitment.detach().cpu() if torch.is_tensor(commitment)
                           else commitment).view(np.uint32).reshape(-1)
         return VerifyCode.OK if np.array_equal(bound, want) else VerifyCode.ROOT_MISMATCH
+
+
+class StridedMerkleTree:
+    """Query-strided binary Merkle commitment (zorch/commit/strided_merkle.py:43-230):
+    one query opens the `rows_per_query` rows {i, i+s, i+2s, ...} (s = height /
+    rows_per_query) under a single path; the strided levels below the s-node
+    query layer are not stored (the verifier re-hashes the opened coset)."""
+
+    def __init__(self, perm: Poseidon2, rows_per_query: int) -> None:
+        if rows_per_query < 1 or rows_per_query & (rows_per_query - 1):
+            raise ValueError(f"rows_per_query ({rows_per_query}) must be a power of two")
+        self.perm = perm
+        self.rows_per_query = rows_per_query
+        self.digest_elems = 8
+        self._top = MerkleTree(perm)
+
+    def __eq__(self, other) -> bool:
+        return (isinstance(other, StridedMerkleTree) and self.perm.handle == other.perm.handle
+                and self.rows_per_query == other.rows_per_query)
+
+    def __hash__(self) -> int:
+        return hash((self.perm.handle, self.rows_per_query))
+
+    def query_stride(self, height: int) -> int:
+        return height // self.rows_per_query
+
+    def commit(self, matrix: torch.Tensor) -> tuple[torch.Tensor, DigestLayers]:
+        """(raw_root (8,), digest layers from the query layer to the root)."""
+        if matrix.dim() != 2:
+            raise ValueError(f"matrix must be 2-D, got ndim={matrix.dim()}")
+        h, w = matrix.shape
+        if h & (h - 1) or h == 0:
+            raise ValueError(f"matrix height ({h}) must be a power of two")
+        if self.rows_per_query > h:
+            raise ValueError(f"rows_per_query ({self.rows_per_query}) > leaves ({h})")
+        m = matrix.contiguous()
+        s = self.query_stride(h)
+        flat = torch.empty((2 * s - 1, 8), dtype=torch.int32, device=m.device)
+        _lib.check(_lib.lib().zc_strided_merkle_commit(
+            self.perm.handle, leaves_layout(m, h, 1, w, 0), self.rows_per_query, ptr(flat),
+            stream_handle()), "strided_merkle_commit")
+        layers = DigestLayers(flat, s)
+        return layers.root, layers
+
+    def opened_rows(self, matrix: torch.Tensor, index: int) -> torch.Tensor:
+        s = self.query_stride(matrix.shape[0])
+        if not 0 <= index < s:
+            raise ValueError(f"index {index} out of range [0, {s})")
+        return matrix[index::s]
+
+    def open(self, matrix: torch.Tensor, layers: DigestLayers,
+             indices: torch.Tensor) -> Opening:
+        """Batched openings: rows [Q, rows_per_query, w] (the strided cosets)
+        and the stored sibling path [log2 s, Q, 8] from the query layer up."""
+        h, w = matrix.shape
+        s = self.query_stride(h)
+        idx = indices.to(torch.int32).contiguous()
+        if idx.numel() and (int(idx.min()) < 0 or int(idx.max()) >= s):
+            raise IndexError(f"query index out of range [0, {s})")
+        members = idx.long()[:, None] + s * torch.arange(self.rows_per_query,
+                                                         device=idx.device)[None, :]
+        rows = matrix[members.reshape(-1)].reshape(idx.numel(), self.rows_per_query, w)
+        empty = _lib.Leaves(None, s, 0, 0, 0)
+        q = idx.numel()
+        paths = torch.empty((layers.depth, q, 8), dtype=torch.int32, device=idx.device)
+        dummy = torch.empty(1, dtype=torch.int32, device=idx.device)
+        _lib.check(_lib.lib().zc_merkle_open(empty, ptr(layers.flat), ptr(idx), q, ptr(dummy),
+                                             ptr(paths), None, stream_handle()), "merkle_open")
+        return Opening(rows, paths)
+
+    def reconstruct_root(self, index: int, opening: Opening) -> np.ndarray:
+        """Re-hash the opened coset, fold it adjacent-pairwise to its query-layer
+        node, then climb the stored path by the index parity, on the host
+        (zorch/commit/strided_merkle.py:198-230)."""
+        rows = opening.row.detach().cpu().numpy().view(np.uint32)
+        layer = [self.perm.hash_host(r) for r in rows.reshape(self.rows_per_query, -1)]
+        while len(layer) > 1:
+            layer = [self.perm.compress_host(layer[2 * x], layer[2 * x + 1])
+                     for x in range(len(layer) // 2)]
+        node, idx = layer[0], int(index)
+        for sib in opening.path.detach().cpu().numpy().view(np.uint32).reshape(-1, 8):
+            node = self.perm.compress_host(node, sib) if idx % 2 == 0 else \
+                self.perm.compress_host(sib, node)
+            idx //= 2
+        return node
+
+    def verify(self, root: torch.Tensor, index: int, opening: Opening) -> bool:
+        depth = opening.path.reshape(-1, 8).shape[0]
+        if not 0 <= int(index) < (1 << depth):
+            return False
+        want = root.detach().cpu().numpy().view(np.uint32).reshape(-1)
+        return bool(np.array_equal(self.reconstruct_root(index, opening), want))

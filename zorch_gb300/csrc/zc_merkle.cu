@@ -62,6 +62,39 @@ struct NodeLeaf {
   }
 };
 
+// Query-layer node y of a query-strided tree (StridedMerkleTree,
+// zorch/commit/strided_merkle.py:100-152): the binary tree, adjacent pairs in
+// coset order, over the sponge-hashed rows y, y + s, ..., y + (rpq-1) s -- what
+// the reference's strided levels compute for residue y. One thread folds the
+// coset with a binary-counter stack (row r merges while bit b of r is set).
+constexpr int kMaxStridedLog = 8;
+struct StridedLeaf {
+  LayoutLeaf rows;
+  int64_t s;
+  int log_rpq;
+  template <class K>
+  __device__ __forceinline__ void digest(int64_t p, uint32_t* d, const K& k) const {
+    uint32_t stack[kMaxStridedLog][8];
+    const int rpq = 1 << log_rpq;
+    uint32_t cur[8];
+    for (int r = 0; r < rpq; r++) {
+      rows.digest(p + (int64_t)r * s, cur, k);
+      int b = 0;
+      for (; (r >> b) & 1; b++) {
+        uint32_t out[8];
+        p2_compress(stack[b], cur, out, k);
+#pragma unroll
+        for (int i = 0; i < 8; i++) cur[i] = out[i];
+      }
+      if (b < kMaxStridedLog)
+#pragma unroll
+        for (int i = 0; i < 8; i++) stack[b][i] = cur[i];
+    }
+#pragma unroll
+    for (int i = 0; i < 8; i++) d[i] = cur[i];
+  }
+};
+
 // fri_fold_values on one element j of a natural-order layer of n elements:
 // g = (f[j] + f[j+n/2])/2 + beta * (f[j] - f[j+n/2]) * xinv, xinv = 1/(2 x_j)
 // (zorch/coding/reed_solomon.py:543-548).
@@ -724,6 +757,31 @@ zc_status zc_merkle_commit(const zc_poseidon2* p, zc_leaves lv, uint32_t* layers
   return with_perm(p, [&](auto k, const P2Params* rt) {
     using K = decltype(k);
     return commit_tree<K>(leaf, layers, lv.num_leaves, rt, st);
+  });
+}
+
+zc_status zc_strided_merkle_commit(const zc_poseidon2* p, zc_leaves lv, int32_t rows_per_query,
+                                   uint32_t* layers, void* stream) {
+  if (!layers || (!lv.base && lv.groups * lv.group_len > 0) || lv.groups < 0 ||
+      lv.group_len < 0)
+    return ZC_BAD_ARG;
+  if (!is_pow2(lv.num_leaves) || !is_pow2(rows_per_query)) {
+    set_error("height and rows_per_query must be powers of two");
+    return ZC_NOT_POW2;
+  }
+  if (rows_per_query > lv.num_leaves || ilog2(rows_per_query) >= kMaxStridedLog) {
+    set_error("rows_per_query exceeds the height or 2^7");
+    return ZC_BAD_SHAPE;
+  }
+  if ((uintptr_t)layers % 16) return ZC_BAD_ARG;
+  if ((int64_t)lv.groups * lv.group_len > (1 << 20)) return ZC_BAD_SHAPE;
+  cudaStream_t st = (cudaStream_t)stream;
+  const int64_t s = lv.num_leaves / rows_per_query;
+  StridedLeaf leaf{LayoutLeaf{lv.base, lv.groups, lv.group_len, lv.group_stride}, s,
+                   ilog2(rows_per_query)};
+  return with_perm(p, [&](auto k, const P2Params* rt) {
+    using K = decltype(k);
+    return commit_tree<K>(leaf, layers, s, rt, st);
   });
 }
 
