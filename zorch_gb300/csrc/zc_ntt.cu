@@ -205,7 +205,7 @@ __device__ void lde_small_body(const uint32_t* x, uint32_t* out, int log_k, int 
 }
 
 template <class F>
-__global__ void __launch_bounds__(kThreads) k_lde_small(const uint32_t* x, uint32_t* out,
+__global__ void __launch_bounds__(kThreads, 2) k_lde_small(const uint32_t* x, uint32_t* out,
                                                         int log_k, int log_b, uint32_t h,
                                                         int brev_out) {
   extern __shared__ uint32_t sm[];
@@ -251,7 +251,7 @@ __device__ void lde_pass1_body(const uint32_t* x, uint32_t* z, int log_k1, int l
 }
 
 template <class F>
-__global__ void __launch_bounds__(kThreads) k_lde_pass1(const uint32_t* x, uint32_t* z, int log_k1,
+__global__ void __launch_bounds__(kThreads, 2) k_lde_pass1(const uint32_t* x, uint32_t* z, int log_k1,
                                                         int log_k2, int log_b, int log_ti,
                                                         uint32_t h) {
   extern __shared__ uint32_t sm[];
@@ -321,7 +321,7 @@ __device__ void lde_pass2_body(const uint32_t* z, uint32_t* out, int log_k1, int
 }
 
 template <class F>
-__global__ void __launch_bounds__(kThreads) k_lde_pass2(const uint32_t* z, uint32_t* out,
+__global__ void __launch_bounds__(kThreads, 2) k_lde_pass2(const uint32_t* z, uint32_t* out,
                                                         int log_k1, int log_k2, int log_b,
                                                         int log_tt, int brev_out) {
   extern __shared__ uint32_t sm[];
@@ -452,7 +452,7 @@ __device__ __forceinline__ int find_job(const int64_t* prefix, int njobs, int64_
 }
 
 template <class F>
-__global__ void __launch_bounds__(kThreads) k_lde_batch(const __grid_constant__ LdeBatch B,
+__global__ void __launch_bounds__(kThreads, 2) k_lde_batch(const __grid_constant__ LdeBatch B,
                                                         unsigned long long* counter) {
   extern __shared__ uint32_t sm[];
   __shared__ long long s_item;
