@@ -27,8 +27,11 @@ by zorch/pcs/jagged/testing/open_test.py:242-303):
   words, testdata/zerocheck_dense/prep_dense.npy, sliced to the round's raw
   area as open_test.py:147-150 does), lzma-compressed raw little-endian;
 - `prep_round.npz`: that round's component openings at the 52 query positions
-  (outputs/component_openings_r0.npz: rows and the 23 sibling levels) and the
-  query draws (outputs/challenges.npz `query_indices`);
+  (outputs/component_openings_r0.npz: rows and the 23 sibling levels), the
+  query draws (outputs/challenges.npz `query_indices`), the opening point
+  z_final (outputs/outer_sumcheck_point.npy) and the round's column
+  evaluation at its last 21 coordinates (outputs/batch_evals_r0.npz, the
+  eval_mle of open.py:202-204);
 - `fold_chain.npz`: the FRI fold betas and separator-bound fold-layer roots
   (challenges.npz `fri_betas`, fri_commitments.npy), the final poly, and the
   query openings (rows, sibling paths) of a subset of the fold layers
@@ -157,6 +160,8 @@ def sp1(ref_root: str) -> None:
         query_indices=ch["query_indices"].astype(np.uint32),
         rows=co["rows"].astype(np.uint32),
         paths=np.stack([co[f"proof_l{l}"] for l in range(depth)]).astype(np.uint32),
+        z_final=np.load(outs / "outer_sumcheck_point.npy").astype(np.uint32),
+        batch_evals=np.load(outs / "batch_evals_r0.npz")["mle0"].astype(np.uint32),
     )
 
     betas = ch["fri_betas"].astype(np.uint32)

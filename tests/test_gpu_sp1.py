@@ -95,6 +95,21 @@ def test_prep_round_commit_and_openings_match_sp1_dump(orc, sp1, golden):
         VerifyCode.WRONG_HEIGHT
 
 
+def test_batch_eval_matches_sp1_dump(orc, golden):
+    """zc_eval_mle of the prep column at the stacking point == the dumped
+    batch evaluation (zorch/pcs/jagged/open.py:202-204)."""
+    z = golden["round"]
+    m = int(z["log_stacking_height"])
+    L = _lib.lib()
+    out = torch.empty((1, 4), dtype=torch.int32, device="cuda")
+    nb = L.zc_eval_mle_workspace_bytes(1, m)
+    ws = torch.empty((nb + 15) // 4, dtype=torch.int32, device="cuda")
+    zd = dev(z["z_final"][-m:])
+    _lib.check(L.zc_eval_mle(KOALABEAR.id, dev(golden["prep"]).data_ptr(), 1, m, zd.data_ptr(),
+                             out.data_ptr(), ws.data_ptr(), nb, 0), "eval_mle")
+    assert np.array_equal(to_host(out), z["batch_evals"])
+
+
 @pytest.mark.parametrize("i", [0, 1, 10, 19, 20])
 def test_bitrev_fold_matches_sp1_dump(orc, golden, i):
     from zorch_gb300.coding import BitReversedReedSolomon

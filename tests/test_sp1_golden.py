@@ -61,6 +61,15 @@ def test_prep_round_component_openings(p2, prep):
     assert np.array_equal(paths, z["paths"])
 
 
+def test_batch_eval_of_the_prep_column(prep):
+    """eval_mle of the prep column at the stacking point z_final[-21:]
+    (zorch/pcs/jagged/open.py:202-204) == the dumped batch evaluation: pins the
+    eq-table orientation (z[0] the most significant index bit)."""
+    z = np.load(G / "prep_round.npz")
+    got = o.eval_mle_base(KB, prep.reshape(1, -1), z["z_final"][-int(z["log_stacking_height"]):])
+    assert np.array_equal(got, z["batch_evals"])
+
+
 def test_fold_layer_openings_bind_to_fri_commitments(p2, chain):
     coms = chain["fri_commitments"]
     n0 = 1 << 23

@@ -161,6 +161,17 @@ __device__ void smem_ntt_dif(uint32_t* a, int log_rows, int logm, int rs, const 
 
 constexpr int kThreads = 512;
 
+// Asynchronous 4-byte global -> shared copies (cp.async): a tile's loads are
+// all in flight at once, overlapping the twiddle-table set-up, instead of one
+// register-staged load per loop iteration waiting on memory.
+__device__ __forceinline__ void cp_async4(uint32_t* smem_dst, const uint32_t* gsrc) {
+  const unsigned d = (unsigned)__cvta_generic_to_shared(smem_dst);
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(d), "l"(gsrc) : "memory");
+}
+__device__ __forceinline__ void cp_async_wait_all() {
+  asm volatile("cp.async.wait_all;\n" ::: "memory");
+}
+
 // One column, all b cosets (single pass). `sm` is the block's dynamic smem.
 // Layout: work[b][rs] | tw[k/2] | hp[k] | wl[128] | wh[128].
 template <class F>
@@ -174,19 +185,23 @@ __device__ void lde_small_body(const uint32_t* x, uint32_t* out, int log_k, int 
   uint32_t* wl = hp + k;    // w_n^e, e < 128
   uint32_t* wh = wl + 128;  // w_n^(128 e), e < 128
   const uint32_t* xc = x + (c << log_k);
+  for (int idx = threadIdx.x; idx < (b << log_k); idx += blockDim.x)
+    cp_async4(work + (idx >> log_k) * rs + pad(idx & (k - 1)), xc + (idx & (k - 1)));
   const uint32_t wn = log_n ? omega_pow<F>(log_n, 1) : F::ONE;
   pow_table<F>(tw, k > 1 ? k / 2 : 1, log_k ? omega_pow<F>(log_k, 1) : F::ONE);
   pow_table<F>(hp, k, h);
   pow_table<F>(wl, 128, wn);
   pow_table<F>(wh, 128, mpow<F>(wn, 128));
+  cp_async_wait_all();
   for (int idx = threadIdx.x; idx < (b << log_k); idx += blockDim.x) {
     const int s = idx >> log_k, i = idx & (k - 1);
-    uint32_t v = mmul<F>(__ldg(xc + i), hp[i]);
+    uint32_t* slot = work + s * rs + pad(i);
+    uint32_t v = mmul<F>(*slot, hp[i]);
     if (s) {
       const int e = s * i;  // < n <= 2^14
       v = mmul<F>(v, mmul<F>(wl[e & 127], wh[e >> 7]));
     }
-    work[s * rs + pad(i)] = v;
+    *slot = v;
   }
   __syncthreads();
   smem_ntt_dif<F>(work, log_b, log_k, rs, tw);
@@ -228,18 +243,22 @@ __device__ void lde_pass1_body(const uint32_t* x, uint32_t* z, int log_k1, int l
   uint32_t* R = tw + (k2 > 1 ? k2 / 2 : 1);
   uint32_t* gi = R + k2;
   const int i1_0 = tile * TI;
+  const uint32_t* xc = x + (c << log_k);
+  for (int idx = threadIdx.x; idx < (TI << log_k2); idx += blockDim.x) {
+    const int d = idx & (TI - 1), i2 = idx >> log_ti;
+    cp_async4(work + d * rs + pad(i2), xc + i1_0 + d + ((int64_t)i2 << log_k1));
+  }
   const uint32_t gs = mmul<F>(h, s ? omega_pow<F>(log_n, (uint32_t)s) : F::ONE);
   const uint32_t G = mpow<F>(gs, (uint64_t)k1);
   pow_table<F>(tw, k2 > 1 ? k2 / 2 : 1, log_k2 ? omega_pow<F>(log_k2, 1) : F::ONE);
   pow_table<F>(R, k2, G);
   for (int i = threadIdx.x; i < TI; i += blockDim.x) gi[i] = mpow<F>(gs, (uint64_t)(i1_0 + i));
   __syncthreads();
-  const uint32_t* xc = x + (c << log_k);
+  cp_async_wait_all();
   for (int idx = threadIdx.x; idx < (TI << log_k2); idx += blockDim.x) {
     const int d = idx & (TI - 1), i2 = idx >> log_ti;
-    uint32_t v = __ldg(xc + i1_0 + d + ((int64_t)i2 << log_k1));
-    v = mmul<F>(mmul<F>(v, gi[d]), R[i2]);
-    work[d * rs + pad(i2)] = v;
+    uint32_t* slot = work + d * rs + pad(i2);
+    *slot = mmul<F>(mmul<F>(*slot, gi[d]), R[i2]);
   }
   __syncthreads();
   smem_ntt_dif<F>(work, log_ti, log_k2, rs, tw);
@@ -282,6 +301,13 @@ __device__ void lde_pass2_body(const uint32_t* z, uint32_t* out, int log_k1, int
   uint32_t* lo = tw + (k1 > 1 ? k1 / 2 : 1);
   uint32_t* hi = lo + TT * lo_n;
   const int t2_0 = tile * TT;
+  const uint32_t* zc_ = z + (c << log_n);
+  for (int idx = threadIdx.x; idx < (1 << (log_rows + log_k1)); idx += blockDim.x) {
+    const int i1 = idx & (k1 - 1), row = idx >> log_k1;
+    const int s = row >> log_tt, dt = row & (TT - 1);
+    cp_async4(work + row * rs + pad(i1),
+              zc_ + ((int64_t)s << log_k) + ((int64_t)(t2_0 + dt) << log_k1) + i1);
+  }
   pow_table<F>(tw, k1 > 1 ? k1 / 2 : 1, log_k1 ? omega_pow<F>(log_k1, 1) : F::ONE);
   for (int e = threadIdx.x; e < TT * (lo_n + hi_n); e += blockDim.x) {
     const int dt = e / (lo_n + hi_n), r = e - dt * (lo_n + hi_n);
@@ -292,13 +318,13 @@ __device__ void lde_pass2_body(const uint32_t* z, uint32_t* out, int log_k1, int
       hi[dt * hi_n + (r - lo_n)] = mpow<F>(base, (uint64_t)(r - lo_n) << kTwLoLog);
   }
   __syncthreads();
-  const uint32_t* zc_ = z + (c << log_n);
+  cp_async_wait_all();
   for (int idx = threadIdx.x; idx < (1 << (log_rows + log_k1)); idx += blockDim.x) {
     const int i1 = idx & (k1 - 1), row = idx >> log_k1;
-    const int s = row >> log_tt, dt = row & (TT - 1);
-    uint32_t v = zc_[((int64_t)s << log_k) + ((int64_t)(t2_0 + dt) << log_k1) + i1];
-    v = mmul<F>(v, mmul<F>(lo[dt * lo_n + (i1 & (lo_n - 1))], hi[dt * hi_n + (i1 >> kTwLoLog)]));
-    work[row * rs + pad(i1)] = v;
+    const int dt = row & (TT - 1);
+    uint32_t* slot = work + row * rs + pad(i1);
+    *slot = mmul<F>(*slot,
+                    mmul<F>(lo[dt * lo_n + (i1 & (lo_n - 1))], hi[dt * hi_n + (i1 >> kTwLoLog)]));
   }
   __syncthreads();
   smem_ntt_dif<F>(work, log_rows, log_k1, rs, tw);
