@@ -653,3 +653,78 @@ def basefold_open(p2: Poseidon2, field: int, mats, z, log_blowup: int, shift_mon
             "fri_roots": np.stack(roots) if roots else np.zeros((0, 8), np.uint32),
             "betas": np.array(betas, np.uint32), "final_poly": final, "positions": positions,
             "component_openings": comp, "query_openings": queries, "final_claim": claim}
+
+
+def sp1_stacked_open(p2: Poseidon2, field: int, blocks, z_final, dense_eval, log_s: int,
+                     log_blowup: int, num_queries: int, t: "Transcript") -> dict:
+    """stacked_basefold_open (zorch/pcs/jagged/open.py:362-460; prologue
+    :185-229, fold zone :237-330, queries :333-359) with pow_bits = 0: batch
+    evaluations at the stacking point, dense_eval and evaluations observed,
+    ceil(log2 total width) EF4 challenges (4 squeezes each) -> partial-Lagrange
+    weights, the batched MLE re-encoded bit-reversed, the round count observed
+    (base), per round message (s(0), s(1)) -> SMCS commit of the [n/2, 8] rows
+    -> observe message, bound root -> EF4 beta -> folds; final poly =
+    codeword[0] observed; grind(0) = observe the zero witness, squeeze once;
+    SP1 positions; openings. blocks: per round [K, S] Montgomery columns."""
+    v = log_s
+    S = 1 << v
+    n = S << log_blowup
+    zs = u32(z_final).reshape(-1, 4)[-v:]
+    blocks = [u32(b) for b in blocks]
+    evals = [eval_mle_base(field, b, zs) for b in blocks]
+    t.observe(u32(dense_eval).reshape(-1))
+    for e in evals:
+        t.observe(e.reshape(-1))
+    total = sum(b.shape[0] for b in blocks)
+    nbv = (total - 1).bit_length() if total > 1 else 0
+    chal = np.zeros((max(nbv, 1), 4), np.uint32)
+    if nbv:
+        chal[:nbv] = t.sample(4 * nbv).reshape(nbv, 4)
+    mle = np.zeros((S, 4), np.uint32)
+    off = 0
+    for b in blocks:
+        LIB.orc_rlc_columns_ex(field, b.reshape(-1), S, b.shape[0], chal.reshape(-1), nbv, off,
+                               int(off > 0), mle.reshape(-1))
+        off += b.shape[0]
+    wt = eq_expand(field, chal[:nbv])
+    claim = np.zeros(4, np.uint32)
+    for c, val in enumerate(np.concatenate(evals)):
+        claim = ef4_add(field, claim, ef4_mul(field, wt[c], val))
+    cw = rs_encode_bitrev(field, mle.T.copy(), log_blowup).T.copy()  # [n, 4], limb by limb
+    t.observe(to_mont(field, [v]))
+    msgs, raw, bound, betas, layers = [], [], [], [], []
+    for i in range(v):
+        rest = zs[: v - i - 1]
+        s0 = eval_mle_ef4(field, mle[0::2], rest)
+        s1 = ef4_add(field, ef4_mul(field, ef4_sub(field, claim, s0), ef4_inv(field, zs[v - 1 - i])),
+                     s0)
+        N = cw.shape[0]
+        leaves = cw.reshape(N // 2, 8)
+        dl = merkle_commit_rows(p2, leaves)
+        b_root = smcs_bind_root(p2, dl[-1][0], (N // 2).bit_length() - 1, 8)
+        msg = np.concatenate([s0, s1])
+        t.observe(msg)
+        t.observe(b_root)
+        beta = t.sample(4)
+        msgs.append(msg)
+        raw.append(dl[-1][0])
+        bound.append(b_root)
+        betas.append(beta)
+        layers.append((leaves, dl))
+        cw = fri_fold_bitrev(field, cw, True, beta, True)
+        mle = mle_fold(field, mle, beta)
+        claim = ef4_add(field, s0, ef4_mul(field, beta, s1))
+    final = cw[0].copy()
+    t.observe(final)
+    t.observe(np.zeros(1, np.uint32))  # grind(0): the canonical-zero witness
+    t.sample(1)
+    raw_q = t.sample(num_queries)
+    positions = sp1_query_positions(from_mont(field, raw_q), n)
+    queries = []
+    for i, (leaves, dl) in enumerate(layers):
+        a = (positions >> (i + 1)).astype(np.int32)
+        queries.append(merkle_open(leaves, leaves.shape[0], 1, 8, 0, dl, a))
+    return {"batch_evals": evals, "uni_msgs": np.stack(msgs), "raw_roots": np.stack(raw),
+            "bound_roots": np.stack(bound), "betas": np.stack(betas), "final_poly": final,
+            "final_codeword": cw, "final_claim": claim, "positions": positions,
+            "query_openings": queries}

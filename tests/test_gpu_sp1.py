@@ -229,3 +229,49 @@ def test_sp1_query_positions_use_canonical_bits(orc, sp1):
     raw = ot.sample(52)
     assert np.array_equal(to_host(pos).astype(np.uint32),
                           orc.from_mont(1, raw) & np.uint32((1 << 20) - 1))
+
+
+@pytest.mark.parametrize("widths,v,log_blowup,queries", [((3, 2), 6, 2, 5), ((1,), 10, 2, 16),
+                                                        ((7, 1, 4), 9, 1, 8)])
+def test_stacked_open_matches_oracle(orc, sp1, widths, v, log_blowup, queries):
+    """The whole stacked open (zorch/pcs/jagged/open.py:362-460) on the GPU ==
+    the oracle's restatement, field for field, and the folded codeword is the
+    constant encoding of the reduced claim."""
+    from zorch_gb300.coding import BitReversedReedSolomon
+    from zorch_gb300.commit import SingleMatrixCommitmentScheme
+    from zorch_gb300.jagged import stacked_basefold_open, stacked_commit
+    from zorch_gb300.transcript import DuplexTranscript
+
+    gperm, cperm = sp1
+    S = 1 << v
+    code = BitReversedReedSolomon(S, 1 << log_blowup, KOALABEAR)
+    smcs = SingleMatrixCommitmentScheme(gperm)
+    blocks = [rand_mont(orc, 1, (w, S), 60 + 3 * i + v) for i, w in enumerate(widths)]
+    rounds = [stacked_commit(smcs, code, dev(b).reshape(b.shape)) for b in blocks]
+    z = rand_mont(orc, 1, (v + 2, 4), 70 + v)
+    de = rand_mont(orc, 1, 4, 71 + v)
+    proof, _ = stacked_basefold_open(smcs, code, rounds, dev(z).reshape(v + 2, 4), dev(de), v,
+                                     num_queries=queries, pow_bits=0,
+                                     transcript=DuplexTranscript.new(gperm))
+    want = orc.sp1_stacked_open(cperm, 1, blocks, z, de, v, log_blowup, queries,
+                                orc.Transcript(cperm))
+    for got, w in zip(proof.batch_evals, want["batch_evals"]):
+        assert np.array_equal(to_host(got), w)
+    assert np.array_equal(to_host(proof.univariate_messages).reshape(v, 8), want["uni_msgs"])
+    assert np.array_equal(to_host(proof.fri_raw_roots), want["raw_roots"])
+    assert np.array_equal(to_host(proof.fri_commitments), want["bound_roots"])
+    assert np.array_equal(to_host(proof.final_poly), want["final_poly"])
+    assert np.array_equal(to_host(proof.positions), want["positions"].astype(np.uint32))
+    for (rows, paths), (wr, wp) in zip(proof.query_openings, want["query_openings"]):
+        assert np.array_equal(to_host(rows), wr) and np.array_equal(to_host(paths), wp)
+    n = S << log_blowup
+    for rd, b, (rows, paths), com in zip(rounds, blocks, proof.component_openings,
+                                         proof.component_commitments):
+        cw = orc.rs_encode_bitrev(1, b, log_blowup)
+        layers = orc.merkle_commit_columns(cperm, cw)
+        wr, wp = orc.merkle_open(cw, n, b.shape[0], 1, n, layers, want["positions"])
+        assert np.array_equal(to_host(rows), wr) and np.array_equal(to_host(paths), wp)
+        assert np.array_equal(to_host(com),
+                              orc.smcs_bind_root(cperm, layers[-1][0], n.bit_length() - 1,
+                                                 b.shape[0]))
+    assert all(np.array_equal(x, want["final_claim"]) for x in want["final_codeword"])

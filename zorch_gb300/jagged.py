@@ -1,5 +1,6 @@
-"""The commit-and-fold half of SP1's stacked BaseFold open on the GPU
-(drop-in for the fold loop and query openings of zorch/pcs/jagged/open.py:237-330).
+"""SP1's stacked BaseFold open on the GPU (drop-in for
+zorch/pcs/jagged/open.py): the commit of a stacked region, the commit-and-fold
+rounds, and the whole open with its interleaved sumcheck.
 
 Each round's layer is a bit-reversed EF4 codeword [n, 4]; it is committed as
 its [n/2, 8] base-limb rows (the adjacent conjugate pair of a fold is one row)
@@ -7,9 +8,10 @@ through the SP1 single-matrix commitment, whose separator-bound root the
 transcript observes, and folded by BitReversedReedSolomon.fold. Round r+1's
 commit runs in the same kernel as round r's fold (zc_fri_fold_commit_bitrev),
 and every root is bound on the device, so the loop never synchronises with
-the host. The interleaved sumcheck message of the reference loop (:266-276) is
-not on this path: the caller supplies each round's beta (the reference's
-byte-match replays them the same way, zorch/pcs/jagged/testing/open_test.py:90-128).
+the host. `StackedFoldCommit.run` takes each round's beta from the caller (the
+reference's byte-match replays them the same way,
+zorch/pcs/jagged/testing/open_test.py:90-128); `stacked_basefold_open` derives
+them from the transcript after the round's sumcheck message (:266-290).
 """
 
 from __future__ import annotations
@@ -17,12 +19,13 @@ from __future__ import annotations
 from dataclasses import dataclass
 from typing import Callable, Sequence
 
+import numpy as np
 import torch
 
 from . import _lib
 from .coding import BitReversedReedSolomon
 from .commit import DigestLayers, SingleMatrixCommitmentScheme, leaves_layout
-from .field import from_mont, ptr, stream_handle
+from .field import from_mont, ptr, stream_handle, to_host
 from .transcript import DuplexTranscript
 
 
@@ -116,3 +119,171 @@ class StackedFoldCommit:
         idx = self.code.layer_positions(positions.to(torch.int32), len(layers))
         return [self.smcs.open_batch(i, layer.leaves, layer.digest_layers)
                 for i, layer in zip(idx, layers)]
+
+
+# ------------------------------------------------------------ stacked open --
+@dataclass
+class StackedRound:
+    """One committed region (zorch/pcs/jagged/open.py:64-82): the [K, S]
+    message block (Montgomery words), its bit-reversed codeword [K, n], the
+    digest layers of its column-major SMCS commit and the bound commitment."""
+
+    block: torch.Tensor
+    codeword: torch.Tensor
+    digest_layers: DigestLayers
+    commitment: torch.Tensor
+
+
+def stacked_commit(smcs: SingleMatrixCommitmentScheme, code: BitReversedReedSolomon,
+                   block: torch.Tensor) -> StackedRound:
+    """Encode the [K, S] block bit-reversed and commit its codeword columns
+    (a leaf is a codeword position across the K columns)."""
+    cw = code.encode(block)
+    commitment, layers = smcs.commit(cw, column_major=True)
+    return StackedRound(block, cw, layers, commitment)
+
+
+@dataclass
+class StackedOpenProof:
+    """zorch/pcs/jagged/open.py:128-176: per round the bound component
+    commitment, the fold layers' raw and bound roots, the sumcheck messages
+    (s(0), s(1)), the final poly (codeword[0]), the proof-of-work witness, the
+    per-round column evaluations, and the component and fold-layer openings
+    (rows, sibling paths)."""
+
+    component_commitments: list
+    fri_raw_roots: torch.Tensor       # [v, 8]
+    fri_commitments: torch.Tensor     # [v, 8]
+    univariate_messages: torch.Tensor  # [v, 2, 4]
+    final_poly: torch.Tensor          # [4]
+    pow_witness: torch.Tensor         # [1]
+    batch_evals: list                 # per round [K, 4]
+    component_openings: list          # per round (rows [Q, K], paths [depth, Q, 8])
+    query_openings: list              # per layer (rows [Q, 8], paths [depth_i, Q, 8])
+    positions: torch.Tensor           # [Q]
+
+
+def _ef4_encode(code: BitReversedReedSolomon, mle: torch.Tensor) -> torch.Tensor:
+    """Bit-reversed encode of an EF4 message [S, 4] limb by limb (the base-field
+    roots act on each coefficient) -> [n, 4]."""
+    limbs = mle.movedim(-1, 0).contiguous()  # [4, S]
+    return code.encode(limbs).movedim(0, -1).contiguous()
+
+
+def stacked_basefold_open(smcs: SingleMatrixCommitmentScheme, code: BitReversedReedSolomon,
+                          rounds, z_final: torch.Tensor, dense_eval: torch.Tensor,
+                          log_stacking_height: int, *, num_queries: int, pow_bits: int,
+                          transcript: DuplexTranscript):
+    """The stacked BaseFold open (zorch/pcs/jagged/open.py:362-460: prologue
+    :185-229, fold zone :237-330, component queries :333-359) on the GPU:
+    evaluate every round's columns at the stacking point, observe dense_eval and
+    the evaluations, batch the rounds with partial-Lagrange weights over
+    ceil(log2 total width) EF4 challenges, re-encode the batched MLE, observe the
+    round count, then per round: sumcheck message, SMCS commit of the
+    pre-fold [n/2, 8] rows, observe message and bound root, EF4 beta, fold the
+    codeword, MLE and claim; observe the final poly, grind, draw SP1 query
+    positions and open every fold layer and every committed round."""
+    from .field import from_mont_np
+
+    if not rounds:
+        raise ValueError("the stacked open needs at least one committed round")
+    if log_stacking_height < 1:
+        raise ValueError(f"need at least one stacking variable, got "
+                         f"log_stacking_height={log_stacking_height}")
+    if z_final.shape[0] < log_stacking_height:
+        raise ValueError(f"z_final has {z_final.shape[0]} coordinates, fewer than "
+                         f"log_stacking_height={log_stacking_height}")
+    S = 1 << log_stacking_height
+    if code.message_len != S:
+        raise ValueError(f"code message_len {code.message_len} != stacking height {S}")
+    if any(rd.block.shape[1] != S for rd in rounds):
+        raise ValueError(f"every round block must stack to height {S}")
+    if pow_bits != 0:
+        raise NotImplementedError("only pow_bits = 0 (the canonical-zero witness) is built")
+    f, L, st = code.field, _lib.lib(), stream_handle()
+    dev = z_final.device
+    v = log_stacking_height
+    n = code.block_len
+    zs = z_final[-v:].contiguous()
+    t = transcript._copy()
+    # prologue: per-round evaluations at the stacking point
+    batch_evals = []
+    for rd in rounds:
+        K = rd.block.shape[0]
+        out = torch.empty((K, 4), dtype=torch.int32, device=dev)
+        nb = L.zc_eval_mle_workspace_bytes(K, v)
+        ws = torch.empty((nb + 15) // 4, dtype=torch.int32, device=dev)
+        _lib.check(L.zc_eval_mle(f.id, ptr(rd.block.contiguous()), K, v, ptr(zs), ptr(out),
+                                 ptr(ws), nb, st), "eval_mle")
+        batch_evals.append(out)
+    t.observe_(dense_eval.reshape(-1))
+    for e in batch_evals:
+        t.observe_(e.reshape(-1))
+    total = sum(int(rd.block.shape[0]) for rd in rounds)
+    nbv = (total - 1).bit_length() if total > 1 else 0
+    chal = torch.zeros((max(nbv, 1), 4), dtype=torch.int32, device=dev)
+    if nbv:
+        chal[:nbv] = t.sample_(4 * nbv).reshape(nbv, 4)
+    mle = torch.empty((S, 4), dtype=torch.int32, device=dev)
+    claim = torch.empty(4, dtype=torch.int32, device=dev)
+    off = 0
+    for rd, e in zip(rounds, batch_evals):
+        K = rd.block.shape[0]
+        acc = int(off > 0)
+        _lib.check(L.zc_rlc_columns_ex(f.id, ptr(rd.block.contiguous()), S, K, ptr(chal), nbv,
+                                       off, acc, ptr(mle), st), "rlc mle")
+        _lib.check(L.zc_rlc_values(f.id, ptr(e), K, ptr(chal), nbv, off, acc, ptr(claim), st),
+                   "rlc values")
+        off += K
+    # fold zone
+    cw = _ef4_encode(code, mle)
+    t.observe_(torch.tensor([f.mont(v)], dtype=torch.int32, device=dev))
+    zh = from_mont_np(f, to_host(zs))
+    zinv = torch.tensor(np.array([f.ef_to_mont(f.ef_inv(tuple(int(x) for x in row)))
+                                  for row in zh], np.uint32).view(np.int32), device=dev)
+    eq = torch.empty((max(S // 2, 1), 4), dtype=torch.int32, device=dev)
+    nb = L.zc_eq_expand_workspace_bytes(v - 1)
+    ews = torch.empty(max((nb + 15) // 4, 4), dtype=torch.int32, device=dev)
+    _lib.check(L.zc_eq_expand(f.id, ptr(zs), v - 1, ptr(eq), ptr(ews), nb, st), "eq_expand")
+    scb = L.zc_sumcheck_workspace_bytes()
+    scws = torch.empty(scb // 4, dtype=torch.int32, device=dev)
+    msgs = torch.empty((v, 8), dtype=torch.int32, device=dev)
+    fold = StackedFoldCommit(smcs, code)
+    layers: list[StackedFoldLayer] = []
+    pending = None
+    for i in range(v):
+        M = S >> (i + 1)
+        _lib.check(L.zc_sumcheck_message(f.id, ptr(mle), M, ptr(eq), ptr(claim),
+                                         ptr(zinv[v - 1 - i]), ptr(msgs[i]), ptr(scws), scb, st),
+                   "sumcheck_message")
+        layer = pending if pending is not None else fold.commit_layer(cw)
+        t.observe_(msgs[i])
+        beta = t.observe_and_sample_(layer.bound_root, 4)
+        cw_next, pending = fold.fold_commit(cw, beta, code.level_of(cw.shape[0]))
+        mle_next = torch.empty((M, 4), dtype=torch.int32, device=dev)
+        eq_next = torch.empty((M // 2, 4), dtype=torch.int32, device=dev) if M >= 2 else None
+        _lib.check(L.zc_sumcheck_fold(f.id, ptr(mle), M, ptr(beta), 4, ptr(msgs[i]),
+                                      ptr(mle_next), ptr(eq) if eq_next is not None else None,
+                                      ptr(eq_next) if eq_next is not None else None, ptr(claim),
+                                      st), "sumcheck_fold")
+        layers.append(layer)
+        mle, eq, cw = mle_next, eq_next, cw_next
+    final_poly = cw[0].contiguous()
+    t.observe_(final_poly)
+    witness = torch.zeros(1, dtype=torch.int32, device=dev)  # grind(0): canonical zero
+    t.observe_(witness)
+    t.sample_(1)
+    t, positions = sample_query_positions(t, n, num_queries)
+    positions = positions.to(torch.int32)
+    query_openings = fold.open_layers(layers, positions)
+    component_openings = []
+    for rd in rounds:
+        K = rd.codeword.shape[0]
+        op = smcs._tree.open_layout(leaves_layout(rd.codeword, n, K, 1, n), rd.digest_layers,
+                                    positions, K, check=False)
+        component_openings.append((op.row, op.path))
+    proof = StackedOpenProof(
+        [rd.commitment for rd in rounds], torch.stack([ly.raw_root for ly in layers]),
+        torch.stack([ly.bound_root for ly in layers]), msgs.reshape(v, 2, 4), final_poly,
+        witness, batch_evals, component_openings, query_openings, positions)
+    return proof, t
