@@ -85,6 +85,12 @@ zc_status zc_from_mont(zc_field field, const uint32_t* in, uint32_t* out, int64_
 zc_status zc_scale(zc_field field, const uint32_t* in, uint32_t* out, int64_t n, uint32_t s_mont,
                    void* stream);
 
+/* The device address of a page-locked host buffer (cudaHostGetDevicePointer),
+ * so a kernel -- e.g. zc_to_mont -- reads host inputs directly over the host
+ * link instead of a staging copy: no counterpart in the reference (its
+ * inputs arrive as device arrays). ZC_BAD_ARG if `host` is not page-locked. */
+zc_status zc_host_device_ptr(const void* host, void** dev);
+
 /* ---- Poseidon2 parameters -------------------------------------------- */
 /* The built-in BabyBear width-16 instance (x^7, 4+4 full, 13 partial rounds).
  * The reference ships no BabyBear instance; see gen_poseidon2_babybear16.py. */
@@ -332,6 +338,16 @@ zc_status zc_duplex_hop_host(const zc_poseidon2* p, const uint32_t* in_buf,
                              const uint32_t* values, int64_t m, int32_t n,
                              uint32_t* in_buf_o, uint32_t* out_buf_o, uint32_t* sponge_o,
                              uint32_t* in_pos_o, uint32_t* out_pos_o, uint32_t* challenges);
+/* Proof-of-work grind (DuplexTranscript.grind / _grind_search,
+ * zorch/transcript.py:439-481; grind_search, zorch/grind.py:66-93) on the
+ * packed 34-word device state: writes to `witness` (one device word) the
+ * lowest witness w in [0, p), as a Montgomery field element, whose challenge
+ * -- observe w, sample once -- has pow_bits zero low canonical bits
+ * (_pow_satisfied, :44-49); 0 when none passes (the reference's unchecked
+ * fallback). pow_bits in [0, 32) else ZC_BAD_ARG. The state is read, not
+ * advanced: observe the witness and sample once, as check_witness does. */
+zc_status zc_duplex_grind(const zc_poseidon2* p, const uint32_t* state, int32_t pow_bits,
+                          uint32_t* witness, void* stream);
 /* Device-resident transcript step on a packed 34-word state: observe m values
  * then squeeze n words into `out`; if positions != NULL also write
  * positions[i] = out[i] mod block_len (sample_positions, zorch/pcs/fold.py:173-182). */

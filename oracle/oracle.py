@@ -78,6 +78,7 @@ def _load() -> C.CDLL:
         "orc_duplex_init": (None, [vp]),
         "orc_duplex_observe": (None, [vp, vp, _u32p, i64]),
         "orc_duplex_sample": (None, [vp, vp, i32, _u32p]),
+        "orc_duplex_grind": (u32, [vp, vp, i32]),
         "orc_rlc_columns": (None, [i32, _u32p, i64, i32, _u32p, _u32p]),
         "orc_fri_commit_phase": (i32, [vp, i32, _u32p, i32, i32, u32, u32, i32, i32, i32, vp,
                                        _u32p, _u32p, _u32p, _i32p, _u32p, _u32p]),
@@ -438,6 +439,26 @@ class Transcript:
         out = np.zeros(max(n, 1), np.uint32)
         LIB.orc_duplex_sample(self.p2.ptr, C.byref(self.st), n, out)
         return out[:n]
+
+    def copy(self) -> "Transcript":
+        t = Transcript(self.p2)
+        t.st = Duplex.from_buffer_copy(self.st)
+        return t
+
+    def grind(self, pow_bits: int) -> int:
+        """Lowest canonical proof-of-work witness (zorch/transcript.py:439-481);
+        the transcript is not advanced (observe the witness and sample once,
+        as check_witness does)."""
+        if not 0 <= pow_bits < 32:
+            raise ValueError(f"pow_bits must be in [0, 32), got {pow_bits}")
+        return int(LIB.orc_duplex_grind(self.p2.ptr, C.byref(self.st), pow_bits))
+
+    def check_witness(self, witness_mont: int, pow_bits: int) -> bool:
+        """Observe the witness (Montgomery word), sample once, test the low
+        `pow_bits` canonical bits (zorch/transcript.py:417-437)."""
+        self.observe([witness_mont])
+        s = int(self.sample(1)[0])
+        return (from_mont(self.p2.field, [s])[0] & ((1 << pow_bits) - 1)) == 0
 
 
 # ------------------------------------------------------- FRI commit phase --

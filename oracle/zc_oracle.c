@@ -883,6 +883,27 @@ void orc_duplex_sample(const orc_p2* P, orc_duplex* t, int n, uint32_t* out) {
   }
 }
 
+/* Proof-of-work grind (DuplexTranscript._grind_search / grind,
+ * zorch/transcript.py:439-481, over grind_search, zorch/grind.py:66-93):
+ * the lowest canonical witness w in [0, p) whose challenge -- observe w as a
+ * field element, sample once -- has `pow_bits` zero low canonical bits
+ * (_pow_satisfied, zorch/transcript.py:44-49). 0 when none passes (the
+ * unchecked fallback). Each candidate replays the transcript literally: copy,
+ * observe, sample. */
+uint32_t orc_duplex_grind(const orc_p2* P, const orc_duplex* t, int pow_bits) {
+  const uint32_t mask = (uint32_t)((1ull << pow_bits) - 1);
+  const uint32_t mod = orc_modulus(P->field);
+  for (uint32_t w = 0; w < mod; w++) {
+    orc_duplex c = *t;
+    const uint32_t v = orc_to_mont(P->field, w);
+    uint32_t s;
+    orc_duplex_observe(P, &c, &v, 1);
+    orc_duplex_sample(P, &c, 1, &s);
+    if ((orc_from_mont(P->field, s) & mask) == 0) return w;
+  }
+  return 0;
+}
+
 /* --------------------------------------------------- FRI commit phase ---- */
 /* fold_rounds(PreFoldPairCommitRound) (zorch/prove.py:26-37,
  * zorch/pcs/fold.py:90-115) over the codeword, each round: pair_leaves

@@ -137,6 +137,8 @@ void orc_rlc_columns_ex(int field, const uint32_t* cw, int64_t n, int w, const u
 void orc_duplex_init(orc_duplex* t);
 void orc_duplex_observe(const orc_p2* p, orc_duplex* t, const uint32_t* v, int64_t m);
 void orc_duplex_sample(const orc_p2* p, orc_duplex* t, int n, uint32_t* out);
+/* lowest canonical proof-of-work witness (0 when none) */
+uint32_t orc_duplex_grind(const orc_p2* p, const orc_duplex* t, int pow_bits);
 
 /* FRI / Basefold commit phase (pre-fold pair commit rounds, then queries). */
 void orc_rlc_columns(int field, const uint32_t* cw, int64_t n, int w, const uint32_t* alpha,

@@ -401,3 +401,17 @@ def test_graphed_fri_commit_phase_equals_eager(orc, perms):
         got = g.replay(coeffs).to_bytes()
         eager, _, _ = prover.commit_phase(code.encode(coeffs), DuplexTranscript.new(gpu))
         assert got == eager.to_bytes()
+
+
+def test_to_mont_reads_pinned_host_memory(orc):
+    """zc_host_device_ptr + zc_to_mont convert a page-locked host buffer in one
+    kernel reading over the host link, equal to the device conversion; a
+    pageable buffer is refused."""
+    from zorch_gb300.field import to_mont, to_mont_from_host
+
+    x = np.random.default_rng(4).integers(0, orc.P_BABYBEAR, size=(3, 1001), dtype=np.uint64)
+    host = torch.from_numpy(x.astype(np.uint32).view(np.int32))
+    got = to_mont_from_host(BABYBEAR, host.pin_memory())
+    assert torch.equal(got, to_mont(BABYBEAR, host.cuda()))
+    with pytest.raises(ValueError):
+        to_mont_from_host(BABYBEAR, host)

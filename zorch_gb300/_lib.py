@@ -57,6 +57,7 @@ def _declare(lib: C.CDLL) -> None:
         "zc_launch_count": (C.c_ulonglong, []),
         "zc_init": (st, [C.c_int]),
         "zc_to_mont": (st, [st, vp, vp, i64, vp]),
+        "zc_host_device_ptr": (st, [vp, C.POINTER(vp)]),
         "zc_from_mont": (st, [st, vp, vp, i64, vp]),
         "zc_scale": (st, [st, vp, vp, i64, u32, vp]),
         "zc_poseidon2_builtin": (st, [st, C.POINTER(vp)]),
@@ -91,6 +92,7 @@ def _declare(lib: C.CDLL) -> None:
         "zc_duplex_hop": (st, [vp, vp, vp, vp, vp, vp, vp, i64, i32, vp, vp, vp, vp, vp, vp, vp]),
         "zc_duplex_hop_host": (st, [vp, vp, vp, vp, vp, vp, vp, i64, i32, vp, vp, vp, vp, vp, vp]),
         "zc_duplex_step": (st, [vp, vp, vp, i64, i32, vp, vp, i64, vp]),
+        "zc_duplex_grind": (st, [vp, vp, i32, vp, vp]),
         "zc_rlc_columns": (st, [st, vp, i64, i32, vp, vp, vp]),
         "zc_fill_uniform": (st, [st, vp, i64, C.c_uint64, vp]),
         "zc_rs_encode_batch_workspace_bytes": (sz, [vp, i32]),

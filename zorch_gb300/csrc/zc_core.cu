@@ -3,6 +3,7 @@
 #include <stdio.h>
 #include <string.h>
 
+#include <algorithm>
 #include <atomic>
 #include <mutex>
 
@@ -194,8 +195,24 @@ __global__ void __launch_bounds__(32) k_duplex_hop(
 
 template <class F>
 __global__ void k_convert(const uint32_t* in, uint32_t* out, int64_t n, int to) {
-  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
-       i += (int64_t)gridDim.x * blockDim.x)
+  // 16-byte accesses when both sides are aligned (more bytes in flight per
+  // thread, which a read of page-locked host memory over the host link needs)
+  const int64_t tid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  int64_t head = 0;
+  if (((uintptr_t)in % 16) == 0 && ((uintptr_t)out % 16) == 0) {
+    const int64_t n4 = n >> 2;
+    const uint4* in4 = reinterpret_cast<const uint4*>(in);
+    uint4* out4 = reinterpret_cast<uint4*>(out);
+    for (int64_t i = tid; i < n4; i += stride) {
+      const uint4 v = in4[i];
+      out4[i] = to ? make_uint4(to_mont<F>(v.x), to_mont<F>(v.y), to_mont<F>(v.z), to_mont<F>(v.w))
+                   : make_uint4(from_mont<F>(v.x), from_mont<F>(v.y), from_mont<F>(v.z),
+                                from_mont<F>(v.w));
+    }
+    head = n4 << 2;
+  }
+  for (int64_t i = head + tid; i < n; i += stride)
     out[i] = to ? to_mont<F>(in[i]) : from_mont<F>(in[i]);
 }
 
@@ -216,6 +233,51 @@ __global__ void k_permute(const P2Params* rt, uint32_t* states, int64_t count) {
   for (int j = 0; j < 16; j++) s[j] = states[i * 16 + j];
   p2_permute(s, k);
   for (int j = 0; j < 16; j++) states[i * 16 + j] = s[j];
+}
+
+// ------------------------------------------------------------- grind ------
+// Proof-of-work search (DuplexTranscript._grind_search, zorch/transcript.py:
+// 439-459, over grind_search, zorch/grind.py:66-93): the lowest witness w in
+// [0, p) whose challenge -- observe w as a field element, sample once -- has
+// `mask` clear in its canonical value. Observing one word and sampling once
+// is always exactly one permutation: of the sponge with the pending prefix
+// in_buf[0:in_pos] and then w written over its front, and the challenge is
+// lane 7 of the result (a completed block is absorbed and lane 7 popped; a
+// partial one is duplexed and lane 7 popped). One thread per candidate on a
+// persistent grid: thread i tries i, i + S, i + 2S, ... and stops once its
+// candidate exceeds the best hit so far, so every witness below the final
+// minimum is tried and the result is the same for every grid size.
+constexpr int kGrindT = 256;
+
+template <class K>
+__global__ void __launch_bounds__(kGrindT) k_grind(const P2Params* rt, const uint32_t* state,
+                                                  uint32_t mask, uint32_t* best) {
+  using F = typename K::F;
+  __shared__ P2Params s_rt;
+  K k = KIn<K>::make(rt, &s_rt);
+  const Duplex* t = reinterpret_cast<const Duplex*>(state);
+  const int in_pos = t->in_pos & 7;
+  uint32_t base[16];
+#pragma unroll
+  for (int j = 0; j < 16; j++) base[j] = (j < 8 && j < in_pos) ? t->in_buf[j] : t->sponge[j];
+  const uint32_t stride = gridDim.x * blockDim.x;
+  const volatile uint32_t* vbest = best;
+  for (uint32_t c = blockIdx.x * blockDim.x + threadIdx.x; c < F::P; c += stride) {
+    if (c > *vbest) break;
+    const uint32_t w = to_mont<F>(c);
+    uint32_t s[16];
+#pragma unroll
+    for (int j = 0; j < 16; j++) s[j] = j == in_pos ? w : base[j];
+    p2_permute(s, k);
+    if ((from_mont<F>(s[7]) & mask) == 0) atomicMin(best, c);
+  }
+}
+
+// The witness as a field element (Montgomery), 0 when no candidate passed.
+template <class F>
+__global__ void k_grind_finish(uint32_t* best) {
+  const uint32_t c = best[0];
+  best[0] = c == 0xffffffffu ? 0u : to_mont<F>(c);
 }
 
 }  // namespace zc
@@ -368,6 +430,21 @@ static zc_status convert(zc_field field, const uint32_t* in, uint32_t* out, int6
   });
 }
 
+zc_status zc_host_device_ptr(const void* host, void** dev) {
+  if (!host || !dev) return ZC_BAD_ARG;
+  cudaPointerAttributes a;
+  if (cudaPointerGetAttributes(&a, host) != cudaSuccess || a.type != cudaMemoryTypeHost) {
+    cudaGetLastError();  // clear the error the failed query recorded
+    set_error("not page-locked host memory");
+    return ZC_BAD_ARG;
+  }
+  void* d = nullptr;
+  const cudaError_t e = cudaHostGetDevicePointer(&d, const_cast<void*>(host), 0);
+  if (e != cudaSuccess) return cuda_fail(e);
+  *dev = d;
+  return ZC_OK;
+}
+
 zc_status zc_to_mont(zc_field field, const uint32_t* in, uint32_t* out, int64_t n, void* stream) {
   return convert(field, in, out, n, 1, stream);
 }
@@ -411,6 +488,33 @@ zc_status zc_duplex_step(const zc_poseidon2* p, uint32_t* state, const uint32_t*
   return with_perm(p, [&](auto k, const P2Params* rt) {
     using K = decltype(k);
     k_duplex_step<K><<<1, 32, 0, st>>>(rt, state, values, m, n, out, positions, block_len);
+    return launch_check();
+  });
+}
+
+zc_status zc_duplex_grind(const zc_poseidon2* p, const uint32_t* state, int32_t pow_bits,
+                          uint32_t* witness, void* stream) {
+  if (!p || !state || !witness) return ZC_BAD_ARG;
+  if (pow_bits < 0 || pow_bits >= 32) {
+    set_error("pow_bits must be in [0, 32)");
+    return ZC_BAD_ARG;
+  }
+  cudaStream_t st = (cudaStream_t)stream;
+  if (pow_bits == 0) {  // the canonical zero witness always passes
+    ZC_CUDA(cudaMemsetAsync(witness, 0, 4, st));
+    return ZC_OK;
+  }
+  ZC_CUDA(cudaMemsetAsync(witness, 0xff, 4, st));
+  // about two expected hits' worth of candidates per sweep, at most one full
+  // wave of resident threads (grind_window_for, zorch/grind.py:33-47)
+  const int64_t want = std::min<int64_t>(int64_t(1) << (pow_bits + 1), 152 * 2048);
+  const unsigned blocks = (unsigned)std::max<int64_t>(4, (want + kGrindT - 1) / kGrindT);
+  const uint32_t mask = (uint32_t)((1ull << pow_bits) - 1);
+  return with_perm(p, [&](auto k, const P2Params* rt) {
+    using K = decltype(k);
+    k_grind<K><<<blocks, kGrindT, 0, st>>>(rt, state, mask, witness);
+    ZC_TRY(launch_check());
+    k_grind_finish<typename K::F><<<1, 1, 0, st>>>(witness);
     return launch_check();
   });
 }

@@ -32,7 +32,7 @@ from . import _lib
 from .batch import BatchCommitter, MatrixJob
 from .coding import ReedSolomon
 from .commit import MerkleTree, Poseidon2, leaves_layout
-from .field import BABYBEAR, ptr, stream_handle, to_mont
+from .field import BABYBEAR, ptr, stream_handle, to_mont, to_mont_from_host
 from .pcs import FriParams, FriProver, pair_layout
 from .transcript import DuplexTranscript
 
@@ -221,9 +221,8 @@ class Server:
         with torch.cuda.stream(stream):
             jobs, keep = [], []
             for r in reqs:
-                if host_fed:
-                    x = r.host.to("cuda", non_blocking=True)
-                    to_mont(BABYBEAR, x, x)
+                if host_fed:  # read the pinned input over the host link
+                    x = to_mont_from_host(BABYBEAR, r.host)
                 else:
                     x = to_mont(BABYBEAR, r.resident)
                 jobs.append(MatrixJob(x, r.log_blowup, 31))
@@ -302,8 +301,7 @@ def run_plain(requests: list[Request], host_fed: bool = False,
         if r.arrival > now:
             time.sleep(r.arrival - now)
         if host_fed:
-            x = r.host.to("cuda")
-            to_mont(BABYBEAR, x, x)
+            x = to_mont_from_host(BABYBEAR, r.host)
         else:
             x = to_mont(BABYBEAR, r.resident)
         code = ReedSolomon(1 << r.log_h, 1 << r.log_blowup, BABYBEAR, coset_shift=31,

@@ -86,9 +86,41 @@ class DuplexTranscript:
         t = self._copy()
         return t, t.observe_and_sample_(values, n)
 
+    # -- proof of work (zorch/transcript.py:417-481) --
+    def check_witness(self, witness: torch.Tensor, *, pow_bits: int):
+        """Observe `witness` (one field element), squeeze one challenge and
+        report whether its low `pow_bits` canonical bits are zero; returns the
+        advanced transcript and a device bool (check_witness,
+        zorch/transcript.py:417-437)."""
+        _validate_pow_bits(pow_bits)
+        if witness.numel() != 1 or witness.dtype != torch.int32:
+            raise ValueError("witness must be one field element (int32 Montgomery word)")
+        t, ch = self.observe_and_sample(witness.reshape(1), 1)
+        canon = torch.empty_like(ch)
+        _lib.check(_lib.lib().zc_from_mont(self.field.id, ptr(ch), ptr(canon), 1,
+                                           stream_handle()), "from_mont")
+        return t, (canon & ((1 << pow_bits) - 1)) == 0
+
+    def grind(self, pow_bits: int) -> tuple["DuplexTranscript", torch.Tensor]:
+        """The lowest proof-of-work witness, searched on the device
+        (zc_duplex_grind), and the transcript advanced past it by
+        check_witness (DuplexTranscript.grind, zorch/transcript.py:461-481).
+        No host round trip: the witness stays a device word."""
+        _validate_pow_bits(pow_bits)
+        witness = torch.empty(1, dtype=torch.int32, device=self.state.device)
+        _lib.check(_lib.lib().zc_duplex_grind(self.permutation.handle, ptr(self.state), pow_bits,
+                                              ptr(witness), stream_handle()), "duplex_grind")
+        t, _ = self.check_witness(witness, pow_bits=pow_bits)
+        return t, witness.reshape(())
+
     def wire(self) -> tuple[torch.Tensor, ...]:
         s = self.state
         return s[0:8], s[8:16], s[16:32], s[32:33], s[33:34]
+
+
+def _validate_pow_bits(pow_bits: int) -> None:
+    if not 0 <= pow_bits < 32:
+        raise ValueError(f"pow_bits must be in [0, 32), got {pow_bits}")
 
 
 def sample_challenge(t: DuplexTranscript, limbs: int = 1):
@@ -135,3 +167,15 @@ class HostDuplexTranscript:
 
     def observe_and_sample(self, values, n: int = 1):
         return self.hop(values, n)
+
+    def check_witness(self, witness, *, pow_bits: int):
+        """The verifier's proof-of-work check on the host: observe the
+        witness (Montgomery word), squeeze once, test the low `pow_bits`
+        canonical bits (zorch/transcript.py:417-437)."""
+        _validate_pow_bits(pow_bits)
+        w = np.asarray(witness, np.uint32).reshape(-1)
+        if w.size != 1:
+            raise ValueError("witness must be one field element")
+        t, ch = self.hop(w, 1)
+        canon = self.permutation.field.canon(int(ch[0]))
+        return t, (canon & ((1 << pow_bits) - 1)) == 0
