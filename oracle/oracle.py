@@ -677,16 +677,17 @@ def basefold_open(p2: Poseidon2, field: int, mats, z, log_blowup: int, shift_mon
 
 
 def sp1_stacked_open(p2: Poseidon2, field: int, blocks, z_final, dense_eval, log_s: int,
-                     log_blowup: int, num_queries: int, t: "Transcript") -> dict:
+                     log_blowup: int, num_queries: int, t: "Transcript",
+                     pow_bits: int = 0) -> dict:
     """stacked_basefold_open (zorch/pcs/jagged/open.py:362-460; prologue
-    :185-229, fold zone :237-330, queries :333-359) with pow_bits = 0: batch
+    :185-229, fold zone :237-330, queries :333-359): batch
     evaluations at the stacking point, dense_eval and evaluations observed,
     ceil(log2 total width) EF4 challenges (4 squeezes each) -> partial-Lagrange
     weights, the batched MLE re-encoded bit-reversed, the round count observed
     (base), per round message (s(0), s(1)) -> SMCS commit of the [n/2, 8] rows
     -> observe message, bound root -> EF4 beta -> folds; final poly =
-    codeword[0] observed; grind(0) = observe the zero witness, squeeze once;
-    SP1 positions; openings. blocks: per round [K, S] Montgomery columns."""
+    codeword[0] observed; grind(pow_bits) = the lowest passing witness
+    observed, squeeze once (:304-307); SP1 positions; openings. blocks: per round [K, S] Montgomery columns."""
     v = log_s
     S = 1 << v
     n = S << log_blowup
@@ -737,7 +738,8 @@ def sp1_stacked_open(p2: Poseidon2, field: int, blocks, z_final, dense_eval, log
         claim = ef4_add(field, s0, ef4_mul(field, beta, s1))
     final = cw[0].copy()
     t.observe(final)
-    t.observe(np.zeros(1, np.uint32))  # grind(0): the canonical-zero witness
+    witness = to_mont(field, [t.grind(pow_bits)])
+    t.observe(witness)
     t.sample(1)
     raw_q = t.sample(num_queries)
     positions = sp1_query_positions(from_mont(field, raw_q), n)
@@ -748,4 +750,4 @@ def sp1_stacked_open(p2: Poseidon2, field: int, blocks, z_final, dense_eval, log
     return {"batch_evals": evals, "uni_msgs": np.stack(msgs), "raw_roots": np.stack(raw),
             "bound_roots": np.stack(bound), "betas": np.stack(betas), "final_poly": final,
             "final_codeword": cw, "final_claim": claim, "positions": positions,
-            "query_openings": queries}
+            "pow_witness": witness, "query_openings": queries}

@@ -231,9 +231,10 @@ def test_sp1_query_positions_use_canonical_bits(orc, sp1):
                           orc.from_mont(1, raw) & np.uint32((1 << 20) - 1))
 
 
-@pytest.mark.parametrize("widths,v,log_blowup,queries", [((3, 2), 6, 2, 5), ((1,), 10, 2, 16),
-                                                        ((7, 1, 4), 9, 1, 8)])
-def test_stacked_open_matches_oracle(orc, sp1, widths, v, log_blowup, queries):
+@pytest.mark.parametrize("widths,v,log_blowup,queries,pow_bits",
+                         [((3, 2), 6, 2, 5, 0), ((1,), 10, 2, 16, 0), ((7, 1, 4), 9, 1, 8, 0),
+                          ((2, 3), 7, 1, 6, 10)])
+def test_stacked_open_matches_oracle(orc, sp1, widths, v, log_blowup, queries, pow_bits):
     """The whole stacked open (zorch/pcs/jagged/open.py:362-460) on the GPU ==
     the oracle's restatement, field for field, and the folded codeword is the
     constant encoding of the reduced claim."""
@@ -251,10 +252,11 @@ def test_stacked_open_matches_oracle(orc, sp1, widths, v, log_blowup, queries):
     z = rand_mont(orc, 1, (v + 2, 4), 70 + v)
     de = rand_mont(orc, 1, 4, 71 + v)
     proof, _ = stacked_basefold_open(smcs, code, rounds, dev(z).reshape(v + 2, 4), dev(de), v,
-                                     num_queries=queries, pow_bits=0,
+                                     num_queries=queries, pow_bits=pow_bits,
                                      transcript=DuplexTranscript.new(gperm))
     want = orc.sp1_stacked_open(cperm, 1, blocks, z, de, v, log_blowup, queries,
-                                orc.Transcript(cperm))
+                                orc.Transcript(cperm), pow_bits)
+    assert np.array_equal(to_host(proof.pow_witness), want["pow_witness"])
     for got, w in zip(proof.batch_evals, want["batch_evals"]):
         assert np.array_equal(to_host(got), w)
     assert np.array_equal(to_host(proof.univariate_messages).reshape(v, 8), want["uni_msgs"])

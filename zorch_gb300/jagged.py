@@ -198,8 +198,6 @@ def stacked_basefold_open(smcs: SingleMatrixCommitmentScheme, code: BitReversedR
         raise ValueError(f"code message_len {code.message_len} != stacking height {S}")
     if any(rd.block.shape[1] != S for rd in rounds):
         raise ValueError(f"every round block must stack to height {S}")
-    if pow_bits != 0:
-        raise NotImplementedError("only pow_bits = 0 (the canonical-zero witness) is built")
     f, L, st = code.field, _lib.lib(), stream_handle()
     dev = z_final.device
     v = log_stacking_height
@@ -270,9 +268,8 @@ def stacked_basefold_open(smcs: SingleMatrixCommitmentScheme, code: BitReversedR
         mle, eq, cw = mle_next, eq_next, cw_next
     final_poly = cw[0].contiguous()
     t.observe_(final_poly)
-    witness = torch.zeros(1, dtype=torch.int32, device=dev)  # grind(0): canonical zero
-    t.observe_(witness)
-    t.sample_(1)
+    t, witness = t.grind(pow_bits)  # the query-phase proof of work (:304-307)
+    witness = witness.reshape(1)
     t, positions = sample_query_positions(t, n, num_queries)
     positions = positions.to(torch.int32)
     query_openings = fold.open_layers(layers, positions)
