@@ -56,6 +56,30 @@ ZC_HD uint32_t mmul(uint32_t a, uint32_t b) {
   return hi < mp ? r + F::P : r;
 }
 
+// Signed Montgomery product on (-p, p], values as int32: |a b - m p| <=
+// p^2 + 2^31 p < 2^32 p, so the result lies in (-p, p) and a chain of products
+// needs no correction step between them (snorm brings the last one back to
+// [0, p)). The low words of a b and m p are equal, so the high words differ by
+// exactly (a b - m p) / 2^32.
+template <class F>
+ZC_HD int32_t smul(int32_t a, int32_t b) {
+  const int64_t c = (int64_t)a * b;
+  const uint32_t m = (uint32_t)c * F::MU;
+#ifdef __CUDA_ARCH__
+  const int32_t mp = __mulhi((int32_t)m, (int32_t)F::P);
+#else
+  const int32_t mp = (int32_t)(((int64_t)(int32_t)m * (int64_t)F::P) >> 32);
+#endif
+  return (int32_t)(c >> 32) - mp;
+}
+
+// (-p, p) -> [0, p): the unsigned minimum of r and r + p.
+template <class F>
+ZC_HD uint32_t snorm(int32_t r) {
+  const uint32_t u = (uint32_t)r, v = u + F::P;
+  return u < v ? u : v;
+}
+
 template <class F>
 ZC_HD uint32_t madd(uint32_t a, uint32_t b) {
   uint32_t r = a + b;

@@ -36,6 +36,25 @@ static __constant__ uint32_t c_bb16_ext_term[64] = ZC_BB16_EXT_TERM_MONT_INIT;
 static __constant__ uint32_t c_bb16_int_rc[ZC_BB16_ROUNDS_P] = ZC_BB16_INT_RC_MONT_INIT;
 static __constant__ uint32_t c_bb16_diag[16] = ZC_BB16_DIAG_MONT_INIT;
 
+// Round-constant addition and S-box x -> (x + c)^alpha for x, c in [0, p):
+// x + c - p lies in [-p, p) and is one three-operand add, and the power chain
+// runs on signed Montgomery products (smul) with a single normalisation at
+// the end. Exponents other than 3, 5, 7 take the generic square-and-multiply.
+template <class F, int ALPHA>
+ZC_HD uint32_t ark_sbox_a(uint32_t x, uint32_t c, uint32_t alpha) {
+  const int32_t a = (int32_t)(x + c - F::P);
+  if (ALPHA == 3) return snorm<F>(smul<F>(smul<F>(a, a), a));
+  if (ALPHA == 5) {
+    const int32_t a2 = smul<F>(a, a);
+    return snorm<F>(smul<F>(smul<F>(a2, a2), a));
+  }
+  if (ALPHA == 7) {
+    const int32_t a2 = smul<F>(a, a);
+    return snorm<F>(smul<F>(smul<F>(a2, a), smul<F>(a2, a2)));
+  }
+  return mpow<F>(madd<F>(x, c), alpha);
+}
+
 // Multiplications by the built-in BabyBear diagonal entries without a
 // Montgomery product (the representation is linear, so a constant c acts on
 // Mont(x) as on x). p = 15 * 2^27 + 1, so for k <= 27 and q = (-x) mod 2^k,
@@ -92,11 +111,8 @@ struct Bb16Builtin {
   __device__ __forceinline__ uint32_t et(int r, int i) const { return c_bb16_ext_term[r * 16 + i]; }
   __device__ __forceinline__ uint32_t ir(int r) const { return c_bb16_int_rc[r]; }
   __device__ __forceinline__ uint32_t dg(int i) const { return c_bb16_diag[i]; }
-  __device__ __forceinline__ uint32_t sbox(uint32_t x) const {
-    uint32_t x2 = mmul<F>(x, x);
-    uint32_t x3 = mmul<F>(x2, x);
-    uint32_t x4 = mmul<F>(x2, x2);
-    return mmul<F>(x3, x4);
+  __device__ __forceinline__ uint32_t ark_sbox(uint32_t x, uint32_t c) const {
+    return ark_sbox_a<F, 7>(x, c, 7);
   }
   __device__ __forceinline__ uint32_t jsum(uint32_t s) const { return s; }
 };
@@ -111,13 +127,12 @@ struct RtParams {
   ZC_HD uint32_t et(int r, int i) const { return p->ext_term[r][i]; }
   ZC_HD uint32_t ir(int r) const { return p->int_rc[r]; }
   ZC_HD uint32_t dg(int i) const { return p->diag[i]; }
-  ZC_HD uint32_t sbox(uint32_t x) const {
-    uint32_t x2 = mmul<F>(x, x);
+  ZC_HD uint32_t ark_sbox(uint32_t x, uint32_t c) const {
     switch (p->alpha) {
-      case 3: return mmul<F>(x2, x);
-      case 5: return mmul<F>(mmul<F>(x2, x2), x);
-      case 7: return mmul<F>(mmul<F>(x2, x), mmul<F>(x2, x2));
-      default: return mpow<F>(x, p->alpha);
+      case 3: return ark_sbox_a<F, 3>(x, c, 3);
+      case 5: return ark_sbox_a<F, 5>(x, c, 5);
+      case 7: return ark_sbox_a<F, 7>(x, c, 7);
+      default: return ark_sbox_a<F, 0>(x, c, p->alpha);
     }
   }
   ZC_HD uint32_t jsum(uint32_t s) const { return p->j_is_one ? s : mmul<F>(s, p->j_scale); }
@@ -163,18 +178,18 @@ ZC_HD void p2_permute(uint32_t* s, const K& k) {
 #pragma unroll 1
   for (int r = 0; r < k.rf_half(); r++) {
 #pragma unroll
-    for (int i = 0; i < 16; i++) s[i] = k.sbox(madd<F>(s[i], k.ei(r, i)));
+    for (int i = 0; i < 16; i++) s[i] = k.ark_sbox(s[i], k.ei(r, i));
     p2_ext_linear<F>(s);
   }
 #pragma unroll 1
   for (int r = 0; r < k.rp(); r++) {
-    s[0] = k.sbox(madd<F>(s[0], k.ir(r)));
+    s[0] = k.ark_sbox(s[0], k.ir(r));
     k.internal_layer(s);
   }
 #pragma unroll 1
   for (int r = 0; r < k.rf_half(); r++) {
 #pragma unroll
-    for (int i = 0; i < 16; i++) s[i] = k.sbox(madd<F>(s[i], k.et(r, i)));
+    for (int i = 0; i < 16; i++) s[i] = k.ark_sbox(s[i], k.et(r, i));
     p2_ext_linear<F>(s);
   }
 }
@@ -211,20 +226,6 @@ ZC_HD void p2_compress(const uint32_t* l, const uint32_t* r, uint32_t* out,
 // make the call (full-warp shuffles), active half or not.
 constexpr unsigned kFullMask = 0xffffffffu;
 
-template <class F, int ALPHA>
-__device__ __forceinline__ uint32_t half_sbox(uint32_t x, uint32_t alpha) {
-  if (ALPHA == 3) return mmul<F>(mmul<F>(x, x), x);
-  if (ALPHA == 5) {
-    const uint32_t x2 = mmul<F>(x, x);
-    return mmul<F>(mmul<F>(x2, x2), x);
-  }
-  if (ALPHA == 7) {
-    const uint32_t x2 = mmul<F>(x, x);
-    return mmul<F>(mmul<F>(x2, x), mmul<F>(x2, x2));
-  }
-  return mpow<F>(x, alpha);
-}
-
 template <class F>
 __device__ __forceinline__ uint32_t half_sum16(uint32_t v) {
   v = madd<F>(v, __shfl_xor_sync(kFullMask, v, 1));
@@ -260,13 +261,13 @@ __device__ __forceinline__ uint32_t half_permute_a(uint32_t x, const P2Params* p
 #pragma unroll 1
   for (int r = 0; r < rfh; r++) {
     const uint32_t c_next = r + 1 < rfh ? p->ext_init[r + 1][l] : p->int_rc[0];
-    x = half_ext_linear<F>(half_sbox<F, ALPHA>(madd<F>(x, c), alpha));
+    x = half_ext_linear<F>(ark_sbox_a<F, ALPHA>(x, c, alpha));
     c = c_next;
   }
 #pragma unroll 1
   for (int r = 0; r < rp; r++) {
     const uint32_t c_next = r + 1 < rp ? p->int_rc[r + 1] : p->ext_term[0][l];
-    const uint32_t s0 = half_sbox<F, ALPHA>(madd<F>(x, c), alpha);  // lane 0's is used
+    const uint32_t s0 = ark_sbox_a<F, ALPHA>(x, c, alpha);  // lane 0's is used
     const uint32_t rest = half_sum16<F>(l == 0 ? 0u : x);           // lanes 1..15
     const uint32_t dx = mmul<F>(dg, l == 0 ? s0 : x);
     uint32_t sum = madd<F>(rest, __shfl_sync(kFullMask, s0, threadIdx.x & 16));
@@ -278,7 +279,7 @@ __device__ __forceinline__ uint32_t half_permute_a(uint32_t x, const P2Params* p
 #pragma unroll 1
   for (int r = 0; r < rfh; r++) {
     const uint32_t c_next = p->ext_term[r + 1 < rfh ? r + 1 : r][l];
-    x = half_ext_linear<F>(half_sbox<F, ALPHA>(madd<F>(x, c), alpha));
+    x = half_ext_linear<F>(ark_sbox_a<F, ALPHA>(x, c, alpha));
     c = c_next;
   }
   return x;
