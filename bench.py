@@ -584,11 +584,11 @@ def main():
     # Hash kernel (dominant): integer instructions executed per Poseidon2
     # permutation of the built-in BabyBear-16 instance, from the ncu capture
     # summarised in profiles/ (thread-level SASS instructions).
-    inst_per_perm = float(os.environ.get("ZC_INST_PER_PERM", "7128"))
-    # DRAM bytes per hashed LDE word of the k_leaf launch (134.34 MB read +
-    # 8.54 MB written for 2^19 leaves x 64 words, profiles/), scaled to this
+    inst_per_perm = float(os.environ.get("ZC_INST_PER_PERM", "6070"))
+    # DRAM bytes per hashed LDE word of the k_leaf launch (134.27 MB read +
+    # 8.60 MB written for 2^19 leaves x 64 words, profiles/), scaled to this
     # workload's leaf launch by its word count.
-    traffic_per_word = (134.341376e6 + 8.544e6) / float(1 << 25)
+    traffic_per_word = (134.273792e6 + 8.598272e6) / float(1 << 25)
     perms = info["perms_leaf"] + info["perms_node"]
     int_peak = 152 * 128 * sm_mhz * 1e6 / 1e9  # Ginst/s: 152 SMs x 128 lanes x clock
     achieved = perms * inst_per_perm / (hash_ms / 1e3) / 1e9
