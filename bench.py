@@ -241,7 +241,10 @@ def trace_workload(args, device):
         root, layers = prover.tree.commit_layout(leaves_layout(cw, nn, K, 1, nn), device)
         if timing is not None:
             timing[2].record(stream)
-        op = prover.tree.open_layout(leaves_layout(cw, nn, K, 1, nn), layers, idx, K)
+        # The device-resident steps leave the index-range flag unread (a host
+        # sync per step); the end-to-end steps, on the same indices, read it.
+        op = prover.tree.open_layout(leaves_layout(cw, nn, K, 1, nn), layers, idx, K,
+                                     check=e2e)
         if e2e:
             out = torch.cat([root.reshape(-1), op.row.reshape(-1), op.path.reshape(-1)])
             host_out = out.cpu()

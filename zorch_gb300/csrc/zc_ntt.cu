@@ -130,7 +130,8 @@ __device__ __forceinline__ void dif_pass(uint32_t* a, int log_rows, int logm, in
           const uint32_t w = tw[pos << (logm - 1 - H)];
           const uint32_t u = v[j], t = v[j2];
           v[j] = madd<F>(u, t);
-          v[j2] = mmul<F>(msub<F>(u, t), w);
+          // u - t in (-p, p) feeds the signed product directly
+          v[j2] = snorm<F>(smul<F>((int32_t)(u - t), (int32_t)w));
         }
       }
     }
@@ -196,12 +197,12 @@ __device__ void lde_small_body(const uint32_t* x, uint32_t* out, int log_k, int 
   for (int idx = threadIdx.x; idx < (b << log_k); idx += blockDim.x) {
     const int s = idx >> log_k, i = idx & (k - 1);
     uint32_t* slot = work + s * rs + pad(i);
-    uint32_t v = mmul<F>(*slot, hp[i]);
+    int32_t v = smul<F>((int32_t)*slot, (int32_t)hp[i]);
     if (s) {
       const int e = s * i;  // < n <= 2^14
-      v = mmul<F>(v, mmul<F>(wl[e & 127], wh[e >> 7]));
+      v = smul<F>(v, smul<F>((int32_t)wl[e & 127], (int32_t)wh[e >> 7]));
     }
-    *slot = v;
+    *slot = snorm<F>(v);
   }
   __syncthreads();
   smem_ntt_dif<F>(work, log_b, log_k, rs, tw);
@@ -258,7 +259,7 @@ __device__ void lde_pass1_body(const uint32_t* x, uint32_t* z, int log_k1, int l
   for (int idx = threadIdx.x; idx < (TI << log_k2); idx += blockDim.x) {
     const int d = idx & (TI - 1), i2 = idx >> log_ti;
     uint32_t* slot = work + d * rs + pad(i2);
-    *slot = mmul<F>(mmul<F>(*slot, gi[d]), R[i2]);
+    *slot = snorm<F>(smul<F>(smul<F>((int32_t)*slot, (int32_t)gi[d]), (int32_t)R[i2]));
   }
   __syncthreads();
   smem_ntt_dif<F>(work, log_ti, log_k2, rs, tw);
@@ -323,8 +324,9 @@ __device__ void lde_pass2_body(const uint32_t* z, uint32_t* out, int log_k1, int
     const int i1 = idx & (k1 - 1), row = idx >> log_k1;
     const int dt = row & (TT - 1);
     uint32_t* slot = work + row * rs + pad(i1);
-    *slot = mmul<F>(*slot,
-                    mmul<F>(lo[dt * lo_n + (i1 & (lo_n - 1))], hi[dt * hi_n + (i1 >> kTwLoLog)]));
+    *slot = snorm<F>(smul<F>((int32_t)*slot,
+                             smul<F>((int32_t)lo[dt * lo_n + (i1 & (lo_n - 1))],
+                                     (int32_t)hi[dt * hi_n + (i1 >> kTwLoLog)])));
   }
   __syncthreads();
   smem_ntt_dif<F>(work, log_rows, log_k1, rs, tw);
