@@ -47,7 +47,8 @@ def parse():
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["zorch", "reference"], default="zorch")
-    ap.add_argument("--workload", choices=["trace", "served", "fri", "uneven"], default="served")
+    ap.add_argument("--workload", choices=["trace", "served", "fri", "uneven", "paths"],
+                    default="served")
     ap.add_argument("--log-rows", type=int, default=20)
     ap.add_argument("--cols", type=int, default=64)
     ap.add_argument("--log-blowup", type=int, default=2)
@@ -385,6 +386,177 @@ def uneven_workload(args, device):
     return batched, plain, elements, shapes
 
 
+def paths_workload(args, device):
+    """Latency of the PCS paths around the commit (Basefold open, the SP1
+    stacked open, the k-ary fold rounds, the query-strided Merkle commit, the
+    proof-of-work grind and one transcript hop) through the public API on the
+    GPU, each beside the oracle on the same inputs on the host cores (the
+    CPU-baseline leg), with the two outputs compared. GPU times are wall time
+    per call with a device synchronize on both sides, mean over --steps calls
+    after warm-up; the oracle runs once per path."""
+    import json as _json
+
+    import torch
+
+    from zorch_gb300 import _lib
+    from zorch_gb300.coding import BitReversedReedSolomon, ReedSolomon
+    from zorch_gb300.commit import (MerkleTree, Poseidon2, SingleMatrixCommitmentScheme,
+                                    StridedMerkleTree)
+    from zorch_gb300.field import BABYBEAR, KOALABEAR, ptr, stream_handle, to_device, to_host
+    from zorch_gb300.jagged import stacked_basefold_open, stacked_commit
+    from zorch_gb300.pcs import BasefoldProver, FoldState, PreFoldKGroupCommitRound, fold_rounds
+    from zorch_gb300.transcript import DuplexTranscript
+
+    cpu = not args.no_cpu_baseline
+    orc = None
+    if cpu:
+        from oracle import oracle as orc
+    rng = np.random.default_rng(args.seed)
+
+    def mont(field, shape):
+        """Seeded uniform field elements, Montgomery words (x 2^32 mod p)."""
+        pm = np.uint64(BABYBEAR.p if field == 0 else KOALABEAR.p)
+        x = rng.integers(0, int(pm), size=shape, dtype=np.uint64)
+        return ((x << np.uint64(32)) % pm).astype(np.uint32)
+
+    def gpu_time(fn):
+        for _ in range(max(args.warmup, 3)):
+            fn()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            out = fn()
+        torch.cuda.synchronize()
+        return 1e3 * (time.perf_counter() - t0) / args.steps, out
+
+    def cpu_time(fn):
+        t0 = time.perf_counter()
+        out = fn()
+        return 1e3 * (time.perf_counter() - t0), out
+
+    rows = {}
+    bb = Poseidon2.builtin(BABYBEAR)
+    sp1d = _json.loads(open(os.path.join(ROOT, "tests", "golden", "sp1_fibonacci",
+                                         "sp1_koalabear16.json")).read())
+    sp1 = Poseidon2.from_params(KOALABEAR, sp1d["alpha"], sp1d["external_initial"],
+                                sp1d["external_terminal"], sp1d["internal_rc"],
+                                sp1d["internal_diag"], sp1d["internal_j_scale"])
+    kb = _json.loads(open(os.path.join(ROOT, "tests", "golden", "koalabear16.json")).read())
+    kbp = Poseidon2.from_params(KOALABEAR, kb["alpha"], kb["external_initial"],
+                                kb["external_terminal"], kb["internal_rc"], kb["internal_diag"],
+                                kb.get("internal_j_scale", 1))
+
+    # f1: Basefold batch open, 2^20 x 8 BabyBear columns, blowup 2, 64 queries
+    v, w, q = 20, 8, 64
+    code = ReedSolomon(1 << v, 2, BABYBEAR, coset_shift=31)
+    prover = BasefoldProver(code, MerkleTree(bb, column_major=True), num_queries=q)
+    cols_h = mont(0, (w, 1 << v))
+    z_h = mont(0, (v, 4))
+    _, data = prover.commit_columns(to_device(cols_h).reshape(w, 1 << v))
+    zd = to_device(z_h).reshape(v, 4)
+    g_ms, (_, proof, _) = gpu_time(lambda: prover.open_batch([data], zd, DuplexTranscript.new(bb)))
+    row = {"config": f"2^{v} x {w} BabyBear columns, blowup 2, {q} queries", "gpu_ms": g_ms}
+    if cpu:
+        cw = to_host(data.codeword)
+        p2 = orc.Poseidon2.babybear16()
+        mats = [{"cols": cols_h, "codeword": cw, "layers": orc.merkle_commit_columns(p2, cw)}]
+        c_ms, want = cpu_time(lambda: orc.basefold_open(p2, 0, mats, z_h, 1, BABYBEAR.mont(31), q,
+                                                         orc.Transcript(p2)))
+        row.update(cpu_ms=c_ms, equal=bool(
+            np.array_equal(to_host(proof.fri_roots), want["fri_roots"])
+            and np.array_equal(to_host(proof.final_poly), want["final_poly"])))
+    rows["basefold_open"] = row
+
+    # f2: SP1 stacked BaseFold open, two committed rounds (8 + 4 columns) of 2^20, blowup 2
+    v, q = 20, 64
+    scode = BitReversedReedSolomon(1 << v, 2, KOALABEAR)
+    smcs = SingleMatrixCommitmentScheme(sp1)
+    blocks = [mont(1, (8, 1 << v)), mont(1, (4, 1 << v))]
+    srounds = [stacked_commit(smcs, scode, to_device(b).reshape(b.shape)) for b in blocks]
+    zf, de = mont(1, (v + 2, 4)), mont(1, (4,))
+    zfd, ded = to_device(zf).reshape(v + 2, 4), to_device(de)
+    g_ms, (sproof, _) = gpu_time(lambda: stacked_basefold_open(
+        smcs, scode, srounds, zfd, ded, v, num_queries=q, pow_bits=0,
+        transcript=DuplexTranscript.new(sp1)))
+    row = {"config": f"KoalaBear, rounds of 8 + 4 columns x 2^{v}, blowup 2, {q} queries",
+           "gpu_ms": g_ms}
+    if cpu:
+        p2 = orc.sp1_koalabear16()
+        c_ms, want = cpu_time(lambda: orc.sp1_stacked_open(p2, 1, blocks, zf, de, v, 1, q,
+                                                            orc.Transcript(p2)))
+        row.update(cpu_ms=c_ms, equal=bool(
+            np.array_equal(to_host(sproof.fri_commitments), want["bound_roots"])
+            and np.array_equal(to_host(sproof.final_poly), want["final_poly"])))
+    rows["sp1_stacked_open"] = row
+
+    # f4: k-ary fold-and-commit rounds (k = 4, two rounds) over a 2^22 KoalaBear codeword
+    k, nr = 4, 2
+    kcode = ReedSolomon(1 << 21, 2, KOALABEAR, fold_factor=k)
+    ktree = MerkleTree(kbp)
+    msg = to_device(mont(1, (1 << 21,)))
+    kcw = kcode.encode(msg)
+
+    def kary():
+        st, _, roots = fold_rounds(PreFoldKGroupCommitRound(kcode, ktree), FoldState(kcw),
+                                   DuplexTranscript.new(kbp), nr)
+        return st.codeword, roots
+    g_ms, (kfinal, kroots) = gpu_time(kary)
+    row = {"config": f"k = {k}, {nr} rounds from a 2^22 KoalaBear codeword", "gpu_ms": g_ms}
+    if cpu:
+        cp = orc.Poseidon2.koalabear16_golden()
+        cw0 = to_host(kcw)
+
+        def kary_cpu():
+            ot, cw, rts = orc.Transcript(cp), cw0, []
+            for _ in range(nr):
+                n = cw.shape[0]
+                dl = orc.merkle_commit(cp, cw, n // k, k, 1, n // k)
+                ot.observe(dl[-1][0])
+                rts.append(dl[-1][0])
+                cw = orc.fri_fold_k(1, cw, False, ot.sample(1), False, 2, 0)
+            return cw, rts
+        c_ms, (wcw, wroots) = cpu_time(kary_cpu)
+        row.update(cpu_ms=c_ms, equal=bool(
+            np.array_equal(to_host(torch.stack(kroots)), np.stack(wroots))
+            and np.array_equal(to_host(kfinal), wcw)))
+    rows["kary_fold_commit"] = row
+
+    # f4: query-strided Merkle commit (WHIR), 2^20 x 8 BabyBear rows, 16 rows per query
+    h, sw, rpq = 1 << 20, 8, 16
+    mat = mont(0, (h, sw))
+    md = to_device(mat).reshape(h, sw)
+    stree = StridedMerkleTree(bb, rpq)
+    g_ms, (sroot, _) = gpu_time(lambda: stree.commit(md))
+    row = {"config": f"2^20 x {sw} BabyBear rows, {rpq} rows per query", "gpu_ms": g_ms}
+    if cpu:
+        c_ms, want = cpu_time(lambda: orc.strided_merkle_commit(orc.Poseidon2.babybear16(), mat,
+                                                                 rpq))
+        row.update(cpu_ms=c_ms, equal=bool(np.array_equal(to_host(sroot).reshape(-1),
+                                                          want[-1].reshape(-1))))
+    rows["strided_merkle_commit"] = row
+
+    # f3: proof-of-work grind (pow_bits 18) and one transcript hop (observe 8, squeeze 1)
+    seed_vals = mont(0, (5,))
+    t0 = DuplexTranscript.new(bb).observe(to_device(seed_vals))
+    g_ms, (_, wit) = gpu_time(lambda: t0.grind(18))
+    row = {"config": "pow_bits 18, BabyBear duplex transcript", "gpu_ms": g_ms}
+    if cpu:
+        ot = orc.Transcript(orc.Poseidon2.babybear16())
+        ot.observe(seed_vals)
+        c_ms, wcanon = cpu_time(lambda: ot.grind(18))
+        row.update(cpu_ms=c_ms, equal=int(to_host(wit.reshape(1))[0]) == BABYBEAR.mont(wcanon))
+    rows["grind"] = row
+    vals8 = to_device(mont(0, (8,)))
+    tt = DuplexTranscript.new(bb)
+    hop_ms, _ = gpu_time(lambda: tt.observe_and_sample_(vals8, 1))
+    rows["transcript_hop"] = {"config": "observe 8 + squeeze 1 on the device (one launch)",
+                              "gpu_ms": hop_ms}
+    for r in rows.values():
+        if "cpu_ms" in r:
+            r["speedup"] = r["cpu_ms"] / r["gpu_ms"]
+    return rows, (orc.threads() if cpu else None)
+
+
 def pct(xs, q):
     return float(np.percentile(np.asarray(xs), q)) if len(xs) else None
 
@@ -406,6 +578,21 @@ def main():
     from zorch_gb300 import _lib
 
     _lib.check(_lib.lib().zc_init(local), "init")
+    if args.workload == "paths":
+        rows, threads = paths_workload(args, device)
+        if rank == 0:
+            print(json.dumps({
+                "metric": "PCS path latency (Basefold open, SP1 stacked open, k-ary fold, "
+                          "strided Merkle commit, grind, transcript hop)",
+                "value": rows["basefold_open"]["gpu_ms"], "unit": "ms per Basefold open",
+                "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+                "higher_is_better": False, "scaling": "weak", "vs_baseline": None,
+                "dtype": "u32 (BabyBear / KoalaBear, Montgomery)", "data": "synthetic, seeded",
+                "workload": "paths", "rows": rows,
+                "cpu_baseline": None if threads is None else {
+                    "kind": "port", "cores": threads,
+                    "sample": "the oracle once per path on the same inputs"}}), flush=True)
+        return
     step, info = trace_workload(args, device)
     stream = torch.cuda.current_stream()
 
