@@ -466,6 +466,19 @@ def paths_workload(args, device):
             np.array_equal(to_host(proof.fri_roots), want["fri_roots"])
             and np.array_equal(to_host(proof.final_poly), want["final_poly"])))
     rows["basefold_open"] = row
+    # the same open replayed from one CUDA graph (GraphedBasefoldOpen)
+    from zorch_gb300.pcs import GraphedBasefoldOpen
+
+    gbo = GraphedBasefoldOpen(prover, [data])
+    t_empty = DuplexTranscript.new(bb)
+    g_ms, (_, gproof, _) = gpu_time(lambda: gbo.replay(zd, t_empty))
+    grow = {"config": row["config"] + ", one graph replay", "gpu_ms": g_ms,
+            "equal_to_eager": bool(torch.equal(gproof.fri_roots, proof.fri_roots)
+                                   and torch.equal(gproof.final_poly, proof.final_poly)
+                                   and torch.equal(gproof.uni_msgs, proof.uni_msgs))}
+    if cpu:
+        grow["cpu_ms"] = row["cpu_ms"]
+    rows["basefold_open_graphed"] = grow
 
     # f2: SP1 stacked BaseFold open, two committed rounds (8 + 4 columns) of 2^20, blowup 2
     v, q = 20, 64

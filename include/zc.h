@@ -289,6 +289,12 @@ zc_status zc_rlc_columns_ex(zc_field field, const uint32_t* cw, int64_t n, int32
 zc_status zc_rlc_values(zc_field field, const uint32_t* values, int32_t w,
                         const uint32_t* challenges, int32_t nbv, int32_t offset,
                         int32_t accumulate, uint32_t* out, void* stream);
+/* Element-wise EF4 inverse of count values (16-byte aligned [count][4]
+ * Montgomery words; in may equal out); zero maps to zero. The 1/z_i the
+ * sumcheck message takes (Basefold's 1/z_last,
+ * zorch/pcs/basefold/kernel.py:52-66), computed on the device. */
+zc_status zc_ef4_inv(zc_field field, const uint32_t* in, uint32_t* out, int64_t count,
+                     void* stream);
 /* One interleaved-sumcheck message (SumcheckKernel.message,
  * zorch/pcs/basefold/kernel.py:52-66): the running MLE mle[2M] (EF4), the eq
  * table eq[M] of the unbound point prefix, the running claim and 1/z_last:

@@ -145,3 +145,49 @@ def test_eval_mle_and_eq_match_oracle(orc):
         _lib.check(L.zc_eq_expand(KOALABEAR.id, zd.data_ptr(), m, out.data_ptr(), ws.data_ptr(),
                                   nb, 0), "eq_expand")
         assert np.array_equal(to_host(out), orc.eq_expand(1, z)), m
+
+
+def test_ef4_inverse_matches_oracle(orc):
+    L = _lib.lib()
+    for field in (0, 1):
+        a = rand_mont(orc, field, (37, 4), 80 + field)
+        a[5] = 0  # zero maps to zero
+        a[6, 1:] = 0  # a base-field element
+        out = torch.empty((37, 4), dtype=torch.int32, device="cuda")
+        _lib.check(L.zc_ef4_inv(field, dev(a).data_ptr(), out.data_ptr(), 37, 0), "ef4_inv")
+        got = to_host(out)
+        for i in range(37):
+            assert np.array_equal(got[i], orc.ef4_inv(field, a[i])), (field, i)
+
+
+def test_graphed_open_replays_the_eager_open(orc):
+    """GraphedBasefoldOpen: one capture, replays at new points and transcripts
+    give the eager open's values and proof bytes."""
+    from zorch_gb300.coding import ReedSolomon
+    from zorch_gb300.commit import MerkleTree, Poseidon2
+    from zorch_gb300.pcs import BasefoldProver, GraphedBasefoldOpen
+    from zorch_gb300.transcript import DuplexTranscript
+
+    v, perm = 11, Poseidon2.builtin(BABYBEAR)
+    code = ReedSolomon(1 << v, 2, BABYBEAR, coset_shift=31)
+    prover = BasefoldProver(code, MerkleTree(perm, column_major=True), num_queries=9)
+    datas = []
+    for i, w in enumerate((5, 3)):
+        _, d = prover.commit_columns(dev(rand_mont(orc, 0, (w, 1 << v), 300 + i)).reshape(w, -1))
+        datas.append(d)
+    graphed = GraphedBasefoldOpen(prover, datas)
+    for k in range(3):
+        z = dev(rand_mont(orc, 0, (v, 4), 400 + k)).reshape(v, 4)
+        t = DuplexTranscript.new(perm).observe(dev(rand_mont(orc, 0, (k + 1,), 500 + k)))
+        values, proof, t_out = prover.open_batch(datas, z, t)
+        g_values, g_proof, g_t = graphed.replay(z, t)
+        for a, b in zip(values, g_values):
+            assert torch.equal(a, b)
+        assert torch.equal(proof.uni_msgs, g_proof.uni_msgs)
+        assert torch.equal(proof.fri_roots, g_proof.fri_roots)
+        assert torch.equal(proof.final_poly, g_proof.final_poly)
+        assert torch.equal(proof.positions, g_proof.positions)
+        for a, b in zip(proof.component_openings + proof.query_openings,
+                        g_proof.component_openings + g_proof.query_openings):
+            assert torch.equal(a.row, b.row) and torch.equal(a.path, b.path)
+        assert torch.equal(t_out.state, g_t.state)

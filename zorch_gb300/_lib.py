@@ -86,6 +86,7 @@ def _declare(lib: C.CDLL) -> None:
         "zc_eval_mle": (st, [st, vp, i32, i32, vp, vp, vp, sz, vp]),
         "zc_rlc_columns_ex": (st, [st, vp, i64, i32, vp, i32, i32, i32, vp, vp]),
         "zc_rlc_values": (st, [st, vp, i32, vp, i32, i32, i32, vp, vp]),
+        "zc_ef4_inv": (st, [st, vp, vp, i64, vp]),
         "zc_sumcheck_workspace_bytes": (sz, []),
         "zc_sumcheck_message": (st, [st, vp, i64, vp, vp, vp, vp, vp, sz, vp]),
         "zc_sumcheck_fold": (st, [st, vp, i64, vp, i32, vp, vp, vp, vp, vp, vp]),

@@ -183,8 +183,6 @@ def stacked_basefold_open(smcs: SingleMatrixCommitmentScheme, code: BitReversedR
     pre-fold [n/2, 8] rows, observe message and bound root, EF4 beta, fold the
     codeword, MLE and claim; observe the final poly, grind, draw SP1 query
     positions and open every fold layer and every committed round."""
-    from .field import from_mont_np
-
     if not rounds:
         raise ValueError("the stacked open needs at least one committed round")
     if log_stacking_height < 1:
@@ -235,10 +233,11 @@ def stacked_basefold_open(smcs: SingleMatrixCommitmentScheme, code: BitReversedR
         off += K
     # fold zone
     cw = _ef4_encode(code, mle)
-    t.observe_(torch.tensor([f.mont(v)], dtype=torch.int32, device=dev))
-    zh = from_mont_np(f, to_host(zs))
-    zinv = torch.tensor(np.array([f.ef_to_mont(f.ef_inv(tuple(int(x) for x in row)))
-                                  for row in zh], np.uint32).view(np.int32), device=dev)
+    nv = torch.zeros(1, dtype=torch.int32, device=dev)
+    nv.fill_(f.mont(v))  # a fill kernel: no host copy
+    t.observe_(nv)
+    zinv = torch.empty_like(zs)  # 1/z per stacking coordinate, on the device
+    _lib.check(L.zc_ef4_inv(f.id, ptr(zs), ptr(zinv), v, st), "ef4_inv")
     eq = torch.empty((max(S // 2, 1), 4), dtype=torch.int32, device=dev)
     nb = L.zc_eq_expand_workspace_bytes(v - 1)
     ews = torch.empty(max((nb + 15) // 4, 4), dtype=torch.int32, device=dev)

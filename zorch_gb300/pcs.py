@@ -360,8 +360,8 @@ class BasefoldProver:
         (Montgomery words on the device; _open_batch_body,
         zorch/pcs/basefold/prover.py:503-547, and _fold_and_query, :419-480):
         returns (values: per matrix [w, 4], proof, transcript). The whole open
-        runs on the device; the only host work is 1/z per coordinate."""
-        from .field import from_mont_np
+        runs on the device with no host synchronisation, so it can be captured
+        in a CUDA graph (GraphedBasefoldOpen)."""
         if not rounds:
             raise ValueError("BaseFold opens at least one committed matrix, got none")
         if z.dim() != 2 or z.shape[1] != 4 or z.shape[0] < 1:
@@ -411,11 +411,11 @@ class BasefoldProver:
             _lib.check(L.zc_rlc_values(f.id, ptr(vals), w, ptr(chal), nbv, off, acc, ptr(claim),
                                        st), "rlc values")
             off += w
-        t.observe_(torch.tensor([f.mont(v), 0, 0, 0], dtype=torch.int32, device=dev))
-        # 1/z per coordinate (statement data, on the host)
-        zh = from_mont_np(f, to_host(zc))
-        zinv = torch.tensor(np.array([f.ef_to_mont(f.ef_inv(tuple(int(x) for x in row)))
-                                      for row in zh], np.uint32).view(np.int32), device=dev)
+        nv = torch.zeros(4, dtype=torch.int32, device=dev)
+        nv[:1].fill_(f.mont(v))  # a fill kernel: no host copy, capturable
+        t.observe_(nv)
+        zinv = torch.empty_like(zc)  # 1/z per coordinate, on the device
+        _lib.check(L.zc_ef4_inv(f.id, ptr(zc), ptr(zinv), v, st), "ef4_inv")
         eq = torch.empty((max(S // 2, 1), 4), dtype=torch.int32, device=dev)
         nb = L.zc_eq_expand_workspace_bytes(v - 1)
         ews = torch.empty(max((nb + 15) // 4, 4), dtype=torch.int32, device=dev)
@@ -585,6 +585,42 @@ class BasefoldVerifier:
                     expected = ef(final[a])
                 ok &= folded == expected
         return bool(ok)
+
+
+class GraphedBasefoldOpen:
+    """BasefoldProver.open_batch over fixed committed matrices captured once
+    into a CUDA graph: the evaluations, the batching, every sumcheck round with
+    its fused fold-and-commit and transcript steps, the query positions and all
+    openings replay with one launch. `replay(z, transcript)` copies the point
+    and the transcript state into static inputs and returns (values, proof,
+    transcript) -- static tensors that the next replay overwrites. The
+    matrices' device buffers are baked into the graph: reuse it for as many
+    openings of those commitments as needed."""
+
+    def __init__(self, prover: BasefoldProver, rounds: Sequence[BasefoldProverData],
+                 device="cuda") -> None:
+        self.prover = prover
+        self.rounds = list(rounds)
+        v = prover.code.message_len.bit_length() - 1
+        self.z = torch.zeros((v, 4), dtype=torch.int32, device=device)
+        self.state = torch.zeros(_lib.DUPLEX_WORDS, dtype=torch.int32, device=device)
+        self._run()  # kernel attributes, allocator warm-up
+        torch.cuda.synchronize()
+        self.graph = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(self.graph):
+            self.out = self._run()
+
+    def _run(self):
+        t = DuplexTranscript(self.prover.tree.perm, self.state)
+        return self.prover.open_batch(self.rounds, self.z, t)
+
+    def replay(self, z: torch.Tensor, transcript: DuplexTranscript):
+        if z.shape != self.z.shape:
+            raise ValueError(f"point shape {tuple(z.shape)} != captured {tuple(self.z.shape)}")
+        self.z.copy_(z, non_blocking=True)
+        self.state.copy_(transcript.state, non_blocking=True)
+        self.graph.replay()
+        return self.out
 
 
 class GraphedFriCommitPhase:
