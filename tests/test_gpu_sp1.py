@@ -13,6 +13,7 @@ layer's dumped values. Integer work: the tolerance is zero.
 
 from __future__ import annotations
 
+import dataclasses
 import lzma
 
 import numpy as np
@@ -277,3 +278,85 @@ def test_stacked_open_matches_oracle(orc, sp1, widths, v, log_blowup, queries, p
                               orc.smcs_bind_root(cperm, layers[-1][0], n.bit_length() - 1,
                                                  b.shape[0]))
     assert all(np.array_equal(x, want["final_claim"]) for x in want["final_codeword"])
+
+
+def _stacked_case(orc, sp1, pow_bits, widths=(3, 2), v=7, queries=6):
+    """A stacked open over rounds of `widths` columns with a consistent
+    statement: dense_eval is the MLE of the batch evaluations at the leading
+    coordinates of z_final (SP1's stacking identity)."""
+    from zorch_gb300.coding import BitReversedReedSolomon
+    from zorch_gb300.commit import SingleMatrixCommitmentScheme
+    from zorch_gb300.jagged import _ef_eval_mle_msb, stacked_basefold_open, stacked_commit
+    from zorch_gb300.transcript import DuplexTranscript
+
+    gperm, _ = sp1
+    f = KOALABEAR
+    S = 1 << v
+    code = BitReversedReedSolomon(S, 2, f)
+    smcs = SingleMatrixCommitmentScheme(gperm)
+    blocks = [rand_mont(orc, 1, (w, S), 90 + i) for i, w in enumerate(widths)]
+    rounds = [stacked_commit(smcs, code, dev(b).reshape(b.shape)) for b in blocks]
+    z = rand_mont(orc, 1, (v + 3, 4), 95)
+    zd = dev(z).reshape(v + 3, 4)
+    probe, _ = stacked_basefold_open(smcs, code, rounds, zd, dev(np.zeros(4, np.uint32)), v,
+                                     num_queries=queries, pow_bits=0,
+                                     transcript=DuplexTranscript.new(gperm))
+    flat = [f.ef_from_mont(r) for e in probe.batch_evals for r in to_host(e).reshape(-1, 4)]
+    lead = [f.ef_from_mont(r) for r in z[:3]]
+    de = np.array(f.ef_to_mont(_ef_eval_mle_msb(f, flat + [(0, 0, 0, 0)] * (8 - len(flat)),
+                                                lead)), np.uint32)
+    proof, _ = stacked_basefold_open(smcs, code, rounds, zd, dev(de), v, num_queries=queries,
+                                     pow_bits=pow_bits, transcript=DuplexTranscript.new(gperm))
+    return smcs, code, list(widths), zd, de, v, proof
+
+
+@pytest.mark.parametrize("pow_bits", [0, 7])
+def test_stacked_open_verifies(orc, sp1, pow_bits):
+    """Open -> verify completeness (zorch/pcs/jagged/testing/open_test.py's
+    real-transcript round trip) through the host verifier."""
+    from zorch_gb300.jagged import stacked_basefold_verify
+    from zorch_gb300.transcript import HostDuplexTranscript
+
+    smcs, code, widths, zd, de, v, proof = _stacked_case(orc, sp1, pow_bits)
+    _, ok = stacked_basefold_verify(smcs, code, widths, zd, de, v, proof,
+                                    HostDuplexTranscript(sp1[0]), num_queries=6,
+                                    pow_bits=pow_bits)
+    assert ok
+
+
+def test_stacked_verify_rejects_tampering(orc, sp1):
+    from zorch_gb300.jagged import stacked_basefold_verify
+    from zorch_gb300.transcript import HostDuplexTranscript
+
+    smcs, code, widths, zd, de, v, proof = _stacked_case(orc, sp1, 5)
+
+    def check(p, de_=de, pow_bits=5):
+        return stacked_basefold_verify(smcs, code, widths, zd, de_, v, p,
+                                       HostDuplexTranscript(sp1[0]), num_queries=6,
+                                       pow_bits=pow_bits)[1]
+
+    assert check(proof)
+
+    def flip(t, idx):
+        t = t.clone()
+        t.view(-1)[idx] ^= 1
+        return t
+
+    bad_de = de.copy()
+    bad_de[1] ^= 1
+    assert not check(proof, de_=bad_de)
+    assert not check(dataclasses.replace(proof, univariate_messages=flip(
+        proof.univariate_messages, 3)))
+    assert not check(dataclasses.replace(proof, final_poly=flip(proof.final_poly, 0)))
+    assert not check(dataclasses.replace(proof, fri_raw_roots=flip(proof.fri_raw_roots, 9)))
+    assert not check(dataclasses.replace(proof, pow_witness=flip(proof.pow_witness, 0)))
+    assert not check(dataclasses.replace(proof, batch_evals=[flip(proof.batch_evals[0], 2),
+                                                             *proof.batch_evals[1:]]))
+    rows, paths = proof.component_openings[1]
+    assert not check(dataclasses.replace(proof, component_openings=[
+        proof.component_openings[0], (flip(rows, 4), paths)]))
+    rows, paths = proof.query_openings[2]
+    assert not check(dataclasses.replace(proof, query_openings=[
+        *proof.query_openings[:2], (flip(rows, 5), paths), *proof.query_openings[3:]]))
+    with pytest.raises(ValueError):
+        check(dataclasses.replace(proof, batch_evals=proof.batch_evals[:1]))

@@ -283,3 +283,158 @@ def stacked_basefold_open(smcs: SingleMatrixCommitmentScheme, code: BitReversedR
         torch.stack([ly.bound_root for ly in layers]), msgs.reshape(v, 2, 4), final_poly,
         witness, batch_evals, component_openings, query_openings, positions)
     return proof, t
+
+
+def _ef_eval_mle_msb(f, values: list, point: list) -> tuple:
+    """MLE of `values` (EF4 tuples, 2^m of them) at `point` (m EF4 tuples),
+    point[0] binding the most significant index bit -- the eq-table order of
+    eval_mle (zorch/poly/eq.py:55-62)."""
+    cur = list(values)
+    for z in point:
+        half = len(cur) // 2
+        cur = [f.ef_add(cur[i], f.ef_mul(z, f.ef_sub(cur[half + i], cur[i]))) for i in range(half)]
+    return cur[0]
+
+
+def stacked_basefold_verify(smcs: SingleMatrixCommitmentScheme, code: BitReversedReedSolomon,
+                            round_widths: Sequence[int], z_final, dense_eval,
+                            log_stacking_height: int, proof: StackedOpenProof, transcript,
+                            *, num_queries: int, pow_bits: int):
+    """Verify a stacked BaseFold open on the host (stacked_basefold_verify,
+    zorch/pcs/jagged/verifier.py:165-356); returns (transcript, ok).
+
+    `transcript` is a HostDuplexTranscript at the state the prover's open
+    started from. Checks, in the open's absorb order: SP1's stacking identity
+    (dense_eval = the MLE of the concatenated batch evaluations at the leading
+    coordinates), the staggered batching, every interleaved sumcheck round
+    against the running claim, each bound fold root against its raw root, the
+    proof of work, the query positions, every component and fold-layer
+    opening against its commitment, the batched component rows against fold
+    layer 0, and the bit-reversed fold chain down to the final poly. Malformed
+    shapes raise ValueError, as the reference does; a wrong proof gives False."""
+    f = code.field
+    host = lambda x: to_host(x) if torch.is_tensor(x) else np.asarray(x, np.uint32)  # noqa: E731
+    ef = lambda w: f.ef_from_mont([int(v) for v in w])  # noqa: E731
+    v = log_stacking_height
+    n = code.block_len
+    if v < 1:
+        raise ValueError(f"need at least one stacking variable, got "
+                         f"log_stacking_height={log_stacking_height}")
+    if num_queries < 1:
+        raise ValueError(f"need at least one query, got num_queries={num_queries}")
+    if not (len(proof.component_commitments) == len(round_widths) == len(proof.batch_evals)
+            == len(proof.component_openings)):
+        raise ValueError(f"round mismatch: {len(proof.component_commitments)} component "
+                         f"commitments, {len(round_widths)} widths, "
+                         f"{len(proof.batch_evals)} batch evals, "
+                         f"{len(proof.component_openings)} component openings")
+    evals = [host(e).reshape(-1, 4) for e in proof.batch_evals]
+    for r, (e, k) in enumerate(zip(evals, round_widths)):
+        if e.shape[0] != k:
+            raise ValueError(f"round {r} batch evals must cover its {k} stacked columns, "
+                             f"got {e.shape[0]}")
+    msgs = host(proof.univariate_messages).reshape(-1, 8)
+    raw = host(proof.fri_raw_roots).reshape(-1, 8)
+    bound = host(proof.fri_commitments).reshape(-1, 8)
+    if msgs.shape[0] != v:
+        raise ValueError(f"need one (s(0), s(1)) message per stacking variable ({v}), "
+                         f"got {msgs.shape[0]}")
+    if bound.shape[0] != v or raw.shape[0] != v or len(proof.query_openings) != v:
+        raise ValueError(f"need one committed fold layer per stacking variable ({v})")
+    zf = [ef(r) for r in host(z_final).reshape(-1, 4)]
+    if len(zf) < v:
+        raise ValueError(f"the folded point must carry at least the {v} stacking "
+                         f"variables, got {len(zf)}")
+    stack_point, batch_point = zf[len(zf) - v:], zf[:len(zf) - v]
+    flat = [ef(r) for e in evals for r in e]
+    width = 1 << len(batch_point)
+    if len(flat) > width:
+        raise ValueError(f"{len(flat)} stacked columns do not fit the {len(batch_point)} "
+                         f"leading point variables")
+    de = host(dense_eval).reshape(-1)
+    ok = ef(de) == _ef_eval_mle_msb(f, flat + [(0, 0, 0, 0)] * (width - len(flat)),
+                                    batch_point)
+    t = transcript.observe(de)
+    for e in evals:
+        t = t.observe(e.reshape(-1))
+    total = sum(int(k) for k in round_widths)
+    nbv = (total - 1).bit_length() if total > 1 else 0
+    chal = []
+    if nbv:
+        t, s = t.sample(4 * nbv)
+        chal = [ef(s[4 * j:4 * j + 4]) for j in range(nbv)]
+
+    def weight(idx: int) -> tuple:
+        w = (1, 0, 0, 0)
+        for j, r in enumerate(chal):
+            bit = (idx >> (nbv - 1 - j)) & 1
+            w = f.ef_mul(w, r if bit else f.ef_sub((1, 0, 0, 0), r))
+        return w
+
+    wts = [weight(c) for c in range(total)]
+    claim = (0, 0, 0, 0)
+    for c, x in enumerate(flat):
+        claim = f.ef_add(claim, f.ef_mul(wts[c], x))
+    t = t.observe([f.mont(v)])
+    betas = []
+    for i in range(v):
+        s0, s1 = ef(msgs[i, :4]), ef(msgs[i, 4:])
+        x = stack_point[v - 1 - i]
+        ok &= claim == f.ef_add(f.ef_mul(f.ef_sub((1, 0, 0, 0), x), s0), f.ef_mul(x, s1))
+        t = t.observe(msgs[i])
+        t, b = t.observe_and_sample(bound[i], 4)
+        beta = ef(b)
+        betas.append(beta)
+        claim = f.ef_add(s0, f.ef_mul(beta, s1))
+        log_h = (n >> (i + 1)).bit_length() - 1
+        ok &= np.array_equal(smcs.bind_root_host(raw[i], log_h, 8), bound[i])
+    final = host(proof.final_poly).reshape(-1)
+    t = t.observe(final)
+    t, ok_pow = t.check_witness(host(proof.pow_witness).reshape(-1), pow_bits=pow_bits)
+    ok &= bool(ok_pow)
+    t, sq = t.sample(num_queries)
+    positions = [f.canon(int(x)) & (n - 1) for x in sq]
+    if [int(x) for x in host(proof.positions).reshape(-1)] != positions:
+        return t, False
+    # Merkle phase
+    from .commit import VerifyCode
+
+    for r, (rows, paths) in enumerate(proof.component_openings):
+        rows, paths = host(rows), host(paths)
+        for qi, q in enumerate(positions):
+            ok &= smcs.verify_batch(proof.component_commitments[r], (n, int(round_widths[r])),
+                                    q, rows[qi], paths[:, qi]) == VerifyCode.OK
+    for i, (rows, paths) in enumerate(proof.query_openings):
+        rows, paths = host(rows), host(paths)
+        for qi, q in enumerate(positions):
+            ok &= smcs.verify_batch(bound[i], (n >> (i + 1), 8), q >> (i + 1), rows[qi],
+                                    paths[:, qi]) == VerifyCode.OK
+    if not ok:
+        return t, False
+    # fold consistency: batched component rows at q == fold layer 0's leg; then
+    # each opened pair (f(x), f(-x)) folds to the next layer's value
+    shift = code.coset_shift or 1
+    inv2 = pow(2, f.p - 2, f.p)
+    comp_rows = [host(rows) for rows, _ in proof.component_openings]
+    layer_rows = [host(rows).reshape(-1, 2, 4) for rows, _ in proof.query_openings]
+    final_ef = ef(final)
+    for qi, q in enumerate(positions):
+        comp, off = (0, 0, 0, 0), 0
+        for rows in comp_rows:
+            for c, xw in enumerate(rows[qi]):
+                comp = f.ef_add(comp, f.ef_scale(wts[off + c], f.canon(int(xw))))
+            off += rows.shape[1]
+        ok &= comp == ef(layer_rows[0][qi][q & 1])
+        for i in range(v):
+            ni = n >> i
+            m = ni.bit_length() - 1
+            a = q >> (i + 1)
+            e = int(bin(a)[2:].zfill(m - 1)[::-1], 2) if m > 1 else 0  # brev_{m-1}(a)
+            xpt = pow(shift, 1 << i, f.p) * pow(f.root_of_unity(m), e, f.p) % f.p
+            lo, hi = ef(layer_rows[i][qi][0]), ef(layer_rows[i][qi][1])
+            folded = f.ef_add(f.ef_scale(f.ef_add(lo, hi), inv2),
+                              f.ef_scale(f.ef_mul(betas[i], f.ef_sub(lo, hi)),
+                                         pow(2 * xpt % f.p, f.p - 2, f.p)))
+            want = ef(layer_rows[i + 1][qi][a & 1]) if i + 1 < v else final_ef
+            ok &= folded == want
+    return t, bool(ok)
