@@ -96,6 +96,13 @@ __device__ void pow_table(uint32_t* tab, int count, uint32_t base) {
   }
 }
 
+// tab[i] = w_{2^log_m}^i for i < count <= 2^log_m, read straight off the
+// root tables (independent entries: no multiply chain, no barrier).
+template <class F>
+__device__ void root_table(uint32_t* tab, int count, int log_m) {
+  for (int i = threadIdx.x; i < count; i += blockDim.x) tab[i] = omega_pow<F>(log_m, (uint32_t)i);
+}
+
 // One radix-2^R pass of a decimation-in-frequency NTT over `rows` rows of
 // m = 2^logm words (row stride rs): the stages of half-size 2^h0 down to
 // 2^(h0-R+1). A group is the 2^R elements base + j*S, S = 2^(h0-R+1); the
@@ -188,11 +195,13 @@ __device__ void lde_small_body(const uint32_t* x, uint32_t* out, int log_k, int 
   const uint32_t* xc = x + (c << log_k);
   for (int idx = threadIdx.x; idx < (b << log_k); idx += blockDim.x)
     cp_async4(work + (idx >> log_k) * rs + pad(idx & (k - 1)), xc + (idx & (k - 1)));
-  const uint32_t wn = log_n ? omega_pow<F>(log_n, 1) : F::ONE;
-  pow_table<F>(tw, k > 1 ? k / 2 : 1, log_k ? omega_pow<F>(log_k, 1) : F::ONE);
+  root_table<F>(tw, k > 1 ? k / 2 : 1, log_k);
+  const uint32_t nmask = (1u << log_n) - 1;  // w_n^e depends on e mod n
+  for (int e = threadIdx.x; e < 128; e += blockDim.x) {
+    wl[e] = omega_pow<F>(log_n, (uint32_t)e & nmask);
+    wh[e] = omega_pow<F>(log_n, ((uint32_t)e << 7) & nmask);
+  }
   pow_table<F>(hp, k, h);
-  pow_table<F>(wl, 128, wn);
-  pow_table<F>(wh, 128, mpow<F>(wn, 128));
   cp_async_wait_all();
   for (int idx = threadIdx.x; idx < (b << log_k); idx += blockDim.x) {
     const int s = idx >> log_k, i = idx & (k - 1);
@@ -244,30 +253,35 @@ __device__ void lde_pass1_body(const uint32_t* x, uint32_t* z, int log_k1, int l
   uint32_t* R = tw + (k2 > 1 ? k2 / 2 : 1);
   uint32_t* gi = R + k2;
   const int i1_0 = tile * TI;
-  const uint32_t* xc = x + (c << log_k);
-  for (int idx = threadIdx.x; idx < (TI << log_k2); idx += blockDim.x) {
-    const int d = idx & (TI - 1), i2 = idx >> log_ti;
-    cp_async4(work + d * rs + pad(i2), xc + i1_0 + d + ((int64_t)i2 << log_k1));
+  // Thread t always owns column d = t mod TI (TI <= kThreads, both powers of
+  // two) and walks i2 = t / TI, + kThreads / TI, ...: the column offsets are
+  // loop-invariant and the row offsets step by constants.
+  const int d = threadIdx.x & (TI - 1), i2_0 = threadIdx.x >> log_ti;
+  const int di = kThreads >> log_ti;
+  uint32_t* wd = work + d * rs;
+  {
+    const uint32_t* src = x + (c << log_k) + i1_0 + d + ((int64_t)i2_0 << log_k1);
+    const int64_t sstep = (int64_t)di << log_k1;
+    for (int i2 = i2_0; i2 < k2; i2 += di, src += sstep) cp_async4(wd + pad(i2), src);
   }
   const uint32_t gs = mmul<F>(h, s ? omega_pow<F>(log_n, (uint32_t)s) : F::ONE);
   const uint32_t G = mpow<F>(gs, (uint64_t)k1);
-  pow_table<F>(tw, k2 > 1 ? k2 / 2 : 1, log_k2 ? omega_pow<F>(log_k2, 1) : F::ONE);
+  root_table<F>(tw, k2 > 1 ? k2 / 2 : 1, log_k2);
   pow_table<F>(R, k2, G);
   for (int i = threadIdx.x; i < TI; i += blockDim.x) gi[i] = mpow<F>(gs, (uint64_t)(i1_0 + i));
   __syncthreads();
   cp_async_wait_all();
-  for (int idx = threadIdx.x; idx < (TI << log_k2); idx += blockDim.x) {
-    const int d = idx & (TI - 1), i2 = idx >> log_ti;
-    uint32_t* slot = work + d * rs + pad(i2);
-    *slot = snorm<F>(smul<F>(smul<F>((int32_t)*slot, (int32_t)gi[d]), (int32_t)R[i2]));
+  {  // each thread scales the words it loaded itself (no barrier needed)
+    const int32_t gd = (int32_t)gi[d];
+    for (int i2 = i2_0; i2 < k2; i2 += di) {
+      uint32_t* slot = wd + pad(i2);
+      *slot = snorm<F>(smul<F>(smul<F>((int32_t)*slot, gd), (int32_t)R[i2]));
+    }
   }
   __syncthreads();
   smem_ntt_dif<F>(work, log_ti, log_k2, rs, tw);
-  uint32_t* zc_ = z + ((c << log_b) + s) * ((int64_t)1 << log_k);
-  for (int idx = threadIdx.x; idx < (TI << log_k2); idx += blockDim.x) {
-    const int d = idx & (TI - 1), p = idx >> log_ti;
-    zc_[((int64_t)brev(p, log_k2) << log_k1) + i1_0 + d] = work[d * rs + pad(p)];
-  }
+  uint32_t* zd = z + ((c << log_b) + s) * ((int64_t)1 << log_k) + i1_0 + d;
+  for (int p = i2_0; p < k2; p += di) zd[(int64_t)brev(p, log_k2) << log_k1] = wd[pad(p)];
 }
 
 template <class F>
@@ -303,48 +317,69 @@ __device__ void lde_pass2_body(const uint32_t* z, uint32_t* out, int log_k1, int
   uint32_t* hi = lo + TT * lo_n;
   const int t2_0 = tile * TT;
   const uint32_t* zc_ = z + (c << log_n);
-  for (int idx = threadIdx.x; idx < (1 << (log_rows + log_k1)); idx += blockDim.x) {
-    const int i1 = idx & (k1 - 1), row = idx >> log_k1;
+  // Row-major tile: thread t owns position i1 = t mod k1 of rows t / k1,
+  // + kThreads / k1, ... when k1 <= kThreads, else positions t, t +
+  // kThreads, ... of every row (both powers of two); row bases are computed
+  // once per row, not per word.
+  const int i1_0 = threadIdx.x & (k1 - 1);
+  const int r_0 = k1 >= kThreads ? 0 : threadIdx.x >> log_k1;
+  const int r_step = k1 >= kThreads ? 1 : kThreads >> log_k1;
+  const int i1_step = k1 >= kThreads ? kThreads : k1;
+  const int rows = 1 << log_rows;
+  for (int row = r_0; row < rows; row += r_step) {
     const int s = row >> log_tt, dt = row & (TT - 1);
-    cp_async4(work + row * rs + pad(i1),
-              zc_ + ((int64_t)s << log_k) + ((int64_t)(t2_0 + dt) << log_k1) + i1);
+    uint32_t* wr = work + row * rs;
+    const uint32_t* zr = zc_ + ((int64_t)s << log_k) + ((int64_t)(t2_0 + dt) << log_k1);
+    for (int i1 = i1_0; i1 < k1; i1 += i1_step) cp_async4(wr + pad(i1), zr + i1);
   }
-  pow_table<F>(tw, k1 > 1 ? k1 / 2 : 1, log_k1 ? omega_pow<F>(log_k1, 1) : F::ONE);
-  for (int e = threadIdx.x; e < TT * (lo_n + hi_n); e += blockDim.x) {
-    const int dt = e / (lo_n + hi_n), r = e - dt * (lo_n + hi_n);
-    const uint32_t base = omega_pow<F>(log_k, (uint32_t)(t2_0 + dt));
-    if (r < lo_n)
-      lo[dt * lo_n + r] = mpow<F>(base, (uint64_t)r);
-    else
-      hi[dt * hi_n + (r - lo_n)] = mpow<F>(base, (uint64_t)(r - lo_n) << kTwLoLog);
+  root_table<F>(tw, k1 > 1 ? k1 / 2 : 1, log_k1);
+  {  // lo[dt][r] = w_k^((t2_0+dt) r), hi[dt][r] = w_k^((t2_0+dt) 64 r), straight off the roots
+    const uint32_t kmask = (1u << log_k) - 1;
+    for (int e = threadIdx.x; e < TT * (lo_n + hi_n); e += blockDim.x) {
+      const int dt = e / (lo_n + hi_n), r = e - dt * (lo_n + hi_n);
+      const uint32_t t2 = (uint32_t)(t2_0 + dt);
+      if (r < lo_n)
+        lo[dt * lo_n + r] = omega_pow<F>(log_k, (t2 * (uint32_t)r) & kmask);
+      else
+        hi[dt * hi_n + (r - lo_n)] =
+            omega_pow<F>(log_k, (t2 * ((uint32_t)(r - lo_n) << kTwLoLog)) & kmask);
+    }
   }
   __syncthreads();
   cp_async_wait_all();
-  for (int idx = threadIdx.x; idx < (1 << (log_rows + log_k1)); idx += blockDim.x) {
-    const int i1 = idx & (k1 - 1), row = idx >> log_k1;
+  for (int row = r_0; row < rows; row += r_step) {  // the words this thread loaded
     const int dt = row & (TT - 1);
-    uint32_t* slot = work + row * rs + pad(i1);
-    *slot = snorm<F>(smul<F>((int32_t)*slot,
-                             smul<F>((int32_t)lo[dt * lo_n + (i1 & (lo_n - 1))],
-                                     (int32_t)hi[dt * hi_n + (i1 >> kTwLoLog)])));
+    uint32_t* wr = work + row * rs;
+    const uint32_t* lr = lo + dt * lo_n;
+    const uint32_t* hr = hi + dt * hi_n;
+    for (int i1 = i1_0; i1 < k1; i1 += i1_step) {
+      uint32_t* slot = wr + pad(i1);
+      *slot = snorm<F>(smul<F>((int32_t)*slot, smul<F>((int32_t)lr[i1 & (lo_n - 1)],
+                                                       (int32_t)hr[i1 >> kTwLoLog])));
+    }
   }
   __syncthreads();
   smem_ntt_dif<F>(work, log_rows, log_k1, rs, tw);
   uint32_t* oc = out + (c << log_n);
-  if (brev_out) {
-    for (int idx = threadIdx.x; idx < (1 << (log_rows + log_k1)); idx += blockDim.x) {
-      const int p = idx & (k1 - 1), row = idx >> log_k1;
+  if (brev_out) {  // row (s, t2) -> the k1 contiguous words at brev_b(s) k + brev_k2(t2) k1
+    for (int row = r_0; row < rows; row += r_step) {
       const int s = row >> log_tt, dt = row & (TT - 1);
-      oc[((int64_t)brev(s, log_b) << log_k) + ((int64_t)brev(t2_0 + dt, log_k2) << log_k1) + p] =
-          work[row * rs + pad(p)];
+      const uint32_t* wr = work + row * rs;
+      uint32_t* orow = oc + ((int64_t)brev(s, log_b) << log_k) +
+                       ((int64_t)brev(t2_0 + dt, log_k2) << log_k1);
+      for (int p = i1_0; p < k1; p += i1_step) orow[p] = wr[pad(p)];
     }
     return;
   }
-  for (int idx = threadIdx.x; idx < (1 << (log_rows + log_k1)); idx += blockDim.x) {
-    const int s = idx & ((1 << log_b) - 1), dt = (idx >> log_b) & (TT - 1);
-    const int p = idx >> (log_b + log_tt);
-    const uint32_t v = work[((s << log_tt) + dt) * rs + pad(p)];
-    oc[((int64_t)(t2_0 + dt + ((int64_t)brev(p, log_k1) << log_k2)) << log_b) + s] = v;
+  {  // out[b (t2 + k2 t1) + s]: thread t owns row (s, dt) = t mod rows and walks
+     // the positions p = t / rows, + kThreads / rows, ... (rows <= kThreads)
+    const int ri = threadIdx.x & (rows - 1);
+    const int s = ri & ((1 << log_b) - 1), dt = ri >> log_b;
+    const uint32_t* wr = work + ((s << log_tt) + dt) * rs;
+    uint32_t* ob = oc + ((int64_t)(t2_0 + dt) << log_b) + s;
+    const int sh = log_k2 + log_b;
+    for (int p = threadIdx.x >> log_rows; p < k1; p += kThreads >> log_rows)
+      ob[(int64_t)brev(p, log_k1) << sh] = wr[pad(p)];
   }
 }
 
