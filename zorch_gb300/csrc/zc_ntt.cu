@@ -240,7 +240,7 @@ __global__ void __launch_bounds__(kThreads, 2) k_lde_small(const uint32_t* x, ui
 // Pass 1 item (coset s, i1 tile, column c): the k2-point DIF NTTs down the
 // strided columns i1 of the message scaled by g_s^(i1 + k1 i2); writes the
 // untwiddled intermediate z[c][s][t2][i1] (t2 = bit-reversed position).
-// Layout: work[TI][rs] | tw[k2/2] | R[k2] | gi[TI].
+// Layout: work[TI][rs] | tw[k2/2] | gi[TI].
 template <class F>
 __device__ void lde_pass1_body(const uint32_t* x, uint32_t* z, int log_k1, int log_k2, int log_b,
                                int log_ti, uint32_t h, int s, int tile, int64_t c,
@@ -250,8 +250,7 @@ __device__ void lde_pass1_body(const uint32_t* x, uint32_t* z, int log_k1, int l
   const int rs = row_stride(k2);
   uint32_t* work = sm;
   uint32_t* tw = work + TI * rs;
-  uint32_t* R = tw + (k2 > 1 ? k2 / 2 : 1);
-  uint32_t* gi = R + k2;
+  uint32_t* gi = tw + (k2 > 1 ? k2 / 2 : 1);
   const int i1_0 = tile * TI;
   // Thread t always owns column d = t mod TI (TI <= kThreads, both powers of
   // two) and walks i2 = t / TI, + kThreads / TI, ...: the column offsets are
@@ -267,15 +266,18 @@ __device__ void lde_pass1_body(const uint32_t* x, uint32_t* z, int log_k1, int l
   const uint32_t gs = mmul<F>(h, s ? omega_pow<F>(log_n, (uint32_t)s) : F::ONE);
   const uint32_t G = mpow<F>(gs, (uint64_t)k1);
   root_table<F>(tw, k2 > 1 ? k2 / 2 : 1, log_k2);
-  pow_table<F>(R, k2, G);
   for (int i = threadIdx.x; i < TI; i += blockDim.x) gi[i] = mpow<F>(gs, (uint64_t)(i1_0 + i));
+  // word (d, i2) is scaled by gs^(i1_0 + d + k1 i2) = gi[d] G^i2: a running
+  // product per thread, G^i2_0 then times G^di per step (no table, no barriers)
+  const uint32_t g_first = mpow<F>(G, (uint64_t)i2_0), g_step = mpow<F>(G, (uint64_t)di);
   __syncthreads();
   cp_async_wait_all();
   {  // each thread scales the words it loaded itself (no barrier needed)
-    const int32_t gd = (int32_t)gi[d];
+    int32_t fac = smul<F>((int32_t)gi[d], (int32_t)g_first);
     for (int i2 = i2_0; i2 < k2; i2 += di) {
       uint32_t* slot = wd + pad(i2);
-      *slot = snorm<F>(smul<F>(smul<F>((int32_t)*slot, gd), (int32_t)R[i2]));
+      *slot = snorm<F>(smul<F>((int32_t)*slot, fac));
+      fac = smul<F>(fac, (int32_t)g_step);
     }
   }
   __syncthreads();
@@ -419,7 +421,7 @@ inline LdePlan plan_lde(int log_k, int log_b, int tile_log = 0) {
   if (tt < 0) tt = 0;
   p.log_tt = tt;
   const int k1 = 1 << p.log_k1, k2 = 1 << p.log_k2;
-  p.smem1 = 4 * ((size_t)(1 << p.log_ti) * row_stride(k2) + (k2 > 1 ? k2 / 2 : 1) + k2 +
+  p.smem1 = 4 * ((size_t)(1 << p.log_ti) * row_stride(k2) + (k2 > 1 ? k2 / 2 : 1) +
                  (1 << p.log_ti));
   const int lo_n = k1 < (1 << kTwLoLog) ? k1 : (1 << kTwLoLog);
   const int hi_n = (k1 >> kTwLoLog) > 0 ? (k1 >> kTwLoLog) : 1;
