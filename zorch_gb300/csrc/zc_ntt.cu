@@ -168,6 +168,7 @@ __device__ void smem_ntt_dif(uint32_t* a, int log_rows, int logm, int rs, const 
 }
 
 constexpr int kThreads = 512;
+constexpr int kLogThreads = 9;
 
 // Asynchronous 4-byte global -> shared copies (cp.async): a tile's loads are
 // all in flight at once, overlapping the twiddle-table set-up, instead of one
@@ -283,7 +284,7 @@ __device__ void lde_pass1_body(const uint32_t* x, uint32_t* z, int log_k1, int l
   __syncthreads();
   smem_ntt_dif<F>(work, log_ti, log_k2, rs, tw);
   uint32_t* zd = z + ((c << log_b) + s) * ((int64_t)1 << log_k) + i1_0 + d;
-  for (int p = i2_0; p < k2; p += di) zd[(int64_t)brev(p, log_k2) << log_k1] = wd[pad(p)];
+  for (int p = i2_0; p < k2; p += di) zd[(uint32_t)brev(p, log_k2) << log_k1] = wd[pad(p)];
 }
 
 template <class F>
@@ -295,14 +296,12 @@ __global__ void __launch_bounds__(kThreads, 2) k_lde_pass1(const uint32_t* x, ui
                     sm);
 }
 
-constexpr int kTwLoLog = 6;  // pass-2 twiddle tables: w^(t2 i1) = lo[i1 & 63] * hi[i1 >> 6]
-
 // Pass 2 item (t2 tile, column c): rows (s, t2) for all b cosets and TT
 // values of t2; each row is multiplied by w_k^(t2 i1), transformed by a
 // k1-point DIF NTT, and written to out[b (t2 + k2 t1) + s] (t1 = bit-reversed
 // position) in contiguous runs of b*TT words -- or, for a bit-reversed
 // codeword, row (s, t2) to the k1 contiguous words at brev_b(s) k + brev_k2(t2) k1.
-// Layout: work[b*TT][rs] | tw[k1/2] | lo[TT][64] | hi[TT][k1/64].
+// Layout: work[b*TT][rs] | tw[k1/2].
 template <class F>
 __device__ void lde_pass2_body(const uint32_t* z, uint32_t* out, int log_k1, int log_k2,
                                int log_b, int log_tt, int tile, int64_t c, uint32_t* sm,
@@ -311,66 +310,57 @@ __device__ void lde_pass2_body(const uint32_t* z, uint32_t* out, int log_k1, int
   const int log_k = log_k1 + log_k2, log_n = log_k + log_b;
   const int log_rows = log_b + log_tt;
   const int rs = row_stride(k1);
-  const int lo_n = k1 < (1 << kTwLoLog) ? k1 : (1 << kTwLoLog);
-  const int hi_n = k1 >> kTwLoLog > 0 ? k1 >> kTwLoLog : 1;
   uint32_t* work = sm;
   uint32_t* tw = work + (rs << log_rows);
-  uint32_t* lo = tw + (k1 > 1 ? k1 / 2 : 1);
-  uint32_t* hi = lo + TT * lo_n;
   const int t2_0 = tile * TT;
   const uint32_t* zc_ = z + (c << log_n);
-  // Row-major tile: thread t owns position i1 = t mod k1 of rows t / k1,
-  // + kThreads / k1, ... when k1 <= kThreads, else positions t, t +
-  // kThreads, ... of every row (both powers of two); row bases are computed
-  // once per row, not per word.
-  const int i1_0 = threadIdx.x & (k1 - 1);
-  const int r_0 = k1 >= kThreads ? 0 : threadIdx.x >> log_k1;
-  const int r_step = k1 >= kThreads ? 1 : kThreads >> log_k1;
-  const int i1_step = k1 >= kThreads ? kThreads : k1;
-  const int rows = 1 << log_rows;
-  for (int row = r_0; row < rows; row += r_step) {
-    const int s = row >> log_tt, dt = row & (TT - 1);
-    uint32_t* wr = work + row * rs;
-    const uint32_t* zr = zc_ + ((int64_t)s << log_k) + ((int64_t)(t2_0 + dt) << log_k1);
-    for (int i1 = i1_0; i1 < k1; i1 += i1_step) cp_async4(wr + pad(i1), zr + i1);
-  }
-  root_table<F>(tw, k1 > 1 ? k1 / 2 : 1, log_k1);
-  {  // lo[dt][r] = w_k^((t2_0+dt) r), hi[dt][r] = w_k^((t2_0+dt) 64 r), straight off the roots
-    const uint32_t kmask = (1u << log_k) - 1;
-    for (int e = threadIdx.x; e < TT * (lo_n + hi_n); e += blockDim.x) {
-      const int dt = e / (lo_n + hi_n), r = e - dt * (lo_n + hi_n);
-      const uint32_t t2 = (uint32_t)(t2_0 + dt);
-      if (r < lo_n)
-        lo[dt * lo_n + r] = omega_pow<F>(log_k, (t2 * (uint32_t)r) & kmask);
-      else
-        hi[dt * hi_n + (r - lo_n)] =
-            omega_pow<F>(log_k, (t2 * ((uint32_t)(r - lo_n) << kTwLoLog)) & kmask);
+  // Thread t owns positions i1 = t mod tpr, + tpr, ... (tpr = min(k1,
+  // kThreads) threads per row, consecutive threads on consecutive words) of
+  // rows dt = t / tpr, + dt_step, ... of every coset s; it loads and scales
+  // exactly these words, so the scale needs no barrier after the loads.
+  const int lt = log_k1 < kLogThreads ? log_k1 : kLogThreads;
+  const int tpr = 1 << lt;
+  const int i1_0 = threadIdx.x & (tpr - 1);
+  const int dt_0 = threadIdx.x >> lt, dt_step = kThreads >> lt;
+  const int b = 1 << log_b;
+  for (int i1 = i1_0; i1 < k1; i1 += tpr)
+    for (int s = 0; s < b; s++) {
+      uint32_t* wp = work + (s << log_tt) * rs + pad(i1);
+      const uint32_t* zp = zc_ + ((int64_t)s << log_k) + ((int64_t)t2_0 << log_k1) + i1;
+      for (int dt = dt_0; dt < TT; dt += dt_step)
+        cp_async4(wp + dt * rs, zp + ((uint32_t)dt << log_k1));
     }
-  }
+  root_table<F>(tw, k1 > 1 ? k1 / 2 : 1, log_k1);
+  // word (s, dt, i1) is scaled by w_k^((t2_0 + dt) i1), the same for every
+  // coset s: a running product over this thread's rows, stepping by
+  // w_k^(dt_step i1)
+  const uint32_t kmask = (1u << log_k) - 1;
   __syncthreads();
   cp_async_wait_all();
-  for (int row = r_0; row < rows; row += r_step) {  // the words this thread loaded
-    const int dt = row & (TT - 1);
-    uint32_t* wr = work + row * rs;
-    const uint32_t* lr = lo + dt * lo_n;
-    const uint32_t* hr = hi + dt * hi_n;
-    for (int i1 = i1_0; i1 < k1; i1 += i1_step) {
-      uint32_t* slot = wr + pad(i1);
-      *slot = snorm<F>(smul<F>((int32_t)*slot, smul<F>((int32_t)lr[i1 & (lo_n - 1)],
-                                                       (int32_t)hr[i1 >> kTwLoLog])));
+  for (int i1 = i1_0; i1 < k1; i1 += tpr) {
+    int32_t fac = (int32_t)omega_pow<F>(log_k, ((uint32_t)(t2_0 + dt_0) * (uint32_t)i1) & kmask);
+    const int32_t step = (int32_t)omega_pow<F>(log_k, ((uint32_t)dt_step * (uint32_t)i1) & kmask);
+    for (int dt = dt_0; dt < TT; dt += dt_step) {
+      uint32_t* wp = work + dt * rs + pad(i1);
+      for (int s = 0; s < b; s++) {
+        uint32_t* slot = wp + (s << log_tt) * rs;
+        *slot = snorm<F>(smul<F>((int32_t)*slot, fac));
+      }
+      fac = smul<F>(fac, step);
     }
   }
   __syncthreads();
   smem_ntt_dif<F>(work, log_rows, log_k1, rs, tw);
   uint32_t* oc = out + (c << log_n);
+  const int rows = 1 << log_rows;
   if (brev_out) {  // row (s, t2) -> the k1 contiguous words at brev_b(s) k + brev_k2(t2) k1
-    for (int row = r_0; row < rows; row += r_step) {
-      const int s = row >> log_tt, dt = row & (TT - 1);
-      const uint32_t* wr = work + row * rs;
-      uint32_t* orow = oc + ((int64_t)brev(s, log_b) << log_k) +
-                       ((int64_t)brev(t2_0 + dt, log_k2) << log_k1);
-      for (int p = i1_0; p < k1; p += i1_step) orow[p] = wr[pad(p)];
-    }
+    for (int s = 0; s < b; s++)
+      for (int dt = dt_0; dt < TT; dt += dt_step) {
+        const uint32_t* wr = work + ((s << log_tt) + dt) * rs;
+        uint32_t* orow = oc + ((int64_t)brev(s, log_b) << log_k) +
+                         ((int64_t)brev(t2_0 + dt, log_k2) << log_k1);
+        for (int p = i1_0; p < k1; p += tpr) orow[p] = wr[pad(p)];
+      }
     return;
   }
   {  // out[b (t2 + k2 t1) + s]: thread t owns row (s, dt) = t mod rows and walks
@@ -381,7 +371,7 @@ __device__ void lde_pass2_body(const uint32_t* z, uint32_t* out, int log_k1, int
     uint32_t* ob = oc + ((int64_t)(t2_0 + dt) << log_b) + s;
     const int sh = log_k2 + log_b;
     for (int p = threadIdx.x >> log_rows; p < k1; p += kThreads >> log_rows)
-      ob[(int64_t)brev(p, log_k1) << sh] = wr[pad(p)];
+      ob[(uint32_t)brev(p, log_k1) << sh] = wr[pad(p)];  // offset < n <= 2^30
   }
 }
 
@@ -423,10 +413,7 @@ inline LdePlan plan_lde(int log_k, int log_b, int tile_log = 0) {
   const int k1 = 1 << p.log_k1, k2 = 1 << p.log_k2;
   p.smem1 = 4 * ((size_t)(1 << p.log_ti) * row_stride(k2) + (k2 > 1 ? k2 / 2 : 1) +
                  (1 << p.log_ti));
-  const int lo_n = k1 < (1 << kTwLoLog) ? k1 : (1 << kTwLoLog);
-  const int hi_n = (k1 >> kTwLoLog) > 0 ? (k1 >> kTwLoLog) : 1;
-  p.smem2 = 4 * ((size_t)(b << p.log_tt) * row_stride(k1) + (k1 > 1 ? k1 / 2 : 1) +
-                 ((size_t)1 << p.log_tt) * (lo_n + hi_n));
+  p.smem2 = 4 * ((size_t)(b << p.log_tt) * row_stride(k1) + (k1 > 1 ? k1 / 2 : 1));
   return p;
 }
 
