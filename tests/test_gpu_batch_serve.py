@@ -135,6 +135,24 @@ def test_served_results_same_alone_and_in_the_mix():
         assert len(m.proof) > 32 if r.fold else len(m.proof) == 32
 
 
+def test_served_host_fed_equals_resident():
+    """Inputs fed from page-locked host memory (copy-engine copies on side
+    streams, then the in-place conversion) give the same proofs as inputs
+    already on the device; likewise for the plain path."""
+    from zorch_gb300.serve import Server, run_plain
+
+    reqs = _small_stream(13)
+    for r in reqs:
+        r.host = r.resident.cpu().pin_memory()
+    server = Server(max_batch=4, streams=3)
+    resident = server.run(reqs)
+    fed = server.run(reqs, host_fed=True)
+    assert [a.proof for a in resident] == [b.proof for b in fed]
+    plain_fed = run_plain(reqs, host_fed=True, perm=server.perm)
+    plain = run_plain(reqs, perm=server.perm)
+    assert [a.proof for a in plain] == [b.proof for b in plain_fed]
+
+
 def test_served_fold_proofs_match_oracle(orc):
     """Root of the row-leaf tree and the fold-and-open proof bytes of a served
     request equal the oracle's, replayed from the same seeded data."""
