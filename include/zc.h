@@ -90,6 +90,13 @@ zc_status zc_scale(zc_field field, const uint32_t* in, uint32_t* out, int64_t n,
  * link instead of a staging copy: no counterpart in the reference (its
  * inputs arrive as device arrays). ZC_BAD_ARG if `host` is not page-locked. */
 zc_status zc_host_device_ptr(const void* host, void** dev);
+/* Canonical -> Montgomery of n words read straight from page-locked host
+ * memory `host` (the conversion kernel's loads cross the host link; no
+ * staging copy), into device `out`, on at most max_ctas CTAs of 1024 threads
+ * (<= 0: the library default, 64) so that the SMs it leaves free keep
+ * running other streams. ZC_BAD_ARG if `host` is not page-locked. */
+zc_status zc_to_mont_from_host(zc_field field, const void* host, uint32_t* out, int64_t n,
+                               int32_t max_ctas, void* stream);
 
 /* ---- Poseidon2 parameters -------------------------------------------- */
 /* The built-in BabyBear width-16 instance (x^7, 4+4 full, 13 partial rounds).

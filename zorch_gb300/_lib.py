@@ -58,6 +58,7 @@ def _declare(lib: C.CDLL) -> None:
         "zc_init": (st, [C.c_int]),
         "zc_to_mont": (st, [st, vp, vp, i64, vp]),
         "zc_host_device_ptr": (st, [vp, C.POINTER(vp)]),
+        "zc_to_mont_from_host": (st, [st, vp, vp, i64, i32, vp]),
         "zc_from_mont": (st, [st, vp, vp, i64, vp]),
         "zc_scale": (st, [st, vp, vp, i64, u32, vp]),
         "zc_poseidon2_builtin": (st, [st, C.POINTER(vp)]),

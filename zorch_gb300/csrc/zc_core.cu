@@ -416,6 +416,9 @@ zc_status zc_poseidon2_permute(const zc_poseidon2* p, uint32_t* states, int64_t 
   });
 }
 
+// CTAs of 1024 threads for a conversion that reads page-locked host memory.
+constexpr int64_t kHostReadCtas = 64;
+
 static zc_status convert(zc_field field, const uint32_t* in, uint32_t* out, int64_t n, int to,
                          void* stream) {
   if (!in || !out || n < 0) return ZC_BAD_ARG;
@@ -426,6 +429,25 @@ static zc_status convert(zc_field field, const uint32_t* in, uint32_t* out, int6
     int64_t blocks = (n + 255) / 256;
     if (blocks > 152 * 16) blocks = 152 * 16;
     k_convert<F><<<(unsigned)blocks, 256, 0, st>>>(in, out, n, to);
+    return launch_check();
+  });
+}
+
+zc_status zc_to_mont_from_host(zc_field field, const void* host, uint32_t* out, int64_t n,
+                               int32_t max_ctas, void* stream) {
+  if (!host || !out || n < 0) return ZC_BAD_ARG;
+  if (n == 0) return ZC_OK;
+  void* src = nullptr;
+  ZC_TRY(zc_host_device_ptr(host, &src));
+  cudaStream_t st = (cudaStream_t)stream;
+  // a bounded number of CTAs: the host link, not the SM count, limits this
+  // kernel, and the SMs it leaves free keep running the other streams' work
+  const int64_t cap = max_ctas > 0 ? max_ctas : kHostReadCtas;
+  return with_field(field, [&](auto f) {
+    using F = decltype(f);
+    int64_t blocks = (n + 1023) / 1024;
+    if (blocks > cap) blocks = cap;
+    k_convert<F><<<(unsigned)blocks, 1024, 0, st>>>(static_cast<const uint32_t*>(src), out, n, 1);
     return launch_check();
   });
 }

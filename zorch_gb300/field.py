@@ -154,23 +154,21 @@ def to_mont(field, t: torch.Tensor, out: torch.Tensor | None = None) -> torch.Te
 
 
 def to_mont_from_host(field, host: torch.Tensor, out: torch.Tensor | None = None,
-                      device="cuda") -> torch.Tensor:
+                      device="cuda", max_ctas: int = 0) -> torch.Tensor:
     """Canonical page-locked host words -> Montgomery device words in one
     kernel that reads the host buffer directly over the host link
-    (zc_host_device_ptr + zc_to_mont): no staging copy through the copy
-    engine. `host` must be pinned (ValueError otherwise)."""
-    import ctypes as C
-
+    (zc_to_mont_from_host): no staging copy through the copy engine, and a
+    bounded number of CTAs (max_ctas, 0 = the library default) so the
+    kernels of other streams keep most SMs. `host` must be pinned
+    (ValueError otherwise)."""
     f = field_of(field)
     if host.device.type != "cpu" or not host.is_pinned():
         raise ValueError("to_mont_from_host needs a page-locked (pinned) host tensor")
     src = host.contiguous()
     if out is None:
         out = torch.empty(src.shape, dtype=torch.int32, device=device)
-    dp = C.c_void_p()
-    _lib.check(_lib.lib().zc_host_device_ptr(src.data_ptr(), C.byref(dp)), "host_device_ptr")
-    _lib.check(_lib.lib().zc_to_mont(f.id, dp.value, ptr(out), src.numel(), stream_handle()),
-               "to_mont")
+    _lib.check(_lib.lib().zc_to_mont_from_host(f.id, src.data_ptr(), ptr(out), src.numel(),
+                                               max_ctas, stream_handle()), "to_mont_from_host")
     return out
 
 
