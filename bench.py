@@ -60,8 +60,8 @@ def parse():
     ap.add_argument("--min-log-h", type=int, default=14)
     ap.add_argument("--max-log-h", type=int, default=24)
     ap.add_argument("--budget-gb", type=float, default=150.0)
-    ap.add_argument("--max-batch", type=int, default=32)
-    ap.add_argument("--streams", type=int, default=3)
+    ap.add_argument("--max-batch", type=int, default=8)
+    ap.add_argument("--streams", type=int, default=4)
     return ap.parse_args()
 
 
