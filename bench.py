@@ -408,15 +408,12 @@ def paths_workload(args, device):
     CPU-baseline leg), with the two outputs compared. GPU times are wall time
     per call with a device synchronize on both sides, mean over --steps calls
     after warm-up; the oracle runs once per path."""
-    import json as _json
-
     import torch
 
-    from zorch_gb300 import _lib
     from zorch_gb300.coding import BitReversedReedSolomon, ReedSolomon
     from zorch_gb300.commit import (MerkleTree, Poseidon2, SingleMatrixCommitmentScheme,
                                     StridedMerkleTree)
-    from zorch_gb300.field import BABYBEAR, KOALABEAR, ptr, stream_handle, to_device, to_host
+    from zorch_gb300.field import BABYBEAR, KOALABEAR, to_device, to_host
     from zorch_gb300.jagged import stacked_basefold_open, stacked_commit
     from zorch_gb300.pcs import BasefoldProver, FoldState, PreFoldKGroupCommitRound, fold_rounds
     from zorch_gb300.transcript import DuplexTranscript
@@ -450,12 +447,12 @@ def paths_workload(args, device):
 
     rows = {}
     bb = Poseidon2.builtin(BABYBEAR)
-    sp1d = _json.loads(open(os.path.join(ROOT, "tests", "golden", "sp1_fibonacci",
-                                         "sp1_koalabear16.json")).read())
+    sp1d = json.loads(open(os.path.join(ROOT, "tests", "golden", "sp1_fibonacci",
+                                        "sp1_koalabear16.json")).read())
     sp1 = Poseidon2.from_params(KOALABEAR, sp1d["alpha"], sp1d["external_initial"],
                                 sp1d["external_terminal"], sp1d["internal_rc"],
                                 sp1d["internal_diag"], sp1d["internal_j_scale"])
-    kb = _json.loads(open(os.path.join(ROOT, "tests", "golden", "koalabear16.json")).read())
+    kb = json.loads(open(os.path.join(ROOT, "tests", "golden", "koalabear16.json")).read())
     kbp = Poseidon2.from_params(KOALABEAR, kb["alpha"], kb["external_initial"],
                                 kb["external_terminal"], kb["internal_rc"], kb["internal_diag"],
                                 kb.get("internal_j_scale", 1))
