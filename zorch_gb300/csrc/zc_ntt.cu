@@ -117,24 +117,31 @@ __device__ __forceinline__ void dif_pass(uint32_t* a, int log_rows, int logm, in
   const int glog = logm - R;
   const int total = 1 << (log_rows + glog);
   const int rmask = (1 << log_rows) - 1;
+  // Stage r of this pass reads the twiddle tw[pos << (sh0 + r)].
+  const int sh0 = logm - 1 - h0;
   for (int gi = threadIdx.x; gi < total; gi += blockDim.x) {
     const int row = gi & rmask, g = gi >> log_rows;
     const int off = g & ((1 << lS) - 1), blk = g >> lS;
     const int base = (blk << (h0 + 1)) | off;
-    uint32_t* ar = a + row * rs;
+    // Member j sits at pad(base + j S) = pad(base) + pad(j S): base's low five
+    // bits plus j S never carry past a 32-word boundary that j S does not
+    // itself cross (off < S, and the group spans 2^(h0+1) aligned words), so
+    // the member offsets are the same for every group of the pass.
+    uint32_t* ar = a + row * rs + pad(base);
     uint32_t v[G];
 #pragma unroll
-    for (int j = 0; j < G; j++) v[j] = ar[pad(base + (j << lS))];
+    for (int j = 0; j < G; j++) v[j] = ar[pad(j << lS)];
 #pragma unroll
     for (int r = 0; r < R; r++) {
       const int hb = R - 1 - r;  // local bit of this stage
-      const int H = h0 - r;      // log2 of the half size
+      // pos = off + jm S with jm = j mod 2^hb: index = (off << sh) + jm (S << sh)
+      const int sh = sh0 + r;
+      const int tb = off << sh, ts = 1 << (lS + sh);
 #pragma unroll
       for (int j = 0; j < G; j++) {
         if (!(j & (1 << hb))) {
           const int j2 = j | (1 << hb);
-          const int pos = off + ((j & ((1 << hb) - 1)) << lS);
-          const uint32_t w = tw[pos << (logm - 1 - H)];
+          const uint32_t w = tw[tb + (j & ((1 << hb) - 1)) * ts];
           const uint32_t u = v[j], t = v[j2];
           v[j] = madd<F>(u, t);
           // u - t in (-p, p) feeds the signed product directly
@@ -143,7 +150,7 @@ __device__ __forceinline__ void dif_pass(uint32_t* a, int log_rows, int logm, in
       }
     }
 #pragma unroll
-    for (int j = 0; j < G; j++) ar[pad(base + (j << lS))] = v[j];
+    for (int j = 0; j < G; j++) ar[pad(j << lS)] = v[j];
   }
 }
 
