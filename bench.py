@@ -279,7 +279,7 @@ def served_workload(args, device, rank):
     one-call-per-polynomial path."""
     import torch
 
-    from zorch_gb300.batch import Autotuner
+    from zorch_gb300.batch import Autotuner, _bucket
     from zorch_gb300.serve import Server, fill_request, make_stream, run_plain
 
     reqs = make_stream(args.requests, args.seed, rate_hz=args.rate, log_h=(args.min_log_h,
@@ -287,8 +287,17 @@ def served_workload(args, device, rank):
     for r in reqs:
         fill_request(r, device)
     torch.cuda.synchronize()
+    # autotune every (log_n, log2 width) bucket of the stream not yet cached:
+    # LDE tile and radix, tree-top depth (untimed set-up, kept in the cache)
+    tuner = Autotuner()
+    for r in reqs:
+        if _bucket(r.log_n, r.width) not in tuner.table:
+            cols = r.resident[:min(r.width, 8)]
+            tuner.tune(r.log_h, cols.shape[0], r.log_blowup, reps=2, columns=cols,
+                       bucket_width=r.width)
+    tuner.save()
     server = Server(budget_bytes=args.budget_gb * 1e9, max_batch=args.max_batch,
-                    streams=args.streams, tuner=Autotuner())
+                    streams=args.streams, tuner=tuner)
     elements = sum(r.elements for r in reqs)
 
     def served(host_fed=False):

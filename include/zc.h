@@ -178,6 +178,7 @@ typedef struct {
   uint32_t shift_mont;    /* 0: no coset */
   int32_t tile_log;       /* 0: default */
   int32_t bit_reversed;   /* 1: bit-reversed codeword (zc_rs_encode_bitrev) */
+  int32_t radix_log;      /* largest radix-2^r shared-memory pass, 2..4; 0: default 4 */
 } zc_lde_job;
 size_t zc_rs_encode_batch_workspace_bytes(const zc_lde_job* jobs, int32_t njobs);
 zc_status zc_rs_encode_batch(zc_field field, const zc_lde_job* jobs, int32_t njobs,
@@ -215,6 +216,8 @@ zc_status zc_merkle_open(zc_leaves leaves, const uint32_t* layers, const int32_t
 typedef struct {
   zc_leaves leaves;
   uint32_t* layers; /* (2L-1)*8 words */
+  int32_t top_log;  /* the levels of <= 2^top_log nodes run fused in one CTA per
+                       tree (half-warp permutations), 1..8; 0: default 8 */
 } zc_merkle_job;
 zc_status zc_merkle_commit_batch(const zc_poseidon2* p, const zc_merkle_job* jobs,
                                  int32_t njobs, void* workspace, size_t workspace_bytes,

@@ -105,11 +105,29 @@ def test_autotuner_choice_keeps_bytes(tmp_path):
     tl = tuner.tune(14, 8, 2)
     assert tl in (13, 14, 15)
     tuner.save()
-    assert Autotuner(tmp_path / "tune.json").tile_log(16, 8) == tl
+    again = Autotuner(tmp_path / "tune.json")
+    assert again.tile_log(16, 8) == tl
+    c = again.choice(16, 8)
+    assert c["radix"] in (3, 4) and c["top"] in (6, 7, 8)
     mats = _mats(7)
     a = BatchCommitter(tuner=tuner).commit([MatrixJob(x, lb) for x, lb in mats])
     b = BatchCommitter().commit([MatrixJob(x, lb) for x, lb in mats])
     for x, y in zip(a, b):
+        assert torch.equal(x.layers.flat, y.layers.flat)
+
+
+@pytest.mark.parametrize("tile,radix,top", [(13, 2, 1), (15, 3, 4), (14, 4, 8), (0, 2, 6)])
+def test_tuning_choices_keep_bytes(tile, radix, top):
+    """Every tile, radix and tree-top depth the tuner may pick gives the same
+    codewords and digest layers as the defaults."""
+    from zorch_gb300.batch import BatchCommitter, MatrixJob
+
+    mats = _mats(11)
+    forced = BatchCommitter(tile_override=tile, radix_override=radix, top_override=top).commit(
+        [MatrixJob(x, lb) for x, lb in mats])
+    plain = BatchCommitter().commit([MatrixJob(x, lb) for x, lb in mats])
+    for x, y in zip(forced, plain):
+        assert torch.equal(x.codeword, y.codeword)
         assert torch.equal(x.layers.flat, y.layers.flat)
 
 

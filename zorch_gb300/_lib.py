@@ -29,7 +29,7 @@ class ZcError(RuntimeError):
 class LdeJob(C.Structure):
     _fields_ = [("coeffs", C.c_void_p), ("out", C.c_void_p), ("batch", C.c_int64),
                 ("log_k", C.c_int32), ("log_blowup", C.c_int32), ("shift_mont", C.c_uint32),
-                ("tile_log", C.c_int32), ("bit_reversed", C.c_int32)]
+                ("tile_log", C.c_int32), ("bit_reversed", C.c_int32), ("radix_log", C.c_int32)]
 
 
 class Leaves(C.Structure):
@@ -40,7 +40,7 @@ class Leaves(C.Structure):
 
 
 class MerkleJob(C.Structure):
-    _fields_ = [("leaves", Leaves), ("layers", C.c_void_p)]
+    _fields_ = [("leaves", Leaves), ("layers", C.c_void_p), ("top_log", C.c_int32)]
 
 
 _lock = threading.Lock()

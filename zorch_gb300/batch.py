@@ -8,8 +8,10 @@ exactly the root a per-matrix BasefoldProver.commit would produce
 (zorch/pcs/basefold/prover.py:437-455): batching changes launches, never bytes.
 
 `GraphedBatch` captures one batch composition into a CUDA graph and replays
-it on new inputs of the same shapes. `Autotuner` picks the LDE shared-memory
-tile per (log_n, width) bucket by timing candidates and caches the choice.
+it on new inputs of the same shapes. `Autotuner` picks, per (log_n, log2
+width) bucket, the LDE shared-memory tile and largest NTT radix and the
+depth of the fused per-tree top (the hash subtree run in one CTA) by timing
+the candidates, and caches the choices as JSON. No choice changes a byte.
 """
 
 from __future__ import annotations
@@ -27,6 +29,8 @@ from .commit import DigestLayers, Poseidon2
 from .field import BABYBEAR, field_of, ptr, stream_handle
 
 _TILE_CANDIDATES = (13, 14, 15)
+_RADIX_CANDIDATES = (3, 4)
+_TOP_CANDIDATES = (6, 7, 8)
 
 
 @dataclass
@@ -68,72 +72,113 @@ def _bucket(log_n: int, width: int) -> str:
 
 
 class Autotuner:
-    """Per-(log_n, log2 width) choice of the LDE shared-memory tile, measured
-    with CUDA events on synthetic data and cached in a JSON file."""
+    """Per-(log_n, log2 width) choice of the LDE shared-memory tile (2^13..2^15
+    words), the largest radix-2^r NTT pass (r = 3, 4) and the fused tree-top
+    depth (the last 6..8 levels in one CTA per tree), measured with CUDA
+    events and cached in a JSON file."""
 
     def __init__(self, path: str | os.PathLike | None = None) -> None:
         default = Path(__file__).resolve().parent / "_build" / "autotune.json"
         self.path = Path(path or os.environ.get("ZC_AUTOTUNE_CACHE", default))
-        self.table: dict[str, int] = {}
+        self.table: dict[str, dict] = {}
         if self.path.exists():
             try:
-                self.table = json.loads(self.path.read_text())
-            except ValueError:
+                raw = json.loads(self.path.read_text())
+                # an entry is {"tile", "radix", "top"}; a bare int is a tile choice
+                self.table = {k: (v if isinstance(v, dict) else {"tile": int(v)})
+                              for k, v in raw.items()}
+            except (ValueError, TypeError):
                 self.table = {}
 
+    def choice(self, log_n: int, width: int) -> dict:
+        """{"tile", "radix", "top"} for the bucket; 0 means the library default."""
+        e = self.table.get(_bucket(log_n, width), {})
+        return {"tile": int(e.get("tile", 0)), "radix": int(e.get("radix", 0)),
+                "top": int(e.get("top", 0))}
+
     def tile_log(self, log_n: int, width: int) -> int:
-        return int(self.table.get(_bucket(log_n, width), 0))
+        return self.choice(log_n, width)["tile"]
 
     def save(self) -> None:
         self.path.parent.mkdir(parents=True, exist_ok=True)
         self.path.write_text(json.dumps(self.table, indent=1, sort_keys=True))
 
-    def tune(self, log_h: int, width: int, log_blowup: int, field=BABYBEAR, reps: int = 3) -> int:
-        """Time every candidate tile on a [width, 2^log_h] matrix; record the best."""
+    @staticmethod
+    def _time(fn, reps: int) -> float:
+        fn()
+        torch.cuda.synchronize()
+        s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        s.record()
+        for _ in range(reps):
+            fn()
+        e.record()
+        torch.cuda.synchronize()
+        return s.elapsed_time(e) / reps
+
+    def tune(self, log_h: int, width: int, log_blowup: int, field=BABYBEAR, reps: int = 3,
+             perm: Poseidon2 | None = None, columns: torch.Tensor | None = None,
+             bucket_width: int | None = None) -> int:
+        """Time every (tile, radix) LDE candidate and every tree-top depth on a
+        [width, 2^log_h] matrix (`columns`, or seeded data); record the best of
+        each for the bucket of (log_h + log_blowup, bucket_width or width) and
+        return the tile. All three choices act per column or per tree top, so
+        a few columns stand in for a wide matrix."""
         f = field_of(field)
-        cols = torch.empty((width, 1 << log_h), dtype=torch.int32, device="cuda")
-        _lib.check(_lib.lib().zc_fill_uniform(f.id, ptr(cols), cols.numel(), 7, stream_handle()),
-                   "fill")
-        best, best_ms = 0, float("inf")
+        cols = columns
+        if cols is None:
+            cols = torch.empty((width, 1 << log_h), dtype=torch.int32, device="cuda")
+            _lib.check(_lib.lib().zc_fill_uniform(f.id, ptr(cols), cols.numel(), 7,
+                                                  stream_handle()), "fill")
+        job = MatrixJob(cols, log_blowup)
+        best, best_ms = (0, 0), float("inf")
         for tl in _TILE_CANDIDATES:
-            bc = BatchCommitter(field=f, tuner=None, tile_override=tl)
-            job = MatrixJob(cols, log_blowup)
-            try:
-                bc.encode([job])
-            except (NotImplementedError, ValueError):
-                continue
-            torch.cuda.synchronize()
-            s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-            s.record()
-            for _ in range(reps):
-                bc.encode([job])
-            e.record()
-            torch.cuda.synchronize()
-            ms = s.elapsed_time(e) / reps
-            if ms < best_ms:
-                best, best_ms = tl, ms
-        self.table[_bucket(log_h + log_blowup, width)] = best
-        return best
+            for rx in _RADIX_CANDIDATES:
+                bc = BatchCommitter(perm, f, tuner=None, tile_override=tl, radix_override=rx)
+                try:
+                    ms = self._time(lambda: bc.encode([job]), reps)
+                except (NotImplementedError, ValueError):
+                    continue
+                if ms < best_ms:
+                    best, best_ms = (tl, rx), ms
+        bc = BatchCommitter(perm, f, tuner=None)
+        cw = bc.encode([job])
+        top, top_ms = 0, float("inf")
+        for tp in _TOP_CANDIDATES:
+            bt = BatchCommitter(bc.perm, f, tuner=None, top_override=tp)
+            ms = self._time(lambda: bt.merkle(cw), reps)
+            if ms < top_ms:
+                top, top_ms = tp, ms
+        self.table[_bucket(log_h + log_blowup, bucket_width or width)] = {
+            "tile": best[0], "radix": best[1], "top": top}
+        return best[0]
 
 
 class BatchCommitter:
     def __init__(self, perm: Poseidon2 | None = None, field=BABYBEAR, generator: int | None = None,
-                 tuner: Autotuner | None = None, tile_override: int = 0) -> None:
+                 tuner: Autotuner | None = None, tile_override: int = 0,
+                 radix_override: int = 0, top_override: int = 0) -> None:
         self.field = field_of(field)
         self.perm = perm if perm is not None else Poseidon2.builtin(self.field)
         self.generator = generator or 0
         self.tuner = tuner
         self.tile_override = tile_override
+        self.radix_override = radix_override
+        self.top_override = top_override
+
+    def _choice(self, log_n: int, width: int) -> dict:
+        c = self.tuner.choice(log_n, width) if self.tuner else {"tile": 0, "radix": 0, "top": 0}
+        return {"tile": self.tile_override or c["tile"], "radix": self.radix_override or c["radix"],
+                "top": self.top_override or c["top"]}
 
     # -- LDE -----------------------------------------------------------------
     def _lde_jobs(self, jobs: list[MatrixJob], outs: list[torch.Tensor]):
         arr = (_lib.LdeJob * len(jobs))()
         for i, (j, o) in enumerate(zip(jobs, outs)):
             h = j.height
-            tl = self.tile_override or (self.tuner.tile_log(j.log_n, j.width) if self.tuner else 0)
+            c = self._choice(j.log_n, j.width)
             arr[i] = _lib.LdeJob(ptr(j.columns), ptr(o), j.width, h.bit_length() - 1,
-                                 j.log_blowup, self.field.mont(j.shift) if j.shift else 0, tl,
-                                 int(j.bit_reversed))
+                                 j.log_blowup, self.field.mont(j.shift) if j.shift else 0,
+                                 c["tile"], int(j.bit_reversed), c["radix"])
         return arr
 
     def encode(self, jobs: list[MatrixJob], outs: list[torch.Tensor] | None = None,
@@ -164,7 +209,8 @@ class BatchCommitter:
         arr = (_lib.MerkleJob * len(codewords))()
         for i, (cw, fl) in enumerate(zip(codewords, flats)):
             w, n = cw.shape
-            arr[i] = _lib.MerkleJob(_lib.Leaves(ptr(cw), n, w, 1, n), ptr(fl))
+            top = self._choice(n.bit_length() - 1, w)["top"]
+            arr[i] = _lib.MerkleJob(_lib.Leaves(ptr(cw), n, w, 1, n), ptr(fl), top)
         if counters is None:
             counters = torch.empty(64, dtype=torch.int32, device=codewords[0].device)
         _lib.check(_lib.lib().zc_merkle_commit_batch(self.perm.handle, arr, len(codewords),

@@ -621,7 +621,8 @@ zc_status tree_batch_wave(const zc_merkle_job* jobs, int n, unsigned long long* 
     d.G = jobs[i].leaves.groups;
     d.g = jobs[i].leaves.group_len;
     d.depth = ilog2(d.L);
-    d.top = d.depth > kTopLog ? d.depth - kTopLog : 0;
+    const int tl = jobs[i].top_log ? jobs[i].top_log : kTopLog;
+    d.top = d.depth > tl ? d.depth - tl : 0;
     max_top = d.top > max_top ? d.top : max_top;
   }
   int dev = 0, sms = 0;
@@ -893,7 +894,12 @@ zc_status zc_merkle_commit_batch(const zc_poseidon2* p, const zc_merkle_job* job
     if (j.leaves.groups < 0 || j.leaves.group_len < 0 ||
         (!j.leaves.base && j.leaves.groups * j.leaves.group_len > 0))
       return ZC_BAD_ARG;
-    if (ilog2(j.leaves.num_leaves) - kTopLog + 1 > 30) return ZC_BAD_SHAPE;
+    if (j.top_log < 0 || j.top_log > kTopLog) {
+      set_error("top_log must be 0 (default) or 1..8");
+      return ZC_BAD_ARG;
+    }
+    if (ilog2(j.leaves.num_leaves) - (j.top_log ? j.top_log : kTopLog) + 1 > 30)
+      return ZC_BAD_SHAPE;
   }
   cudaStream_t st = (cudaStream_t)stream;
   unsigned long long* ctr = (unsigned long long*)workspace;

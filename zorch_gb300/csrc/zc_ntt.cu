@@ -156,9 +156,15 @@ __device__ __forceinline__ void dif_pass(uint32_t* a, int log_rows, int logm, in
 
 // DIF NTT of each row, natural order in, bit-reversed order out (position p
 // holds output index brev(p)); stages split into balanced passes of <= 4.
+// Largest radix-2^R register pass by default (radix-2^5 passes spill under
+// the 64-register cap the two-CTA occupancy needs).
+constexpr int kMaxRadixLog = 4;
+
+// max_r (2..4) bounds the passes' radix: ceil(logm / max_r) balanced passes.
 template <class F>
-__device__ void smem_ntt_dif(uint32_t* a, int log_rows, int logm, int rs, const uint32_t* tw) {
-  const int passes = (logm + 3) / 4;
+__device__ void smem_ntt_dif(uint32_t* a, int log_rows, int logm, int rs, const uint32_t* tw,
+                             int max_r = kMaxRadixLog) {
+  const int passes = (logm + max_r - 1) / max_r;
   int h0 = logm - 1;
   for (int q = 0; q < passes; q++) {
     const int remaining = h0 + 1;
@@ -192,7 +198,8 @@ __device__ __forceinline__ void cp_async_wait_all() {
 // Layout: work[b][rs] | tw[k/2] | hp[k] | wl[128] | wh[128].
 template <class F>
 __device__ void lde_small_body(const uint32_t* x, uint32_t* out, int log_k, int log_b,
-                               uint32_t h, int64_t c, uint32_t* sm, int brev_out) {
+                               uint32_t h, int64_t c, uint32_t* sm, int brev_out,
+                               int max_r = kMaxRadixLog) {
   const int k = 1 << log_k, b = 1 << log_b, log_n = log_k + log_b;
   const int rs = row_stride(k);
   uint32_t* work = sm;
@@ -222,7 +229,7 @@ __device__ void lde_small_body(const uint32_t* x, uint32_t* out, int log_k, int 
     *slot = snorm<F>(v);
   }
   __syncthreads();
-  smem_ntt_dif<F>(work, log_b, log_k, rs, tw);
+  smem_ntt_dif<F>(work, log_b, log_k, rs, tw, max_r);
   uint32_t* oc = out + (c << log_n);
   if (brev_out) {  // out[brev_b(s) k + p] = row s, position p
     for (int idx = threadIdx.x; idx < (b << log_k); idx += blockDim.x) {
@@ -252,7 +259,7 @@ __global__ void __launch_bounds__(kThreads, 2) k_lde_small(const uint32_t* x, ui
 template <class F>
 __device__ void lde_pass1_body(const uint32_t* x, uint32_t* z, int log_k1, int log_k2, int log_b,
                                int log_ti, uint32_t h, int s, int tile, int64_t c,
-                               uint32_t* sm) {
+                               uint32_t* sm, int max_r = kMaxRadixLog) {
   const int k1 = 1 << log_k1, k2 = 1 << log_k2, TI = 1 << log_ti;
   const int log_k = log_k1 + log_k2, log_n = log_k + log_b;
   const int rs = row_stride(k2);
@@ -289,7 +296,7 @@ __device__ void lde_pass1_body(const uint32_t* x, uint32_t* z, int log_k1, int l
     }
   }
   __syncthreads();
-  smem_ntt_dif<F>(work, log_ti, log_k2, rs, tw);
+  smem_ntt_dif<F>(work, log_ti, log_k2, rs, tw, max_r);
   uint32_t* zd = z + ((c << log_b) + s) * ((int64_t)1 << log_k) + i1_0 + d;
   for (int p = i2_0; p < k2; p += di) zd[(uint32_t)brev(p, log_k2) << log_k1] = wd[pad(p)];
 }
@@ -312,7 +319,7 @@ __global__ void __launch_bounds__(kThreads, 2) k_lde_pass1(const uint32_t* x, ui
 template <class F>
 __device__ void lde_pass2_body(const uint32_t* z, uint32_t* out, int log_k1, int log_k2,
                                int log_b, int log_tt, int tile, int64_t c, uint32_t* sm,
-                               int brev_out) {
+                               int brev_out, int max_r = kMaxRadixLog) {
   const int k1 = 1 << log_k1, TT = 1 << log_tt;
   const int log_k = log_k1 + log_k2, log_n = log_k + log_b;
   const int log_rows = log_b + log_tt;
@@ -357,7 +364,7 @@ __device__ void lde_pass2_body(const uint32_t* z, uint32_t* out, int log_k1, int
     }
   }
   __syncthreads();
-  smem_ntt_dif<F>(work, log_rows, log_k1, rs, tw);
+  smem_ntt_dif<F>(work, log_rows, log_k1, rs, tw, max_r);
   uint32_t* oc = out + (c << log_n);
   const int rows = 1 << log_rows;
   if (brev_out) {  // row (s, t2) -> the k1 contiguous words at brev_b(s) k + brev_k2(t2) k1
@@ -489,7 +496,7 @@ struct LdeJobDev {
   uint32_t* z;
   int64_t batch;
   uint32_t h;
-  int8_t log_k, log_b, log_k1, log_k2, log_ti, log_tt, small, brev_out;
+  int8_t log_k, log_b, log_k1, log_k2, log_ti, log_tt, small, brev_out, max_r;
 };
 
 struct LdeBatch {
@@ -524,19 +531,19 @@ __global__ void __launch_bounds__(kThreads, 2) k_lde_batch(const __grid_constant
     const LdeJobDev& J = B.job[j];
     const int64_t local = it - B.prefix[j];
     if (B.phase == 0 && J.small) {
-      lde_small_body<F>(J.x, J.out, J.log_k, J.log_b, J.h, local, sm, J.brev_out);
+      lde_small_body<F>(J.x, J.out, J.log_k, J.log_b, J.h, local, sm, J.brev_out, J.max_r);
     } else if (B.phase == 0) {
       const int b = 1 << J.log_b;
       const int64_t per_col = (int64_t)b << (J.log_k1 - J.log_ti);
       const int64_t c = local / per_col;
       const int r = (int)(local - c * per_col);
       lde_pass1_body<F>(J.x, J.z, J.log_k1, J.log_k2, J.log_b, J.log_ti, J.h, r & (b - 1),
-                        r >> J.log_b, c, sm);
+                        r >> J.log_b, c, sm, J.max_r);
     } else {
       const int64_t tiles = (int64_t)1 << (J.log_k2 - J.log_tt);
       const int64_t c = local / tiles;
       lde_pass2_body<F>(J.z, J.out, J.log_k1, J.log_k2, J.log_b, J.log_tt,
-                        (int)(local - c * tiles), c, sm, J.brev_out);
+                        (int)(local - c * tiles), c, sm, J.brev_out, J.max_r);
     }
     __syncthreads();  // the item's shared memory is free again
   }
@@ -575,6 +582,7 @@ zc_status lde_batch_wave(const zc_lde_job* jobs, int n, uint32_t* zbase, unsigne
     d.log_tt = (int8_t)p.log_tt;
     d.small = p.small ? 1 : 0;
     d.brev_out = j.bit_reversed ? 1 : 0;
+    d.max_r = (int8_t)(j.radix_log ? j.radix_log : kMaxRadixLog);
     d.z = p.small ? nullptr : z;
     if (!p.small) z += ((size_t)j.batch) << (j.log_k + j.log_blowup);
     B.prefix[i] = totA;
@@ -791,6 +799,10 @@ zc_status zc_rs_encode_batch(zc_field field, const zc_lde_job* jobs, int32_t njo
     for (int i = 0; i < njobs; i++) {
       const zc_lde_job& j = jobs[i];
       if (!j.coeffs || !j.out || j.batch < 0 || j.log_k < 0 || j.log_blowup < 0) return ZC_BAD_ARG;
+      if (j.radix_log != 0 && (j.radix_log < 2 || j.radix_log > kMaxRadixLog)) {
+        set_error("radix_log must be 0 (default) or 2..4");
+        return ZC_BAD_ARG;
+      }
       if (j.log_k + j.log_blowup > F::TWO_ADICITY || j.log_k > 24) return ZC_BAD_SHAPE;
       const LdePlan p = plan_lde(j.log_k, j.log_blowup, j.tile_log);
       const size_t cap = 227 * 1024;
