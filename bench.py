@@ -527,6 +527,17 @@ def paths_workload(args, device):
             np.array_equal(to_host(sproof.fri_commitments), want["bound_roots"])
             and np.array_equal(to_host(sproof.final_poly), want["final_poly"])))
     rows["sp1_stacked_open"] = row
+    from zorch_gb300.jagged import GraphedStackedOpen
+
+    gso = GraphedStackedOpen(smcs, scode, srounds, v + 2, v, num_queries=q, pow_bits=0)
+    t_sp1 = DuplexTranscript.new(sp1)
+    g_ms, (gsp, _) = gpu_time(lambda: gso.replay(zfd, ded, t_sp1))
+    grow = {"config": row["config"] + ", one graph replay", "gpu_ms": g_ms,
+            "equal_to_eager": bool(torch.equal(gsp.fri_commitments, sproof.fri_commitments)
+                                   and torch.equal(gsp.final_poly, sproof.final_poly))}
+    if cpu:
+        grow["cpu_ms"] = row["cpu_ms"]
+    rows["sp1_stacked_open_graphed"] = grow
 
     # f4: k-ary fold-and-commit rounds (k = 4, two rounds) over a 2^22 KoalaBear codeword
     k, nr = 4, 2

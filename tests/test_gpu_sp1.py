@@ -360,3 +360,38 @@ def test_stacked_verify_rejects_tampering(orc, sp1):
         *proof.query_openings[:2], (flip(rows, 5), paths), *proof.query_openings[3:]]))
     with pytest.raises(ValueError):
         check(dataclasses.replace(proof, batch_evals=proof.batch_evals[:1]))
+
+
+def test_graphed_stacked_open_replays_the_eager_open(orc, sp1):
+    """GraphedStackedOpen: one capture, replays at new statements and
+    transcripts give the eager open's proof, field for field."""
+    from zorch_gb300.jagged import GraphedStackedOpen, stacked_basefold_open
+    from zorch_gb300.transcript import DuplexTranscript
+
+    smcs, code, widths, zd, de, v, _ = _stacked_case(orc, sp1, 3)
+    rounds = _rounds_of(orc, sp1, code, smcs)
+    g = GraphedStackedOpen(smcs, code, rounds, zd.shape[0], v, num_queries=6, pow_bits=3)
+    for k in range(3):
+        z = dev(rand_mont(orc, 1, tuple(zd.shape), 700 + k)).reshape(zd.shape)
+        d = dev(rand_mont(orc, 1, 4, 710 + k))
+        t = DuplexTranscript.new(sp1[0]).observe(dev(rand_mont(orc, 1, (k + 2,), 720 + k)))
+        want, wt = stacked_basefold_open(smcs, code, rounds, z, d, v, num_queries=6, pow_bits=3,
+                                         transcript=t)
+        got, gt = g.replay(z, d, t)
+        for name in ("fri_raw_roots", "fri_commitments", "univariate_messages", "final_poly",
+                     "pow_witness", "positions"):
+            assert torch.equal(getattr(got, name), getattr(want, name)), name
+        for a, b in zip(got.batch_evals, want.batch_evals):
+            assert torch.equal(a, b)
+        for (ra, pa), (rb, pb) in zip(got.query_openings + got.component_openings,
+                                      want.query_openings + want.component_openings):
+            assert torch.equal(ra, rb) and torch.equal(pa, pb)
+        assert torch.equal(gt.state, wt.state)
+
+
+def _rounds_of(orc, sp1, code, smcs, widths=(3, 2), v=7):
+    from zorch_gb300.jagged import stacked_commit
+
+    S = 1 << v
+    blocks = [rand_mont(orc, 1, (w, S), 90 + i) for i, w in enumerate(widths)]
+    return [stacked_commit(smcs, code, dev(b).reshape(b.shape)) for b in blocks]

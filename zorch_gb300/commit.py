@@ -205,12 +205,12 @@ class MerkleTree:
         return Opening(rows, paths)
 
     def open_rows(self, matrix: torch.Tensor, layers: DigestLayers,
-                  indices: torch.Tensor) -> Opening:
+                  indices: torch.Tensor, check: bool = True) -> Opening:
         """Open `matrix` (always leaf-major [L, w] like the reference) at every
-        index (zorch/pcs/fold.py:142-149)."""
+        index (zorch/pcs/fold.py:142-149); `check` as in open_layout."""
         m = matrix.contiguous()
         lv = leaves_layout(m, m.shape[0], 1, m.shape[1], 0)
-        return self.open_layout(lv, layers, indices, m.shape[1])
+        return self.open_layout(lv, layers, indices, m.shape[1], check=check)
 
     def reconstruct_root(self, index: int, opening: Opening) -> np.ndarray:
         """Rebuild the raw root from an opening's row and leaf-first path
@@ -301,10 +301,12 @@ class SingleMatrixCommitmentScheme:
         return self.perm.compress_host(np.asarray(raw_root, np.uint32).reshape(-1), params)
 
     def open_batch(self, indices: torch.Tensor, matrix: torch.Tensor,
-                   layers: DigestLayers) -> tuple[torch.Tensor, torch.Tensor]:
+                   layers: DigestLayers, check: bool = True) -> tuple[torch.Tensor, torch.Tensor]:
         """(rows [Q, width], proofs [log_height, Q, 8]) (zorch/commit/smcs.py:158-183):
-        `matrix` is the committed row-major [height, width] matrix."""
-        op = self._tree.open_rows(matrix, layers, indices)
+        `matrix` is the committed row-major [height, width] matrix. `check`
+        reads the device's out-of-range flag back (a host synchronisation);
+        callers whose indices are in range by construction pass False."""
+        op = self._tree.open_rows(matrix, layers, indices, check=check)
         return op.row, op.path
 
     def verify_batch(self, commitment, dims: tuple[int, int], index: int, row, proof) -> int:

@@ -112,12 +112,14 @@ class StackedFoldCommit:
         """run() with the betas given up front ([R, 4] device words)."""
         return self.run(codeword, len(betas), lambda r, _layer: betas[r])
 
-    def open_layers(self, layers: Sequence[StackedFoldLayer], positions: torch.Tensor):
+    def open_layers(self, layers: Sequence[StackedFoldLayer], positions: torch.Tensor,
+                    check: bool = True):
         """Each layer's pair row opened at the halved positions a_i = q >> (i+1)
         (BitReversedReedSolomon.layer_positions; zorch/pcs/jagged/open.py:313-317):
-        a list of (rows [Q, 8], proofs [depth_i, Q, 8])."""
+        a list of (rows [Q, 8], proofs [depth_i, Q, 8]). `check=False` skips the
+        range read-back for positions drawn below n (then a_i < n / 2^(i+1))."""
         idx = self.code.layer_positions(positions.to(torch.int32), len(layers))
-        return [self.smcs.open_batch(i, layer.leaves, layer.digest_layers)
+        return [self.smcs.open_batch(i, layer.leaves, layer.digest_layers, check=check)
                 for i, layer in zip(idx, layers)]
 
 
@@ -271,7 +273,7 @@ def stacked_basefold_open(smcs: SingleMatrixCommitmentScheme, code: BitReversedR
     witness = witness.reshape(1)
     t, positions = sample_query_positions(t, n, num_queries)
     positions = positions.to(torch.int32)
-    query_openings = fold.open_layers(layers, positions)
+    query_openings = fold.open_layers(layers, positions, check=False)  # masked below n
     component_openings = []
     for rd in rounds:
         K = rd.codeword.shape[0]
@@ -438,3 +440,46 @@ def stacked_basefold_verify(smcs: SingleMatrixCommitmentScheme, code: BitReverse
             want = ef(layer_rows[i + 1][qi][a & 1]) if i + 1 < v else final_ef
             ok &= folded == want
     return t, bool(ok)
+
+
+class GraphedStackedOpen:
+    """stacked_basefold_open over fixed committed rounds captured once into a
+    CUDA graph: the batch evaluations, the batching, every interleaved
+    sumcheck round with its fused fold-and-commit, the grind, the SP1 query
+    positions and all openings replay with one launch. `replay(z_final,
+    dense_eval, transcript)` copies the statement and the transcript state
+    into static inputs and returns (proof, transcript) -- static tensors the
+    next replay overwrites. The rounds' device buffers are baked into the
+    graph."""
+
+    def __init__(self, smcs: SingleMatrixCommitmentScheme, code: BitReversedReedSolomon,
+                 rounds: Sequence[StackedRound], num_vars: int, log_stacking_height: int, *,
+                 num_queries: int, pow_bits: int, device="cuda") -> None:
+        self.args = (smcs, code, list(rounds))
+        self.log_s = log_stacking_height
+        self.kw = dict(num_queries=num_queries, pow_bits=pow_bits)
+        self.z = torch.zeros((num_vars, 4), dtype=torch.int32, device=device)
+        self.dense = torch.zeros(4, dtype=torch.int32, device=device)
+        self.state = torch.zeros(_lib.DUPLEX_WORDS, dtype=torch.int32, device=device)
+        self._run()  # kernel attributes, allocator warm-up
+        torch.cuda.synchronize()
+        self.graph = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(self.graph):
+            self.out = self._run()
+
+    def _run(self):
+        smcs, code, rounds = self.args
+        t = DuplexTranscript(smcs.perm, self.state)
+        return stacked_basefold_open(smcs, code, rounds, self.z, self.dense, self.log_s,
+                                     transcript=t, **self.kw)
+
+    def replay(self, z_final: torch.Tensor, dense_eval: torch.Tensor,
+               transcript: DuplexTranscript):
+        if z_final.shape != self.z.shape:
+            raise ValueError(f"point shape {tuple(z_final.shape)} != captured "
+                             f"{tuple(self.z.shape)}")
+        self.z.copy_(z_final, non_blocking=True)
+        self.dense.copy_(dense_eval.reshape(-1), non_blocking=True)
+        self.state.copy_(transcript.state, non_blocking=True)
+        self.graph.replay()
+        return self.out
