@@ -140,14 +140,17 @@ def fold_and_open(req: Request, cw: torch.Tensor, root: torch.Tensor, perm: Pose
     t.observe_(root)
     rlc = batch_columns(cw, t)
     rounds = max(req.log_n - FOLD_FINAL_LOG, 0)
-    t.observe_(torch.tensor([BABYBEAR.mont(rounds)], dtype=torch.int32, device=cw.device))
+    # a fill kernel, not a host->device copy: the copy would block this thread
+    # until the batch's stream drained
+    t.observe_(torch.full((1,), BABYBEAR.mont(rounds), dtype=torch.int32, device=cw.device))
     code = ReedSolomon(1 << req.log_h, 1 << req.log_blowup, BABYBEAR, coset_shift=31,
                        generator=31)
     prover = FriProver(FriParams(code, tree, rounds, FOLD_QUERIES, 4))
     proof, t, _ = prover.commit_phase(rlc, t)
     layers = layers if layers is not None else _ResidentLayers.get(req.rid)
+    # positions are drawn below n on the device: no range read-back (a sync)
     rows = tree.open_layout(leaves_layout(cw, n, cw.shape[0], 1, n), layers, proof.positions,
-                            cw.shape[0])
+                            cw.shape[0], check=False)
     return proof, rows
 
 
