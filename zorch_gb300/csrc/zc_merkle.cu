@@ -282,7 +282,7 @@ __global__ void __launch_bounds__(8 * kSubT) k_subtree(Leaf leaf, uint32_t* laye
 // One thread per leaf (or per parent for NodeLeaf): no shared memory, no
 // barriers, so every warp stays busy for the whole launch.
 template <class K, class Leaf>
-__global__ void __launch_bounds__(kMaxT) k_leaf(Leaf leaf, uint32_t* out, int64_t count,
+__global__ void __launch_bounds__(kMaxT, 5) k_leaf(Leaf leaf, uint32_t* out, int64_t count,
                                                 const P2Params* rt) {
   __shared__ P2Params s_rt;
   K k = KIn<K>::make(rt, &s_rt);
