@@ -279,10 +279,25 @@ __global__ void __launch_bounds__(8 * kSubT) k_subtree(Leaf leaf, uint32_t* laye
   }
 }
 
+// Resident 256-thread CTAs per SM k_leaf is compiled for: five for the
+// built-in instance (its level and leaf forms then use 40-46 registers, where
+// the unbounded build gave the level form 32; the 2^22 x 64 trace hash went
+// 9.18 -> 9.00 ms); no bound for run-time parameter sets, whose constants come
+// from shared memory and which would spill under it. The batched tree kernel
+// keeps the compiler's choice: bounding it measured slower.
+template <class K>
+struct HashOcc {
+  static constexpr int v = 1;
+};
+template <>
+struct HashOcc<Bb16Builtin> {
+  static constexpr int v = 5;
+};
+
 // One thread per leaf (or per parent for NodeLeaf): no shared memory, no
 // barriers, so every warp stays busy for the whole launch.
 template <class K, class Leaf>
-__global__ void __launch_bounds__(kMaxT, 5) k_leaf(Leaf leaf, uint32_t* out, int64_t count,
+__global__ void __launch_bounds__(kMaxT, HashOcc<K>::v) k_leaf(Leaf leaf, uint32_t* out, int64_t count,
                                                 const P2Params* rt) {
   __shared__ P2Params s_rt;
   K k = KIn<K>::make(rt, &s_rt);
