@@ -16,7 +16,6 @@ the candidates, and caches the choices as JSON. No choice changes a byte.
 
 from __future__ import annotations
 
-import ctypes as C
 import json
 import os
 from dataclasses import dataclass

@@ -482,7 +482,6 @@ class BasefoldVerifier:
         self.num_queries = num_queries
 
     def verify(self, commitments, z, values, proof: BasefoldProof) -> bool:
-        from .field import from_mont_np
         from .transcript import HostDuplexTranscript
         f, code, tree = self.code.field, self.code, self.tree
         host = lambda x: to_host(x) if torch.is_tensor(x) else np.asarray(x, np.uint32)  # noqa: E731

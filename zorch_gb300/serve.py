@@ -33,7 +33,7 @@ from .batch import BatchCommitter, MatrixJob
 from .coding import ReedSolomon
 from .commit import MerkleTree, Poseidon2, leaves_layout
 from .field import BABYBEAR, ptr, stream_handle, to_mont, to_mont_from_host
-from .pcs import FriParams, FriProver, pair_layout
+from .pcs import FriParams, FriProver
 from .transcript import DuplexTranscript
 
 
