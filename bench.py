@@ -911,11 +911,16 @@ def main():
                      "traffic": traffic_per_word * info["leaves"] * args.cols,
                      "traffic_note": "bytes per launch, scaled from the 2^19 x 64 ncu capture",
                      "peak_source": "152 SMs x 128 INT32 lanes x sm_max_mhz (MEASURED_PEAKS.json)",
-                     "ms": hash_ms, "perms": perms},
+                     "binding_unit": "FMA-heavy pipe (the Montgomery products' wide and high "
+                                     "multiplies), 81 % of its peak cycles in the ncu capture",
+                     "ms": hash_ms, "perms": perms,
+                     "perm_rate": perms / (hash_ms / 1e3)},
         "roofline_ntt": {"bound": "hbm", "kernel": "coset LDE (k_lde_pass1+pass2)",
                          "achieved": info["ntt_bytes"] / (ntt_ms / 1e3) / 1e9, "peak": hbm_peak,
                          "unit": "GB/s", "frac": info["ntt_bytes"] / (ntt_ms / 1e3) / 1e9 / hbm_peak,
-                         "ms": ntt_ms, "peak_source": "MEASURED_PEAKS.json hbm_gbs (of measured)"},
+                         "ms": ntt_ms, "peak_source": "MEASURED_PEAKS.json hbm_gbs (of measured)",
+                         "binding_unit": "integer issue (issue active 62-70 %, FMA-heavy pipe "
+                                         "63 % in the ncu capture), not HBM"},
         "clocks": clk,
         "gpu_launches": int(launches),
     }
