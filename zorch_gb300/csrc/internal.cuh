@@ -36,9 +36,15 @@ struct KIn<RtParams<F>> {
 };
 
 // Calls fn(K{}, device_params) with the provider matching the handle.
+void set_error(const char* msg);
+
 template <class Fn>
 zc_status with_perm(const zc_poseidon2* p, Fn&& fn) {
   if (!p) return ZC_BAD_ARG;
+  if (!p->dev) {
+    set_error("Poseidon2 handle has no device copy (created without a CUDA device)");
+    return ZC_BAD_ARG;
+  }
   if (p->builtin) return fn(Bb16Builtin{}, p->dev);
   if (p->field == ZC_FIELD_BABYBEAR) return fn(RtParams<BabyBear>{}, p->dev);
   return fn(RtParams<KoalaBear>{}, p->dev);
@@ -51,7 +57,6 @@ zc_status with_field(zc_field f, Fn&& fn) {
   return ZC_BAD_ARG;
 }
 
-void set_error(const char* msg);
 zc_status ensure_init();
 
 }  // namespace zc

@@ -312,7 +312,23 @@ zc_status zc_init(int device) {
   return ZC_OK;
 }
 
+// Whether this process can use a CUDA device at all (checked once).
+static bool have_device() {
+  static const bool have = [] {
+    int n = 0;
+    const bool ok = cudaGetDeviceCount(&n) == cudaSuccess && n > 0;
+    cudaGetLastError();  // clear the error a failed query recorded
+    return ok;
+  }();
+  return have;
+}
+
+// Device copy of the constants; without any CUDA device the handle stays
+// host-only (dev == nullptr): the host permutation, sponge, compression and
+// duplex hop work, every device entry refuses it (with_perm).
 static zc_status upload_params(zc_poseidon2* h) {
+  h->dev = nullptr;
+  if (!have_device()) return ZC_OK;
   ZC_CUDA(cudaMalloc((void**)&h->dev, sizeof(P2Params)));
   ZC_CUDA(cudaMemcpy(h->dev, &h->host, sizeof(P2Params), cudaMemcpyHostToDevice));
   return ZC_OK;
@@ -326,8 +342,9 @@ zc_status zc_poseidon2_builtin(zc_field field, const zc_poseidon2** out) {
   }
   static std::mutex mu;
   static zc_poseidon2* inst[64] = {};
-  int dev = 0;
-  ZC_CUDA(cudaGetDevice(&dev));
+  int dev = 0;  // slot 0 serves the host-only instance of a machine without a GPU
+  if (have_device()) ZC_CUDA(cudaGetDevice(&dev));
+  if (dev < 0 || dev >= 64) return ZC_BAD_ARG;
   std::lock_guard<std::mutex> lock(mu);
   if (!inst[dev]) {
     zc_poseidon2* h = new zc_poseidon2();
