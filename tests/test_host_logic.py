@@ -75,3 +75,44 @@ def test_max_over_ranks_gloo_two_ranks():
         p.join(120)
         assert p.exitcode == 0
     assert dict(out) == {0: 2.0, 1: 2.0}
+
+
+def test_autotuner_cache_reads_old_and_new_entries(tmp_path):
+    """The tuning cache maps a (log_n, log2 width) bucket to its choices; a
+    bare integer (a tile choice alone) still reads, unknown buckets give the
+    library defaults (0), and a save/load round trip keeps every field."""
+    import json
+
+    from zorch_gb300.batch import Autotuner, _bucket
+
+    path = tmp_path / "tune.json"
+    path.write_text(json.dumps({"20:3": 13, "22:6": {"tile": 15, "radix": 3, "top": 7}}))
+    t = Autotuner(path)
+    assert t.choice(20, 8) == {"tile": 13, "radix": 0, "top": 0}
+    assert t.choice(22, 64) == {"tile": 15, "radix": 3, "top": 7}
+    assert t.choice(22, 100) == {"tile": 15, "radix": 3, "top": 7}   # same log2-width bucket
+    assert t.choice(18, 1) == {"tile": 0, "radix": 0, "top": 0}
+    assert t.tile_log(22, 64) == 15
+    t.table[_bucket(16, 2)] = {"tile": 14, "radix": 4, "top": 6}
+    t.save()
+    again = Autotuner(path)
+    assert again.choice(16, 3) == {"tile": 14, "radix": 4, "top": 6}
+    path.write_text("not json")
+    assert Autotuner(path).choice(16, 3) == {"tile": 0, "radix": 0, "top": 0}
+
+
+def test_batch_committer_choice_prefers_overrides():
+    from zorch_gb300.batch import Autotuner, BatchCommitter
+
+    class Fixed(Autotuner):
+        def __init__(self):
+            self.table = {}
+
+        def choice(self, log_n, width):
+            return {"tile": 13, "radix": 3, "top": 6}
+
+    bc = BatchCommitter.__new__(BatchCommitter)
+    bc.tuner, bc.tile_override, bc.radix_override, bc.top_override = Fixed(), 0, 4, 0
+    assert bc._choice(20, 8) == {"tile": 13, "radix": 4, "top": 6}
+    bc.tuner = None
+    assert bc._choice(20, 8) == {"tile": 0, "radix": 4, "top": 0}
