@@ -67,3 +67,41 @@ def test_host_permutation_matches_oracle(orc):
                         (kb, orc.Poseidon2.koalabear16_golden(), 1)):
         st = orc.to_mont(f, np.arange(16 * 5, dtype=np.uint32).reshape(5, 16))
         assert np.array_equal(gpu.permute_host(st), np.stack([cpu.permute(s) for s in st]))
+
+
+def test_struct_layouts_match_the_header(tmp_path):
+    """The ctypes mirrors of the ABI structs (zorch_gb300/_lib.py) have the
+    header's size and field offsets, as a C compiler lays them out."""
+    import shutil
+    import subprocess
+
+    from zorch_gb300 import _lib
+
+    cc = shutil.which("gcc") or shutil.which("cc")
+    if cc is None:
+        import pytest
+
+        pytest.skip("no C compiler")
+    structs = {"zc_leaves": _lib.Leaves, "zc_lde_job": _lib.LdeJob,
+               "zc_merkle_job": _lib.MerkleJob}
+    lines = ["#include <stdio.h>", "#include <stddef.h>", '#include "zc.h"', "int main(void) {"]
+    for cname, py in structs.items():
+        lines.append(f'  printf("{cname} size %zu\\n", sizeof({cname}));')
+        for fname, _ in py._fields_:
+            lines.append(f'  printf("{cname} {fname} %zu\\n", offsetof({cname}, {fname}));')
+    lines += ["  return 0;", "}"]
+    src = tmp_path / "layout.c"
+    src.write_text("\n".join(lines) + "\n")
+    exe = tmp_path / "layout"
+    # the header declares stream arguments as void*, so no CUDA header is needed
+    subprocess.run([cc, "-std=c11", "-I", str(ROOT / "include"), str(src), "-o", str(exe)],
+                   check=True)
+    out = subprocess.run([str(exe)], check=True, capture_output=True, text=True).stdout
+    got = {}
+    for line in out.splitlines():
+        s, f, v = line.split()
+        got[(s, f)] = int(v)
+    for cname, py in structs.items():
+        assert got[(cname, "size")] == ctypes.sizeof(py), cname
+        for fname, _ in py._fields_:
+            assert got[(cname, fname)] == getattr(py, fname).offset, (cname, fname)
