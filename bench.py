@@ -62,7 +62,16 @@ def parse():
     ap.add_argument("--budget-gb", type=float, default=150.0)
     ap.add_argument("--max-batch", type=int, default=8)
     ap.add_argument("--streams", type=int, default=4)
+    ap.add_argument("--cal-requests", type=int, default=200,
+                    help="requests of the calibrated-rate served stream")
     return ap.parse_args()
+
+
+def make_stream_for(args):
+    from zorch_gb300.serve import make_stream
+
+    return make_stream(args.requests, args.seed, rate_hz=args.rate,
+                       log_h=(args.min_log_h, args.max_log_h))
 
 
 def dist_env():
@@ -167,16 +176,20 @@ def cpu_trace_sample(log_rows, cols, log_blowup, queries, threads=0, reps=1):
     return (cols << log_rows) / best, best, orc.threads()
 
 
-# Height cap of the CPU samples of the served stream (about 3 s per pass of
-# the whole 24-request stream on 16 Arm cores).
+# Height cap of the CPU samples of the served stream (per-polynomial pair-leaf
+# commitments): the cpu_baseline leg passes the 24-request stream once at
+# 2^16 rows; each step of the reference arm at 2^14 rows (a few seconds on 16
+# Arm cores), so that a 20-step run ends within a few minutes.
 CPU_CAP_LOG_H = 16
+REF_CAP_LOG_H = 14
 
 
-def cpu_served_sample(args, cap_log_h=CPU_CAP_LOG_H):
+def cpu_served_sample(args, cap_log_h=CPU_CAP_LOG_H, mode="fri"):
     """The oracle on a bounded sample of the served stream: every request of
-    the seeded stream with its height capped at 2^cap_log_h rows -- LDE,
-    row-leaf Merkle commit, and for fold requests the partial-Lagrange
-    batching, EF4 fold rounds to 2^8 and 64 query openings."""
+    the seeded stream with its height capped at 2^cap_log_h rows -- LDE, the
+    commitment ("fri": every column's pair-leaf tree, "matrix": one row-leaf
+    tree), and for fold requests the partial-Lagrange batching, EF4 fold
+    rounds to 2^8 and 64 query openings of the commitment and every layer."""
     from oracle import oracle as orc
     from zorch_gb300.serve import FOLD_FINAL_LOG, FOLD_QUERIES, make_stream
 
@@ -191,19 +204,30 @@ def cpu_served_sample(args, cap_log_h=CPU_CAP_LOG_H):
         lh = min(r.log_h, cap_log_h)
         x = rng.integers(0, P, size=(r.width, 1 << lh), dtype=np.uint64).astype(np.uint32)
         cw = orc.rs_encode(0, orc.to_mont(0, x), r.log_blowup, shift)
-        layers = orc.merkle_commit_columns(p2, cw)
+        w, n = cw.shape
+        if mode == "fri":
+            L = n // 2
+            col_layers = [orc.merkle_commit(p2, cw[c], L, 2, 1, L) for c in range(w)]
+            commitment = np.concatenate([ly[-1][0] for ly in col_layers])
+        else:
+            layers = orc.merkle_commit_columns(p2, cw)
+            commitment = layers[-1][0]
         elements += r.width << lh
         if r.fold:
             t = orc.Transcript(p2)
-            t.observe(layers[-1][0])
+            t.observe(commitment)
             nbv = (r.width - 1).bit_length()
             rlc = orc.rlc_columns(0, cw, t.sample(4 * nbv) if nbv else [])
             rounds = max(lh + r.log_blowup - FOLD_FINAL_LOG, 0)
             t.observe(orc.to_mont(0, np.array([rounds], np.uint32)))
             if rounds:
                 proof = orc.fri_commit_phase(p2, 0, rlc, rounds, FOLD_QUERIES, 4, t, shift)
-                n = cw.shape[1]
-                orc.merkle_open(cw, n, r.width, 1, n, layers, proof.positions)
+                if mode == "fri":
+                    a = (proof.positions.astype(np.int64) % L).astype(np.int32)
+                    for c in range(w):
+                        orc.merkle_open(cw[c], L, 2, 1, L, col_layers[c], a)
+                else:
+                    orc.merkle_open(cw, n, w, 1, n, layers, proof.positions)
     dt = time.perf_counter() - t0
     return elements / dt, dt, orc.threads(), elements
 
@@ -317,7 +341,9 @@ def served_workload(args, device, rank):
     """Config-5 stream: Poisson arrivals, log2 heights 14..24, widths
     log-uniform 1..256, blowup 2 or 4, 30% fold-and-open. The same seeded
     stream is served by the continuous-batching server and by the plain
-    one-call-per-polynomial path."""
+    drop-in path, in each commitment mode ("fri": one pair-leaf tree per
+    column, FriProver.commit; "matrix": one row-leaf tree per request,
+    BasefoldProver.commit) -- the two arms of a mode return identical bytes."""
     import torch
 
     from zorch_gb300.batch import Autotuner, _bucket
@@ -337,23 +363,102 @@ def served_workload(args, device, rank):
             tuner.tune(r.log_h, cols.shape[0], r.log_blowup, reps=2, columns=cols,
                        bucket_width=r.width)
     tuner.save()
-    server = Server(budget_bytes=args.budget_gb * 1e9, max_batch=args.max_batch,
-                    streams=args.streams, tuner=tuner)
-    elements = sum(r.elements for r in reqs)
+    servers = {m: Server(budget_bytes=args.budget_gb * 1e9, max_batch=args.max_batch,
+                         streams=args.streams, tuner=tuner, mode=m) for m in ("fri", "matrix")}
 
-    def served(host_fed=False):
+    def served(mode, host_fed=False, stream=None):
         t0 = time.perf_counter()
-        res = server.run(reqs, host_fed=host_fed)
+        res = servers[mode].run(stream if stream is not None else reqs, host_fed=host_fed)
         torch.cuda.synchronize()
         return res, time.perf_counter() - t0
 
-    def plain():
+    def plain(mode, stream=None):
         t0 = time.perf_counter()
-        res = run_plain(reqs, perm=server.perm)
+        res = run_plain(stream if stream is not None else reqs, perm=servers[mode].perm,
+                        mode=mode, budget_bytes=args.budget_gb * 1e9)
         torch.cuda.synchronize()
         return res, time.perf_counter() - t0
 
-    return reqs, served, plain, elements
+    return reqs, served, plain, servers
+
+
+def served_hash_roofline(reqs, server, mode):
+    """LDE and hash device time of the served stream's commits, one request at
+    a time on the current stream with CUDA events around each phase (the
+    server overlaps requests on several streams, so per-kernel times are
+    taken on this serial replay of the same commits): returns (lde_ms,
+    hash_ms, permutations, lde_bytes)."""
+    import torch
+
+    from zorch_gb300.batch import MatrixJob
+    from zorch_gb300.field import BABYBEAR, to_mont
+    from zorch_gb300.serve import FRI_LAYER_CAP
+
+    bc = server.committer
+    stream = torch.cuda.current_stream()
+    lde_ms = hash_ms = 0.0
+    perms = lde_bytes = 0
+    for r in reqs:
+        x = to_mont(BABYBEAR, r.resident)
+        e = [torch.cuda.Event(enable_timing=True) for _ in range(3)]
+        e[0].record(stream)
+        cws = bc.encode([MatrixJob(x, r.log_blowup, 31)])
+        e[1].record(stream)
+        w, n = cws[0].shape
+        if mode == "fri":
+            if 32 * w * n <= FRI_LAYER_CAP:
+                bc.pair_trees(cws)
+            else:
+                per = max(1, FRI_LAYER_CAP // (32 * n))
+                buf = torch.empty((min(per, w), n - 1, 8), dtype=torch.int32, device=x.device)
+                for c0 in range(0, w, per):
+                    cnt = min(per, w - c0)
+                    bc.pair_trees([cws[0][c0:c0 + cnt]], flats=[buf[:cnt]])
+            perms += w * (n - 1)
+        else:
+            bc.merkle(cws)
+            perms += n * ((w + 7) // 8) + n - 1
+        e[2].record(stream)
+        torch.cuda.synchronize()
+        lde_ms += e[0].elapsed_time(e[1])
+        hash_ms += e[1].elapsed_time(e[2])
+        lde_bytes += 4 * r.elements + 4 * w * n
+        del cws, x
+    return lde_ms, hash_ms, perms, lde_bytes
+
+
+def request_perms(r, mode):
+    """Poseidon2 permutations of a request's commit and fold-and-open (the
+    work model used to set the calibrated arrival rate)."""
+    n = 1 << r.log_n
+    perms = r.width * (n - 1) if mode == "fri" else n * ((r.width + 7) // 8) + n - 1
+    if r.fold:
+        perms += n  # fold layers' pair-leaf trees: n/2 + n/4 + ... leaves and nodes
+    return perms
+
+
+def calibrated_stream(args, n, seed, rate, device):
+    """A long stream of the config-5 distribution at a set arrival rate whose
+    requests read their inputs from one shared seeded buffer (views of its
+    first w*h words): the data of a request does not change its cost, and the
+    stream's inputs then take one buffer instead of one per request. With
+    device None only the shapes are drawn."""
+    import torch
+
+    from zorch_gb300 import _lib
+    from zorch_gb300.field import ptr, stream_handle
+    from zorch_gb300.serve import make_stream
+
+    reqs = make_stream(n, seed, rate_hz=rate, log_h=(args.min_log_h, args.max_log_h))
+    if device is None:
+        return reqs
+    big = max(r.elements for r in reqs)
+    buf = torch.empty(big, dtype=torch.int32, device=device)
+    _lib.check(_lib.lib().zc_fill_uniform(0, ptr(buf), big, seed, stream_handle()), "fill")
+    for r in reqs:
+        r.resident = buf[: r.elements].view(r.width, 1 << r.log_h)
+    torch.cuda.synchronize()
+    return reqs
 
 
 def fri_workload(args, device):
@@ -820,59 +925,143 @@ def main():
                                       "graph, autotuned tile/radix/tree top per bucket",
                           "field": "babybear",
                           "l2": "inputs larger than L2"}
+    served_roof = None
     if args.workload == "served":
-        reqs, served, plain, elements = served_workload(args, device, rank)
-        for _ in range(max(args.warmup, 3)):
-            served()
-        sv_launch0 = _lib.lib().zc_launch_count()
-        clocks = Clocks(local).start()
-        barrier()
-        times, lat = [], []
-        for _ in range(args.steps):
-            res, dt = served()
-            times.append(dt)
-            lat += [r.latency for r in res]
-        barrier()
-        clk = clocks.stop()
-        launches = _lib.lib().zc_launch_count() - sv_launch0
-        sv_s = max_over_ranks(sum(times), device)
-        plain(); torch.cuda.synchronize()  # warm
-        p_res, p_dt = plain()
-        e2e_res, e2e_dt = served(host_fed=False)
-        # host-fed: inputs from pinned host memory, H2D inside the timed region
+        reqs, served, plain, servers = served_workload(args, device, rank)
+        modes = {}
+        for mode in ("fri", "matrix"):
+            for _ in range(max(args.warmup, 3)):
+                served(mode)
+            l0 = _lib.lib().zc_launch_count()
+            if mode == "fri":
+                clocks = Clocks(local).start()
+            barrier()
+            times, lat = [], []
+            for _ in range(args.steps):
+                res, dt = served(mode)
+                times.append(dt)
+                lat += [r.latency for r in res]
+            barrier()
+            m = {"launches": _lib.lib().zc_launch_count() - l0, "s": max_over_ranks(sum(times),
+                                                                                    device)}
+            if mode == "fri":
+                clk = clocks.stop()
+            plain(mode)  # warm
+            p_res, p_dt = plain(mode)
+            done = [r for r in res if r.proof]
+            elements = sum(q.elements for q, r in zip(reqs, res) if r.proof)
+            m.update({
+                "res": res, "elements": elements, "lat": lat,
+                "plain_dt": p_dt, "plain_res": p_res,
+                "bytes_equal": len(done) > 0 and all(a.proof == b.proof
+                                                    for a, b in zip(res, p_res)),
+                "rejected": len(res) - len(done)})
+            modes[mode] = m
+        # end to end: inputs from pinned host memory read by the conversion
+        # kernel, proofs back in pinned buffers, all inside the timed region
         for r in reqs:
             r.host = r.resident.cpu().pin_memory()
         torch.cuda.synchronize()
-        served(host_fed=True)
-        h_runs = max(1, min(args.steps, 3))
-        h0 = time.perf_counter()
-        for _ in range(h_runs):
-            h_res, _ = served(host_fed=True)
-        torch.cuda.synchronize()
-        h_dt = max_over_ranks(time.perf_counter() - h0, device) / h_runs
-        value = elements * args.steps * world / sv_s
-        e2e_value = elements * world / h_dt
-        plain_value = elements / p_dt
+        for mode in ("fri", "matrix"):
+            served(mode, host_fed=True)
+            h_runs = max(1, min(args.steps, 3))
+            h0 = time.perf_counter()
+            for _ in range(h_runs):
+                h_res, _ = served(mode, host_fed=True)
+            torch.cuda.synchronize()
+            modes[mode]["h_dt"] = max_over_ranks(time.perf_counter() - h0, device) / h_runs
+            modes[mode]["bytes_equal_host_fed"] = all(
+                a.proof == b.proof for a, b in zip(modes[mode]["res"], h_res))
+        for r in reqs:
+            r.host = None
+        # hash / LDE rooflines on the served stream's own commits (serial replay)
+        lde_ms, hash_ms_sv, perms_sv, lde_bytes_sv = served_hash_roofline(reqs, servers["fri"],
+                                                                          "fri")
+        served_roof = {"lde_ms": lde_ms, "hash_ms": hash_ms_sv, "perms": perms_sv,
+                       "lde_bytes": lde_bytes_sv}
+        blocks = {}
+        for mode, m in modes.items():
+            el = m["elements"]
+            blocks[mode] = {
+                "value": el * args.steps * world / m["s"], "unit": "elem/s",
+                "requests_per_s": len(reqs) * args.steps / (m["s"] / world),
+                "latency_ms": {"p50": 1e3 * pct(m["lat"], 50), "p99": 1e3 * pct(m["lat"], 99)},
+                "e2e": el * world / m["h_dt"],
+                "plain": {"value": el / m["plain_dt"], "unit": "elem/s",
+                          "requests_per_s": len(reqs) / m["plain_dt"],
+                          "latency_ms": {
+                              "p50": 1e3 * pct([r.latency for r in m["plain_res"]], 50),
+                              "p99": 1e3 * pct([r.latency for r in m["plain_res"]], 99)},
+                          "path": ("one FriProver.commit_one call per polynomial (column); "
+                                   "result read back per request" if mode == "fri" else
+                                   "one BasefoldProver.commit call per request; result read "
+                                   "back per request")},
+                "served_over_plain": (el * args.steps / m["s"]) / (el / m["plain_dt"]),
+                "bytes_identical_served_vs_plain": m["bytes_equal"],
+                "bytes_identical_host_fed": m["bytes_equal_host_fed"],
+                "rejected_over_budget": m["rejected"],
+                "commitment": ("per-polynomial pair-leaf roots (FriProver.commit)"
+                               if mode == "fri" else
+                               "one row-leaf root per request (BasefoldProver.commit)"),
+            }
+        # calibrated served rate: arrivals at 0.8 x the plain path's measured
+        # request rate, a long stream, both arms on the same stream
+        del reqs
+        torch.cuda.empty_cache()
+        cal = {}
+        for mode in ("fri", "matrix"):
+            # the plain path's capacity in permutations/s on the 24-request
+            # stream, over the mean permutations of a request of the longer
+            # stream (hashing is most of a request's device time)
+            shapes = make_stream_for(args)
+            rate = sum(request_perms(q, mode) for q in shapes) / modes[mode]["plain_dt"]
+            probe = calibrated_stream(args, args.cal_requests, args.seed + 1, 1.0, None)
+            mean = sum(request_perms(q, mode) for q in probe) / len(probe)
+            lam = 0.8 * rate / mean
+            stream_c = calibrated_stream(args, args.cal_requests, args.seed + 1, lam, device)
+            served(mode, stream=stream_c[:8])  # warm the shapes' kernels
+            c_res, c_dt = served(mode, stream=stream_c)
+            p_res, p_dt = plain(mode, stream=stream_c)
+            ok = [r for r in c_res if r.proof]
+            cal[mode] = {
+                "rate_per_s": lam, "requests": len(stream_c),
+                "rate_rule": "0.8 x the plain path's permutations/s on the 24-request stream / "
+                             "the mean permutations per request of this stream",
+                "rejected_over_budget": len(c_res) - len(ok),
+                "served": {"requests_per_s": len(ok) / c_dt,
+                           "latency_ms": {"p50": 1e3 * pct([r.latency for r in ok], 50),
+                                          "p99": 1e3 * pct([r.latency for r in ok], 99)}},
+                "plain": {"requests_per_s": len(ok) / p_dt,
+                          "latency_ms": {
+                              "p50": 1e3 * pct([r.latency for r in p_res if r.proof], 50),
+                              "p99": 1e3 * pct([r.latency for r in p_res if r.proof], 99)}},
+                "bytes_identical_served_vs_plain": all(a.proof == b.proof
+                                                       for a, b in zip(c_res, p_res)),
+            }
+            blocks[mode]["calibrated"] = cal[mode]
+            del stream_c
+            torch.cuda.empty_cache()
+        head = modes["fri"]
+        value = blocks["fri"]["value"]
+        e2e_value = blocks["fri"]["e2e"]
+        launches = head["launches"]
         served_info = {
-            "requests": len(reqs), "elements_per_step": elements,
-            "requests_per_s": len(reqs) * args.steps / (sv_s / world),
-            "fold_requests": sum(r.fold for r in reqs),
-            "latency_ms": {"p50": 1e3 * pct(lat, 50), "p99": 1e3 * pct(lat, 99)},
-            "plain": {"value": plain_value, "unit": "elem/s", "requests_per_s": len(reqs) / p_dt,
-                      "latency_ms": {"p50": 1e3 * pct([r.latency for r in p_res], 50),
-                                     "p99": 1e3 * pct([r.latency for r in p_res], 99)},
-                      "path": "one call per polynomial (FriProver.commit), host sync per call"},
-            "served_over_plain": value / world / plain_value,
-            "bytes_identical_across_runs": all(a.proof == b.proof for a, b in zip(res, e2e_res))
-            and all(a.proof == b.proof for a, b in zip(res, h_res)),
+            "headline_mode": "fri", "requests": args.requests,
+            "elements_per_step": head["elements"],
+            "requests_per_s": blocks["fri"]["requests_per_s"],
+            "fold_requests": sum(q.fold for q in make_stream_for(args)),
+            "latency_ms": blocks["fri"]["latency_ms"],
+            "served_over_plain": blocks["fri"]["served_over_plain"],
+            "fri": blocks["fri"], "matrix": blocks["matrix"],
         }
-        info["h2d_bytes"] = 4 * elements
-        info["d2h_bytes"] = sum(len(r.proof) for r in res)
-        ms_max = sv_s * 1e3
-        info["config"] = {"workload": f"served commit stream: {len(reqs)} requests, Poisson "
+        info["h2d_bytes"] = 4 * head["elements"]
+        info["d2h_bytes"] = sum(len(r.proof) for r in head["res"])
+        ms_max = head["s"] * 1e3
+        info["config"] = {"workload": f"served commit stream: {args.requests} requests, Poisson "
                                       f"{args.rate:g}/s, log2 h {args.min_log_h}..{args.max_log_h}, "
                                       "w log-uniform 1..256, blowup 2|4, 30% fold to 2^8 + 64 "
-                                      "queries", "budget_gb": args.budget_gb,
+                                      "queries; headline: per-polynomial commitments "
+                                      "(FriProver.commit bytes)", "budget_gb": args.budget_gb,
                           "max_batch": args.max_batch, "streams": args.streams,
                           "field": "babybear", "hash": "poseidon2-16 (built-in)",
                           "l2": "inputs larger than L2"}
@@ -893,8 +1082,47 @@ def main():
     # workload's leaf launch by its word count.
     traffic_per_word = (134.273792e6 + 8.598272e6) / float(1 << 25)
     perms = info["perms_leaf"] + info["perms_node"]
-    int_peak = 152 * 128 * sm_mhz * 1e6 / 1e9  # Ginst/s: 152 SMs x 128 lanes x clock
-    achieved = perms * inst_per_perm / (hash_ms / 1e3) / 1e9
+    sms = torch.cuda.get_device_properties(device).multi_processor_count
+    int_peak = sms * 128 * sm_mhz * 1e6 / 1e9  # Ginst/s: SMs x 128 lanes x clock
+    peak_src = (f"{sms} SMs (cudaDevAttrMultiProcessorCount) x 128 lanes x sm_max_mhz "
+                "(MEASURED_PEAKS.json): the thread-instruction issue peak")
+    binding = ("FMA-heavy pipe (the Montgomery products' wide and high multiplies): 81 % of "
+               "its peak cycles in the ncu capture of the leaf launch "
+               "(profiles/k_leaf_poseidon2_trace_2p17x64_blowup4.md)")
+
+    def hash_roof(perms_, ms_, kernel, traffic):
+        ach = perms_ * inst_per_perm / (ms_ / 1e3) / 1e9
+        return {"bound": "int32", "kernel": kernel, "achieved": ach, "peak": int_peak,
+                "unit": "Ginst/s", "frac": ach / int_peak, "traffic": traffic,
+                "peak_source": peak_src, "binding_unit": binding, "ms": ms_, "perms": perms_,
+                "perm_rate": perms_ / (ms_ / 1e3), "inst_per_perm": inst_per_perm}
+
+    def ntt_roof(bytes_, ms_, kernel):
+        ach = bytes_ / (ms_ / 1e3) / 1e9
+        return {"bound": "hbm", "kernel": kernel, "achieved": ach, "peak": hbm_peak,
+                "unit": "GB/s", "frac": ach / hbm_peak, "ms": ms_,
+                "peak_source": "MEASURED_PEAKS.json hbm_gbs (of measured)",
+                "binding_unit": "integer issue (issue active 62-70 %, FMA-heavy pipe 63 % in "
+                                "the ncu capture), not HBM"}
+
+    trace_roof = hash_roof(perms, hash_ms, "Poseidon2 Merkle hashing of the 2^20 x 64 trace "
+                           "commit (k_leaf leaves + levels + fused top)",
+                           traffic_per_word * info["leaves"] * args.cols)
+    trace_roof["traffic_note"] = "bytes per launch, scaled from the 2^19 x 64 ncu capture"
+    trace_ntt = ntt_roof(info["ntt_bytes"], ntt_ms, "coset LDE of the 2^20 x 64 trace "
+                                                    "(k_lde_pass1 + pass2)")
+    if served_roof is not None:
+        roofline = hash_roof(served_roof["perms"], served_roof["hash_ms"],
+                             "Poseidon2 pair-leaf Merkle hashing of the served stream "
+                             "(k_tree_batch leaves + levels, k_tree_top), CUDA events around "
+                             "each request's tree commit on a serial replay", None)
+        roofline["traffic_note"] = ("not captured on the served stream; the leaf kernel reads "
+                                    "each codeword word once (trace capture: 1.00x the "
+                                    "algorithmic bytes)")
+        roofline_ntt = ntt_roof(served_roof["lde_bytes"], served_roof["lde_ms"],
+                                "coset LDE of the served stream (k_lde_batch phases)")
+    else:
+        roofline, roofline_ntt = trace_roof, trace_ntt
     out = {
         "metric": METRIC,
         "value": value,
@@ -912,26 +1140,14 @@ def main():
         "config": info["config"] | {"parallelism": f"replicas x{world}"},
         "e2e": {"value": e2e_value, "unit": "elem/s", "h2d_bytes_per_step": info["h2d_bytes"],
                 "d2h_bytes_per_step": info["d2h_bytes"]},
-        "roofline": {"bound": "int32",
-                     "kernel": "Poseidon2 Merkle hashing (k_leaf leaves + levels + fused top)",
-                     "achieved": achieved, "peak": int_peak, "unit": "Ginst/s",
-                     "frac": achieved / int_peak,
-                     "traffic": traffic_per_word * info["leaves"] * args.cols,
-                     "traffic_note": "bytes per launch, scaled from the 2^19 x 64 ncu capture",
-                     "peak_source": "152 SMs x 128 INT32 lanes x sm_max_mhz (MEASURED_PEAKS.json)",
-                     "binding_unit": "FMA-heavy pipe (the Montgomery products' wide and high "
-                                     "multiplies), 81 % of its peak cycles in the ncu capture",
-                     "ms": hash_ms, "perms": perms,
-                     "perm_rate": perms / (hash_ms / 1e3)},
-        "roofline_ntt": {"bound": "hbm", "kernel": "coset LDE (k_lde_pass1+pass2)",
-                         "achieved": info["ntt_bytes"] / (ntt_ms / 1e3) / 1e9, "peak": hbm_peak,
-                         "unit": "GB/s", "frac": info["ntt_bytes"] / (ntt_ms / 1e3) / 1e9 / hbm_peak,
-                         "ms": ntt_ms, "peak_source": "MEASURED_PEAKS.json hbm_gbs (of measured)",
-                         "binding_unit": "integer issue (issue active 62-70 %, FMA-heavy pipe "
-                                         "63 % in the ncu capture), not HBM"},
+        "roofline": roofline,
+        "roofline_ntt": roofline_ntt,
         "clocks": clk,
         "gpu_launches": int(launches),
     }
+    if served_roof is not None:
+        out["roofline_trace"] = trace_roof
+        out["roofline_ntt_trace"] = trace_ntt
     if served_info is not None:
         out[{"served": "served", "fri": "fri", "uneven": "batched"}[args.workload]] = served_info
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
@@ -976,7 +1192,7 @@ def reference_arm(args, rank, world):
     vals, secs, elems = [], 0.0, 0
     for _ in range(args.steps):
         if served:
-            v, s, thr, e = cpu_served_sample(args)
+            v, s, thr, e = cpu_served_sample(args, cap_log_h=REF_CAP_LOG_H)
         else:
             v, s, thr = cpu_trace_sample(log_rows, args.cols, args.log_blowup, args.queries)
             e = args.cols << log_rows
@@ -999,12 +1215,13 @@ def reference_arm(args, rank, world):
         "dtype": "u32 (BabyBear, Montgomery)",
         "data": "synthetic: seeded uniform [0, p) canonical BabyBear elements",
         "config": {"workload": (f"served stream sample: the {args.requests}-request stream with "
-                                f"heights capped at 2^{CPU_CAP_LOG_H}" if served else
+                                f"heights capped at 2^{REF_CAP_LOG_H}, per-polynomial "
+                                "pair-leaf commitments" if served else
                                 f"trace commit 2^{log_rows}x{args.cols} slice, blowup "
                                 f"{1 << args.log_blowup}, row leaves, {args.queries} openings")},
         "cpu_baseline": {"value": value, "unit": "elem/s", "cores": thr, "kind": "port",
                          "sample": ("each step: every request of the served stream, height capped "
-                                    f"at 2^{CPU_CAP_LOG_H}, incl. fold-and-open" if served else
+                                    f"at 2^{REF_CAP_LOG_H}, incl. fold-and-open" if served else
                                     f"2^{log_rows} x {args.cols} per step") +
                                    "; the reference is Python over FRX/hash-frx wheels absent "
                                    "here, so its C restatement (oracle/) runs instead"},

@@ -144,9 +144,8 @@ zc_status zc_rs_encode_bitrev(zc_field field, const uint32_t* coeffs, int64_t ba
  * caller workspace: no counterpart in the reference. For callers that cannot
  * allocate device memory at call time -- a handler inside an XLA/FRX custom
  * call (the framework owns the device memory and by default preallocates most
- * of it, so a cudaMalloc there can fail or fragment its pool), code being
- * recorded into a CUDA graph (cudaMalloc is not a stream operation and cannot
- * be captured), or a serving loop that must not stall on the allocator. The
+ * of it, so a cudaMalloc there can fail or fragment its pool), or a serving
+ * loop that must not stall on the allocator. The
  * four-step intermediate lives in a fixed 64 MiB (2^24-word) static device
  * array that every GPU loading this library holds until the process exits;
  * columns are processed in chunks that fit it, and a size whose single column
@@ -157,6 +156,8 @@ zc_status zc_rs_encode_bitrev(zc_field field, const uint32_t* coeffs, int64_t ba
  * them. The first call on a device performs set-up (root tables, the device
  * address of the array) and synchronises that device: make it before any
  * stream capture, and early, before another runtime preallocates the memory.
+ * A cudaDeviceReset discards that set-up with every other per-device table of
+ * this library: do not use the library on a device after resetting it.
  * Arguments and results as zc_rs_encode. */
 zc_status zc_rs_encode_noalloc(zc_field field, const uint32_t* coeffs, int64_t batch, int log_k,
                                int log_blowup, uint32_t shift_mont, uint32_t generator,
@@ -209,15 +210,35 @@ zc_status zc_strided_merkle_commit(const zc_poseidon2* p, zc_leaves leaves, int3
 zc_status zc_merkle_open(zc_leaves leaves, const uint32_t* layers, const int32_t* idx,
                          int32_t q, uint32_t* rows, uint32_t* paths, uint32_t* oob_flag,
                          void* stream);
+/* zc_merkle_open at leaf (idx[i] >> shift) mod num_leaves: a fold layer's
+ * opening at the layer position of the sampled query positions
+ * (code.layer_positions: natural order a_i = q mod (n >> (i+1)), shift 0,
+ * zorch/coding/reed_solomon.py:320-329; bit-reversed order a_i = q >> (i+1),
+ * shift i+1, :521-528; opened by _open_one, zorch/pcs/fri/prover.py:176-181),
+ * with the reduction done by the kernel. Every index is in range by
+ * construction, so there is no flag. shift in [0, 31]. */
+zc_status zc_merkle_open_reduced(zc_leaves leaves, const uint32_t* layers, const int32_t* idx,
+                                 int32_t q, int32_t shift, uint32_t* rows, uint32_t* paths,
+                                 void* stream);
 
 /* Batched commit of many trees (the per-matrix MerkleTree.commit calls of a
- * batch, zorch/commit/merkle.py:118-202) in 1 + (max depth - 8) + 1 launches.
- * workspace: >= 256 bytes, 256-byte aligned (per-launch work counters). */
+ * batch, zorch/commit/merkle.py:118-202, and the per-polynomial _commit_one
+ * calls of FriProver.commit, zorch/pcs/fri/prover.py:92-99, 141-148) in
+ * 1 + (max depth - 8) + 1 launches. A job with count > 1 is a family of
+ * `count` trees of one shape: tree t hashes the leaves of `leaves` with its
+ * base moved by t*leaf_stride words and writes its layers at
+ * layers + t*layer_stride (e.g. each column of a [w, n] codeword as its own
+ * pair-leaf tree). workspace: >= 256 bytes, 256-byte aligned (per-launch work
+ * counters). */
 typedef struct {
   zc_leaves leaves;
-  uint32_t* layers; /* (2L-1)*8 words */
-  int32_t top_log;  /* the levels of <= 2^top_log nodes run fused in one CTA per
-                       tree (half-warp permutations), 1..8; 0: default 8 */
+  uint32_t* layers;     /* (2L-1)*8 words per tree */
+  int32_t top_log;      /* the levels of <= 2^top_log nodes run fused in one CTA per
+                           tree (half-warp permutations), 1..8; 0: default 8 */
+  int32_t count;        /* trees in the family; 0 or 1: one tree */
+  int64_t leaf_stride;  /* words between successive trees' leaf bases */
+  int64_t layer_stride; /* words between successive trees' layers, >= (2L-1)*8,
+                           a multiple of 4 */
 } zc_merkle_job;
 zc_status zc_merkle_commit_batch(const zc_poseidon2* p, const zc_merkle_job* jobs,
                                  int32_t njobs, void* workspace, size_t workspace_bytes,
@@ -272,6 +293,27 @@ zc_status zc_fri_fold_commit_bitrev(const zc_poseidon2* p, const uint32_t* cw, i
  * aligned). */
 zc_status zc_smcs_bind_root(const zc_poseidon2* p, const uint32_t* raw_root, uint32_t log_height,
                             uint32_t width, uint32_t* out, void* stream);
+
+/* ---- FRI open: the DEEP quotient --------------------------------------- */
+/* Replaces _eval_poly (zorch/pcs/fri/prover.py:42-49): out = sum_i
+ * coeffs[i] z^i for k >= 1 base coefficients, z a base element (z_limbs = 1)
+ * or an EF4 element (z_limbs = 4, out 16-byte aligned); out has z_limbs words.
+ * workspace: zc_eval_poly_workspace_bytes(k) bytes, 16-byte aligned. */
+size_t zc_eval_poly_workspace_bytes(int64_t k);
+zc_status zc_eval_poly(zc_field field, const uint32_t* coeffs, int64_t k, const uint32_t* z,
+                       int32_t z_limbs, uint32_t* out, void* workspace, size_t workspace_bytes,
+                       void* stream);
+/* The layer-0 DEEP quotient of _open_one (zorch/pcs/fri/prover.py:160-164):
+ * out[j] = (cw[j] - v) / (x_j - z) over the n-point evaluation domain, x_j =
+ * shift * w_n^j (bit_reversed = 0) or shift * w_n^brev(j) (the
+ * BitReversedReedSolomon codeword order); z and v (device words) have z_limbs
+ * (1 or 4) limbs, and so does each output element (EF4 output 16-byte
+ * aligned). A zero denominator (z on the domain) gives a zero quotient.
+ * shift_mont 0: no coset. generator as zc_rs_encode. */
+zc_status zc_deep_quotient(zc_field field, const uint32_t* cw, int64_t n, const uint32_t* z,
+                           int32_t z_limbs, const uint32_t* v, uint32_t shift_mont,
+                           uint32_t generator, int32_t bit_reversed, uint32_t* out,
+                           void* stream);
 
 /* ---- Basefold open: the multilinear side ------------------------------ */
 /* EF4 values are 4 Montgomery words (c0..c3), 16-byte aligned on the device.

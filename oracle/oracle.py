@@ -82,6 +82,8 @@ def _load() -> C.CDLL:
         "orc_rlc_columns": (None, [i32, _u32p, i64, i32, _u32p, _u32p]),
         "orc_fri_commit_phase": (i32, [vp, i32, _u32p, i32, i32, u32, u32, i32, i32, i32, vp,
                                        _u32p, _u32p, _u32p, _i32p, _u32p, _u32p]),
+        "orc_eval_poly_ef4": (None, [i32, _u32p, i64, _u32p, _u32p]),
+        "orc_deep_quotient": (i32, [i32, _u32p, i64, _u32p, i32, _u32p, u32, u32, i32, _u32p]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(lib, name)
@@ -527,6 +529,72 @@ def fri_commit_phase(p2: Poseidon2, field: int, codeword, num_rounds: int, num_q
         ro += row_sizes[r]
         po += path_sizes[r]
     return CommitPhaseProof(roots, betas, final, pos, rl, pl)
+
+
+# ---------------------------------------------------------------- FRI open --
+def eval_poly_at(field: int, coeffs, z) -> np.ndarray:
+    """f(z) (_eval_poly, zorch/pcs/fri/prover.py:42-49) for a base point
+    (1 word) or an EF4 point (4 words); Montgomery words in and out."""
+    c = u32(coeffs).reshape(-1)
+    z = u32(z).reshape(-1)
+    if z.size == 1:
+        return np.array([LIB.orc_eval_poly(field, c, c.size, int(z[0]))], np.uint32)
+    out = np.zeros(4, np.uint32)
+    LIB.orc_eval_poly_ef4(field, c, c.size, z, out)
+    return out
+
+
+def deep_quotient(field: int, cw, z, v, shift_mont: int = 0, generator: int = 0,
+                  bit_reversed: bool = False) -> np.ndarray:
+    """(cw - v) / (domain - z) (zorch/pcs/fri/prover.py:164): [n] for a base
+    point, [n, 4] for an EF4 point."""
+    cw = u32(cw).reshape(-1)
+    z = u32(z).reshape(-1)
+    v = u32(v).reshape(-1)
+    limbs = z.size
+    out = np.zeros(cw.size * limbs, np.uint32)
+    rc = LIB.orc_deep_quotient(field, cw, cw.size, z, limbs, v, shift_mont, generator,
+                               int(bit_reversed), out)
+    if rc:
+        raise ValueError(f"deep_quotient failed ({rc})")
+    return out if limbs == 1 else out.reshape(-1, 4)
+
+
+@dataclass
+class FriOpenProof:
+    """FriProof (zorch/pcs/fri/config.py:56-69) in pytree flatten order:
+    value, fri_roots, final_layer, f_opening (row, path), query openings."""
+
+    value: np.ndarray
+    phase: CommitPhaseProof
+    f_rows: np.ndarray
+    f_paths: np.ndarray
+
+    def to_bytes(self) -> bytes:
+        parts = [self.value, self.phase.roots, self.phase.final_layer, self.f_rows, self.f_paths]
+        for r, p in zip(self.phase.rows, self.phase.paths):
+            parts += [r, p]
+        return b"".join(np.ascontiguousarray(x, dtype="<u4").tobytes() for x in parts)
+
+
+def fri_open(p2: Poseidon2, field: int, coeffs, codeword, f_layers, z, num_rounds: int,
+             num_queries: int, beta_limbs: int, transcript: Transcript, shift_mont: int = 0,
+             generator: int = 0) -> FriOpenProof:
+    """_open_one (zorch/pcs/fri/prover.py:151-187) on a natural-order
+    codeword with its committed pair-leaf layers: v = f(z); the DEEP quotient
+    layer; observe f's root; the fold rounds, final layer and positions
+    (fri_commit_phase); f's pair leaf opened at each position mod n/2.
+    `transcript` is advanced in place."""
+    cw = u32(codeword).reshape(-1)
+    n = cw.size
+    v = eval_poly_at(field, coeffs, z)
+    q = deep_quotient(field, cw, z, v, shift_mont, generator)
+    transcript.observe(f_layers[-1][0])
+    phase = fri_commit_phase(p2, field, q, num_rounds, num_queries, beta_limbs, transcript,
+                             shift_mont, generator)
+    a0 = (phase.positions.astype(np.int64) % (n // 2)).astype(np.int32)
+    rows, paths = merkle_open(cw, n // 2, 2, 1, n // 2, f_layers, a0)
+    return FriOpenProof(v, phase, rows, paths)
 
 
 # ------------------------------------------------------------ basefold open --

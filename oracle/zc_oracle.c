@@ -745,6 +745,84 @@ void orc_ef4_inv(int field, const uint32_t* a, uint32_t* out) {
   memcpy(out, r, 16);
 }
 
+/* f(z) for an EF4 point z: Horner over the base coefficients
+ * (_eval_poly, zorch/pcs/fri/prover.py:42-49, with z in the extension). */
+void orc_eval_poly_ef4(int field, const uint32_t* coeffs, int64_t k, const uint32_t* z,
+                       uint32_t* out) {
+  const fld* F = FLD(field);
+  uint32_t acc[4] = {0, 0, 0, 0};
+  for (int64_t i = k - 1; i >= 0; i--) {
+    ef4_mul(F, acc, z, acc);
+    acc[0] = fadd(F, acc[0], coeffs[i]);
+  }
+  memcpy(out, acc, 16);
+}
+
+/* The DEEP quotient of _open_one (zorch/pcs/fri/prover.py:160-164):
+ * out[j] = (cw[j] - v) / (x_j - z) with x_j = shift * w^j (natural order) or
+ * shift * w^brev(j) (bit-reversed codeword), z and v of z_limbs (1 or 4)
+ * limbs; out has z_limbs limbs per element. Inverses by blocks of 1024:
+ * prefix products, one inversion per block (Fermat), back substitution; a zero
+ * denominator gives a zero quotient. */
+int orc_deep_quotient(int field, const uint32_t* cw, int64_t n, const uint32_t* z, int z_limbs,
+                      const uint32_t* v, uint32_t shift_mont, uint32_t generator, int bitrev,
+                      uint32_t* out) {
+  const fld* F = FLD(field);
+  if (!is_pow2(n) || (z_limbs != 1 && z_limbs != 4)) return 1;
+  int log_n = 0;
+  while (((int64_t)1 << log_n) < n) log_n++;
+  const uint32_t w = log_n ? root_of_unity(F, log_n, generator) : F->one;
+  const uint32_t sh = shift_mont ? shift_mont : F->one;
+  const int64_t B = 1024;
+  const int64_t nblocks = (n + B - 1) / B;
+#pragma omp parallel for num_threads(orc_get_threads()) schedule(static)
+  for (int64_t b = 0; b < nblocks; b++) {
+    uint32_t(*den)[4] = malloc(sizeof(uint32_t[4]) * (size_t)B);
+    uint32_t(*pre)[4] = malloc(sizeof(uint32_t[4]) * (size_t)B);
+    char* zero = malloc((size_t)B);
+    const int64_t j0 = b * B;
+    const int64_t m = n - j0 < B ? n - j0 : B;
+    uint32_t acc[4] = {F->one, 0, 0, 0};
+    for (int64_t i = 0; i < m; i++) {
+      const int64_t j = j0 + i;
+      const int64_t e = bitrev ? brev64(j, log_n) : j;
+      const uint32_t x = fmul(F, sh, fpow(F, w, (uint64_t)e));
+      uint32_t d[4] = {fsub(F, x, z[0]), 0, 0, 0};
+      if (z_limbs == 4)
+        for (int l = 1; l < 4; l++) d[l] = fsub(F, 0, z[l]);
+      zero[i] = (d[0] | d[1] | d[2] | d[3]) == 0;
+      if (zero[i]) d[0] = F->one;
+      memcpy(den[i], d, 16);
+      ef4_mul(F, acc, d, acc);
+      memcpy(pre[i], acc, 16);
+    }
+    uint32_t inv[4];
+    if (z_limbs == 1) {
+      inv[0] = finv(F, acc[0]);
+      inv[1] = inv[2] = inv[3] = 0;
+    } else {
+      orc_ef4_inv(field, acc, inv);
+    }
+    for (int64_t i = m - 1; i >= 0; i--) {
+      uint32_t di[4];
+      if (i) ef4_mul(F, inv, pre[i - 1], di);
+      else memcpy(di, inv, 16);
+      if (i) ef4_mul(F, inv, den[i], inv);
+      uint32_t num[4] = {fsub(F, cw[j0 + i], v[0]), 0, 0, 0};
+      if (z_limbs == 4)
+        for (int l = 1; l < 4; l++) num[l] = fsub(F, 0, v[l]);
+      uint32_t q[4];
+      ef4_mul(F, num, di, q);
+      if (zero[i]) q[0] = q[1] = q[2] = q[3] = 0;
+      memcpy(out + (j0 + i) * z_limbs, q, sizeof(uint32_t) * (size_t)z_limbs);
+    }
+    free(den);
+    free(pre);
+    free(zero);
+  }
+  return 0;
+}
+
 /* expand_eq_to_hypercube(z, 1) (zorch/poly/eq.py:92-130, expand_hypercube_step
  * :55-62): eq(w, z) for w in {0,1}^m, z[0] on the most significant index bit;
  * each step splits an entry s into (s - s z_j, s z_j) at (2i, 2i+1). */

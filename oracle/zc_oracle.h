@@ -133,6 +133,13 @@ void orc_mle_fold(int field, const uint32_t* mle, int64_t M, const uint32_t* bet
 void orc_rlc_columns_ex(int field, const uint32_t* cw, int64_t n, int w, const uint32_t* chal,
                         int nbv, int offset, int accumulate, uint32_t* out);
 
+/* FRI open: f(z) for an EF4 point, and the DEEP quotient (cw - v)/(x - z). */
+void orc_eval_poly_ef4(int field, const uint32_t* coeffs, int64_t k, const uint32_t* z,
+                       uint32_t* out);
+int orc_deep_quotient(int field, const uint32_t* cw, int64_t n, const uint32_t* z, int z_limbs,
+                      const uint32_t* v, uint32_t shift_mont, uint32_t generator, int bitrev,
+                      uint32_t* out);
+
 /* Duplex transcript (overwrite mode, rate 8, width 16) */
 void orc_duplex_init(orc_duplex* t);
 void orc_duplex_observe(const orc_p2* p, orc_duplex* t, const uint32_t* v, int64_t m);

@@ -9,6 +9,7 @@ import pytest
 torch = pytest.importorskip("torch")
 pytestmark = pytest.mark.gpu
 
+import serve_oracle  # noqa: E402
 from zorch_gb300 import _lib  # noqa: E402
 from zorch_gb300.field import BABYBEAR, to_host  # noqa: E402
 
@@ -141,65 +142,98 @@ def _small_stream(seed, n=10):
     return reqs
 
 
-def test_served_results_same_alone_and_in_the_mix():
+@pytest.mark.parametrize("mode", ["fri", "matrix"])
+def test_served_results_same_alone_and_in_the_mix(mode):
     from zorch_gb300.serve import Server
 
     reqs = _small_stream(11)
-    mixed = Server(max_batch=6, streams=2).run(reqs)
+    mixed = Server(max_batch=6, streams=2, mode=mode).run(reqs)
     assert [r.rid for r in mixed] == [r.rid for r in reqs]
     for r, m in zip(reqs, mixed):
-        alone = Server(max_batch=1, streams=1).run([r])[0]
+        alone = Server(max_batch=1, streams=1, mode=mode).run([r])[0]
         assert alone.proof == m.proof
-        assert len(m.proof) > 32 if r.fold else len(m.proof) == 32
+        head = 32 * (r.width if mode == "fri" else 1)
+        assert len(m.proof) > head if r.fold else len(m.proof) == head
+
+
+@pytest.mark.parametrize("mode", ["fri", "matrix"])
+def test_served_bytes_equal_plain_path(mode):
+    """Like for like: every request of a mixed stream gets the same bytes from
+    the continuous-batching server as from the plain one-call-per-polynomial
+    ("fri", FriProver.commit per column) or one-call-per-matrix ("matrix",
+    BasefoldProver.commit) drop-in path."""
+    from zorch_gb300.serve import Server, run_plain
+
+    reqs = _small_stream(17, 12)
+    served = Server(max_batch=5, streams=3, mode=mode).run(reqs)
+    plain = run_plain(reqs, mode=mode)
+    assert [r.rid for r in served] == [r.rid for r in plain]
+    for a, b in zip(served, plain):
+        assert a.proof == b.proof
+
+
+def test_batched_pair_trees_equal_per_polynomial_commit(orc):
+    """BatchCommitter.commit_polys (every column's pair-leaf tree, tree families
+    in one batched commit) == FriProver.commit_one per column == the oracle."""
+    from zorch_gb300.batch import BatchCommitter, MatrixJob
+    from zorch_gb300.coding import ReedSolomon
+    from zorch_gb300.commit import MerkleTree
+    from zorch_gb300.pcs import FriParams, FriProver
+
+    mats = _mats(21)
+    bc = BatchCommitter()
+    committed = bc.commit_polys([MatrixJob(x, lb) for x, lb in mats])
+    p2 = orc.Poseidon2.babybear16()
+    for (x, lb), c in zip(mats, committed):
+        h = x.shape[1]
+        code = ReedSolomon(h, 1 << lb, BABYBEAR, coset_shift=31, generator=31)
+        prover = FriProver(FriParams(code, MerkleTree(bc.perm), 0, 0))
+        for col in range(0, x.shape[0], max(1, x.shape[0] // 5)):
+            cp = prover.commit_one(x[col])
+            assert torch.equal(cp.codeword, c.codeword[col])
+            assert torch.equal(cp.digest_layers.flat, c.flat[col])
+            assert torch.equal(cp.root, c.roots[col])
+            if c.codeword.shape[1] <= (1 << 14):
+                cw = to_host(c.codeword[col])
+                L = cw.size // 2
+                want = orc.merkle_commit(p2, cw, L, 2, 1, L)
+                assert np.array_equal(to_host(c.roots[col]), want[-1][0])
 
 
 def test_served_host_fed_equals_resident():
-    """Inputs fed from page-locked host memory (copy-engine copies on side
-    streams, then the in-place conversion) give the same proofs as inputs
-    already on the device; likewise for the plain path."""
+    """Inputs fed from page-locked host memory (read by the conversion kernel
+    over the host link) give the same proofs as inputs already on the device;
+    likewise for the plain path."""
     from zorch_gb300.serve import Server, run_plain
 
     reqs = _small_stream(13)
     for r in reqs:
         r.host = r.resident.cpu().pin_memory()
-    server = Server(max_batch=4, streams=3)
-    resident = server.run(reqs)
-    fed = server.run(reqs, host_fed=True)
-    assert [a.proof for a in resident] == [b.proof for b in fed]
-    plain_fed = run_plain(reqs, host_fed=True, perm=server.perm)
-    plain = run_plain(reqs, perm=server.perm)
-    assert [a.proof for a in plain] == [b.proof for b in plain_fed]
+    for mode in ("fri", "matrix"):
+        server = Server(max_batch=4, streams=3, mode=mode)
+        resident = server.run(reqs)
+        fed = server.run(reqs, host_fed=True)
+        assert [a.proof for a in resident] == [b.proof for b in fed]
+        plain_fed = run_plain(reqs, host_fed=True, perm=server.perm, mode=mode)
+        plain = run_plain(reqs, perm=server.perm, mode=mode)
+        assert [a.proof for a in plain] == [b.proof for b in plain_fed]
+        assert [a.proof for a in plain] == [b.proof for b in resident]
 
 
-def test_served_fold_proofs_match_oracle(orc):
-    """Root of the row-leaf tree and the fold-and-open proof bytes of a served
-    request equal the oracle's, replayed from the same seeded data."""
-    from zorch_gb300.serve import FOLD_FINAL_LOG, FOLD_QUERIES, Server
+@pytest.mark.parametrize("mode", ["fri", "matrix"])
+def test_served_proofs_match_oracle(orc, mode):
+    """Commitment and fold-and-open proof bytes of served requests equal the
+    oracle's, replayed from the same seeded data."""
+    from zorch_gb300.serve import Server
 
-    reqs = [r for r in _small_stream(12, 8) if r.fold][:2]
-    res = Server().run(reqs)
+    reqs = _small_stream(12, 8)
+    reqs = [r for r in reqs if r.fold][:2] + [r for r in reqs if not r.fold][:2]
+    res = Server(mode=mode).run(reqs)
     p2 = orc.Poseidon2.babybear16()
-    for r, got in zip(reqs, res):
+    for r, got in zip(sorted(reqs, key=lambda q: q.rid), res):
         x = orc.to_mont(0, to_host(r.resident))
-        cw = orc.rs_encode(0, x, r.log_blowup, BABYBEAR.mont(31))
-        layers = orc.merkle_commit_columns(p2, cw)
-        root = layers[-1][0]
-        words = np.frombuffer(got.proof, dtype=np.uint32)
-        assert np.array_equal(words[:8], root)
-        t = orc.Transcript(p2)
-        t.observe(root)
-        nbv = (cw.shape[0] - 1).bit_length()
-        rlc = orc.rlc_columns(0, cw, t.sample(4 * nbv) if nbv else [])
-        rounds = r.log_h + r.log_blowup - FOLD_FINAL_LOG
-        t.observe([BABYBEAR.mont(rounds)])
-        proof = orc.fri_commit_phase(p2, 0, rlc, rounds, FOLD_QUERIES, 4, t, BABYBEAR.mont(31))
-        n = cw.shape[1]
-        rows, paths = orc.merkle_open(cw, n, cw.shape[0], 1, n, layers, proof.positions)
-        parts = [root, proof.roots.reshape(-1), proof.final_layer.reshape(-1),
-                 proof.positions.astype(np.uint32), rows.reshape(-1), paths.reshape(-1)]
-        for rr, pp in zip(proof.rows, proof.paths):
-            parts += [rr.reshape(-1), pp.reshape(-1)]
-        assert np.array_equal(words, np.concatenate(parts))
+        want = serve_oracle.request_words(orc, p2, r, x, mode)
+        assert np.array_equal(np.frombuffer(got.proof, dtype=np.uint32), want)
 
 
 def test_partial_lagrange_batching_matches_oracle(orc):
@@ -227,7 +261,7 @@ def test_plain_path_per_polynomial_roots(orc):
     from zorch_gb300.serve import run_plain
 
     reqs = [r for r in _small_stream(13, 6)][:3]
-    res = run_plain(reqs)
+    res = run_plain(reqs, mode="fri")
     p2 = orc.Poseidon2.babybear16()
     for r, got in zip(reqs, res):
         x = orc.to_mont(0, to_host(r.resident))
@@ -237,3 +271,19 @@ def test_plain_path_per_polynomial_roots(orc):
             L = cw.size // 2
             root = orc.merkle_commit(p2, cw, L, 2, 1, L)[-1][0]
             assert np.array_equal(words[8 * c: 8 * c + 8], root)
+
+
+def test_chunked_pair_trees_keep_roots():
+    """Trees committed in column chunks through a reused buffer (the unopened
+    wide requests of the server) give the same roots as the whole family."""
+    from zorch_gb300.batch import BatchCommitter, MatrixJob
+
+    mats = _mats(22)
+    bc = BatchCommitter()
+    jobs = [MatrixJob(x, lb) for x, lb in mats]
+    whole = bc.commit_polys(jobs)
+    for cap in (1, 32 * 3 * (1 << 15)):
+        chunked = bc.commit_polys(jobs, keep_layers=[False] * len(jobs), layer_cap=cap)
+        for a, b in zip(whole, chunked):
+            assert torch.equal(a.roots, b.roots)
+            assert torch.equal(a.codeword, b.codeword)

@@ -1,13 +1,20 @@
-"""The configurations at their full sizes.
+"""The configurations at their full sizes, byte for byte against the oracle
+(its C restatement runs with OpenMP on every host core):
 
-Where the oracle finishes in seconds the comparison is byte for byte (the
-config-3 commit phase at 2^22 coefficients, blowup 2, 15 rounds, 100
-queries). Where it would not (the 2^20 x 64 trace at blowup 4, the 48-matrix
-uneven batch), size-independent properties are checked instead: every opened
-row equals the codeword there, every authentication path rebuilds the root
-through the oracle's hash, codeword entries equal a Horner evaluation of the
-message on the coset domain, internal nodes equal the compression of their
-children, and the batched path equals the per-matrix path exactly.
+- config 2: the 2^20 x 64 trace at blowup 4 -- the root and all 128 opened
+  rows and authentication paths;
+- config 3: the FRI commit phase at 2^22 coefficients, blowup 2, 15 rounds,
+  100 queries -- the proof bytes;
+- config 4: the bench's own 48 seeded uneven matrices -- all 48 roots of the
+  batched commit;
+- config 5: the bench's own 24-request served stream -- every request of at
+  most 2^20 rows (commitment and fold-and-open proof, per-polynomial and
+  row-leaf modes); the taller requests equal the plain path's bytes, and
+  one column of the tallest request equals the oracle's pair-leaf root.
+
+Size-independent properties are checked beside the bytes: opened rows equal
+the codeword, paths rebuild the root through the oracle's hash, codeword
+entries equal a Horner evaluation of the message on the coset domain.
 """
 
 from __future__ import annotations
@@ -34,7 +41,7 @@ def _canonical(shape, seed):
                                                 dtype=np.uint64).astype(np.uint32)
 
 
-def test_config2_trace_commit_properties(orc):
+def test_config2_trace_commit_bytes(orc):
     from zorch_gb300.coding import ReedSolomon
     from zorch_gb300.commit import MerkleTree, Poseidon2
     from zorch_gb300.pcs import BasefoldProver
@@ -49,30 +56,24 @@ def test_config2_trace_commit_properties(orc):
     rng = np.random.default_rng(3)
     idx = rng.integers(0, n, size=Q).astype(np.int32)
     op = prover.open_rows(data, torch.from_numpy(idx).cuda())
+    root_h, rows, paths = to_host(root), to_host(op.row), to_host(op.path)
+    # the oracle: LDE, row-leaf tree, openings
     p2 = orc.Poseidon2.babybear16()
-    root_h = to_host(root)
-    rows, paths = to_host(op.row), to_host(op.path)
-    cw_cols = {}
-    for q in range(Q):
-        assert np.array_equal(orc.reconstruct_root(p2, rows[q], int(idx[q]), paths[:, q]), root_h)
-    # opened rows are the codeword's rows
-    cw = data.codeword
-    gathered = to_host(cw[:, torch.from_numpy(idx).long().cuda()].T.contiguous())
-    assert np.array_equal(gathered, rows)
-    # codeword entries = Horner of the message on shift * w^j
     xm_h = orc.to_mont(0, x)
+    cw_o = orc.rs_encode(0, xm_h, log_b, BABYBEAR.mont(31))
+    layers = orc.merkle_commit_columns(p2, cw_o)
+    rows_o, paths_o = orc.merkle_open(cw_o, n, w, 1, n, layers, idx)
+    assert np.array_equal(root_h, layers[-1][0])
+    assert np.array_equal(rows, rows_o.reshape(rows.shape))
+    assert np.array_equal(paths, paths_o.reshape(paths.shape))
+    # properties beside the bytes: paths rebuild the root, entries are Horner
+    for q in range(0, Q, 16):
+        assert np.array_equal(orc.reconstruct_root(p2, rows[q], int(idx[q]), paths[:, q]), root_h)
     sh = BABYBEAR.mont(31)
     for c in rng.integers(0, w, size=3):
         for j in rng.integers(0, n, size=4):
             pt = orc.domain_point(0, log_h + log_b, sh, int(j))
-            cw_cols.setdefault(int(c), None)
-            assert int(to_host(cw[int(c), int(j)].reshape(1))[0]) == orc.eval_poly(0, xm_h[c], pt)
-    # internal nodes compress their children
-    for level in (1, 5, 12, 22):
-        lay, below = to_host(data.digest_layers[level]), data.digest_layers[level - 1]
-        for i in rng.integers(0, lay.shape[0], size=3):
-            kids = to_host(below[2 * int(i): 2 * int(i) + 2])
-            assert np.array_equal(lay[i], p2.compress(kids[0], kids[1]))
+            assert int(cw_o[int(c), int(j)]) == orc.eval_poly(0, xm_h[c], pt)
 
 
 def test_config3_fri_commit_phase_full_size_bytes(orc):
@@ -99,39 +100,74 @@ def test_config3_fri_commit_phase_full_size_bytes(orc):
     assert got == want.to_bytes()
 
 
-def test_config4_uneven_batch_equals_per_matrix(orc):
-    """48 matrices, log2 heights 12..22, widths 1..128, blowup 2/4/8, one
-    batched launch set vs 48 per-matrix commits; paths verify via the oracle."""
+def test_config4_uneven_batch_bytes(orc):
+    """The bench's 48 uneven matrices (seed 5: widths 1..128, log2 heights
+    12..22, blowup 2/4/8, zc_fill_uniform data seeded 900 + i), one batched
+    commit: every codeword's root equals the oracle's, and a per-matrix
+    commit gives the same digest layers."""
     from zorch_gb300.batch import BatchCommitter, MatrixJob
     from zorch_gb300.commit import MerkleTree
     from zorch_gb300.field import ptr, stream_handle
 
-    rng = np.random.default_rng(44)
+    rng = np.random.default_rng(5)
     shapes = [(int(rng.integers(1, 129)), int(rng.integers(12, 23)), int(rng.choice([1, 2, 3])))
               for _ in range(48)]
-    mats = []
+    canon = []
     for i, (w, lh, lb) in enumerate(shapes):
         xx = torch.empty((w, 1 << lh), dtype=torch.int32, device="cuda")
-        _lib.check(_lib.lib().zc_fill_uniform(0, ptr(xx), xx.numel(), 4400 + i, stream_handle()),
+        _lib.check(_lib.lib().zc_fill_uniform(0, ptr(xx), xx.numel(), 900 + i, stream_handle()),
                    "fill")
-        mats.append((to_mont(BABYBEAR, xx), lb))
+        canon.append(xx)
     bc = BatchCommitter()
-    batched = bc.commit([MatrixJob(x, lb) for x, lb in mats])
+    batched = bc.commit([MatrixJob(to_mont(BABYBEAR, x), lb) for x, (_, _, lb) in
+                         zip(canon, shapes)])
+    roots = [to_host(b.root) for b in batched]
     tree = MerkleTree(bc.perm, column_major=True)
-    from zorch_gb300.coding import rs_encode
-
-    p2 = orc.Poseidon2.babybear16()
-    for (x, lb), b in zip(mats, batched):
-        cw = rs_encode(BABYBEAR, x, lb, BABYBEAR.mont(31), 0)
-        assert torch.equal(cw, b.codeword)
-        root, _ = tree.commit(cw)
-        assert torch.equal(root, b.root)
-        idx = torch.from_numpy(rng.integers(0, cw.shape[1], size=2).astype(np.int32)).cuda()
-        op = tree.open_layout(_lib.Leaves(ptr(cw), cw.shape[1], cw.shape[0], 1, cw.shape[1]),
-                              b.layers, idx, cw.shape[0])
-        rows, paths = to_host(op.row), to_host(op.path)
-        for q in range(2):
-            assert np.array_equal(
-                orc.reconstruct_root(p2, rows[q], int(idx[q]), paths[:, q]), to_host(b.root))
-    del batched
+    for b in batched[:6]:  # per-matrix commit == batched, layer for layer
+        _, layers = tree.commit(b.codeword)
+        assert torch.equal(layers.flat, b.layers.flat)
+    hosts = [to_host(x) for x in canon]
+    del batched, canon
     torch.cuda.empty_cache()
+    p2 = orc.Poseidon2.babybear16()
+    for (w, lh, lb), x, root in zip(shapes, hosts, roots):
+        cw = orc.rs_encode(0, orc.to_mont(0, x), lb, BABYBEAR.mont(31))
+        assert np.array_equal(orc.merkle_commit_columns(p2, cw)[-1][0], root), (w, lh, lb)
+        del cw
+
+
+def test_config5_served_stream_bytes(orc):
+    """The bench's 24-request stream (seed 5, heights 2^14..2^24, widths
+    1..256, blowup 2|4, 30% fold-and-open) served in both modes: each request
+    of at most 2^20 rows is byte-identical to the oracle's replay; every
+    taller one equals the plain path's bytes, and the tallest request's first
+    column root equals the oracle's pair-leaf root."""
+    import serve_oracle
+    from zorch_gb300.serve import Server, fill_request, make_stream, run_plain
+
+    reqs = make_stream(24, 5, rate_hz=0.0, log_h=(14, 24))
+    for r in reqs:
+        fill_request(r)
+    torch.cuda.synchronize()
+    p2 = orc.Poseidon2.babybear16()
+    for mode in ("fri", "matrix"):
+        served = Server(max_batch=8, streams=4, mode=mode).run(reqs)
+        small = [r for r in reqs if r.log_h <= 20]
+        tall = [r for r in reqs if r.log_h > 20]
+        assert len(small) >= 12
+        for r in small:
+            want = serve_oracle.request_words(orc, p2, r, orc.to_mont(0, to_host(r.resident)),
+                                              mode)
+            assert np.array_equal(np.frombuffer(served[r.rid].proof, np.uint32), want), r
+        plain = run_plain(tall, mode=mode)
+        for r, pl in zip(tall, plain):
+            assert served[r.rid].proof == pl.proof, r
+        if mode == "fri":
+            top = max(tall, key=lambda q: (q.log_h, q.log_blowup))
+            col = orc.to_mont(0, to_host(top.resident[0]))
+            cw = orc.rs_encode(0, col, top.log_blowup, BABYBEAR.mont(31))
+            L = cw.size // 2
+            root = orc.merkle_commit(p2, cw, L, 2, 1, L)[-1][0]
+            assert np.array_equal(np.frombuffer(served[top.rid].proof, np.uint32)[:8], root)
+        del served
+        torch.cuda.empty_cache()

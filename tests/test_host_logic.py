@@ -116,3 +116,17 @@ def test_batch_committer_choice_prefers_overrides():
     assert bc._choice(20, 8) == {"tile": 13, "radix": 4, "top": 6}
     bc.tuner = None
     assert bc._choice(20, 8) == {"tile": 0, "radix": 4, "top": 0}
+
+
+def test_xla_ffi_shim_is_header_gated(tmp_path, monkeypatch):
+    """libzc_xla.so is built only where xla/ffi/api/ffi.h is found; the
+    committed handlers name the four custom-call targets."""
+    from zorch_gb300 import build as zb
+
+    monkeypatch.setenv("XLA_FFI_INCLUDE_DIR", str(tmp_path))
+    if zb.xla_ffi_include_dir() is None:
+        assert zb.build_xla() is None
+    src = zb.XLA_SRC.read_text()
+    for name in ("zc_rs_encode_ffi", "zc_merkle_commit_ffi", "zc_fri_fold_commit_ffi",
+                 "zc_duplex_hop_ffi"):
+        assert f"XLA_FFI_DEFINE_HANDLER_SYMBOL({name}," in src

@@ -1,13 +1,13 @@
 """zc_rs_encode_noalloc: the LDE entry point that allocates nothing.
 
-It exists for callers that cannot allocate device memory when they call in
-(an XLA/FRX custom-call handler whose framework owns and preallocates the
-GPU's memory, a sequence being recorded into a CUDA graph, a serving loop
-that must not stall on the allocator). Its four-step intermediate lives in a
-fixed 64 MiB static device array; this file checks, through the C ABI, that
-its output equals the workspace entry point's (zc_rs_encode) exactly, on two
-calls in a row, and that a column too large for the fixed array is refused.
-Collected last on purpose: the other GPU tests have run when it runs.
+It exists for callers that cannot allocate device memory when they call in:
+an XLA/FRX custom-call handler, whose framework owns the GPU's memory and
+preallocates most of it, or a serving loop that must not stall on the
+allocator. Its four-step intermediate lives in a fixed 64 MiB static device
+array; this file checks, through the C ABI, that its output equals the
+workspace entry point's (zc_rs_encode) exactly, on two calls in a row, and
+that a column too large for the fixed array is refused. Collected last on
+purpose: the other GPU tests have run when it runs.
 """
 
 from __future__ import annotations
@@ -20,9 +20,11 @@ pytestmark = pytest.mark.gpu
 from zorch_gb300 import _lib  # noqa: E402
 from zorch_gb300.field import BABYBEAR, KOALABEAR, ptr, stream_handle  # noqa: E402
 
-# (field, batch, log_k, log_blowup): four-step sizes that use the scratch; the
-# last one needs several chunks (2^22-word columns, 4 per 2^24-word chunk).
-CASES = [(BABYBEAR, 3, 16, 2), (KOALABEAR, 2, 13, 3), (BABYBEAR, 6, 20, 2), (BABYBEAR, 2, 10, 1)]
+# (field, batch, log_k, log_blowup): every case is past the single-pass size
+# (k > 4096 or k * blowup > 2^14), so each runs the four-step passes through
+# the scratch; the third needs several chunks (2^22-word columns, 4 per
+# 2^24-word chunk).
+CASES = [(BABYBEAR, 3, 16, 2), (KOALABEAR, 2, 13, 3), (BABYBEAR, 6, 20, 2), (KOALABEAR, 5, 14, 1)]
 
 
 @pytest.fixture(scope="module", autouse=True)

@@ -40,7 +40,8 @@ class Leaves(C.Structure):
 
 
 class MerkleJob(C.Structure):
-    _fields_ = [("leaves", Leaves), ("layers", C.c_void_p), ("top_log", C.c_int32)]
+    _fields_ = [("leaves", Leaves), ("layers", C.c_void_p), ("top_log", C.c_int32),
+                ("count", C.c_int32), ("leaf_stride", C.c_int64), ("layer_stride", C.c_int64)]
 
 
 _lock = threading.Lock()
@@ -73,6 +74,7 @@ def _declare(lib: C.CDLL) -> None:
         "zc_rs_encode_bitrev": (st, [st, vp, i64, C.c_int, C.c_int, u32, u32, vp, vp, sz, vp]),
         "zc_merkle_commit": (st, [vp, Leaves, vp, vp]),
         "zc_merkle_open": (st, [Leaves, vp, vp, i32, vp, vp, vp, vp]),
+        "zc_merkle_open_reduced": (st, [Leaves, vp, vp, i32, i32, vp, vp, vp]),
         "zc_strided_merkle_commit": (st, [vp, Leaves, i32, vp, vp]),
         "zc_fri_fold": (st, [st, vp, i64, C.c_int, vp, C.c_int, u32, u32, vp, vp]),
         "zc_fri_fold_commit": (st, [vp, vp, i64, C.c_int, vp, C.c_int, u32, u32, vp, vp, vp]),
@@ -100,6 +102,9 @@ def _declare(lib: C.CDLL) -> None:
         "zc_rs_encode_batch_workspace_bytes": (sz, [vp, i32]),
         "zc_rs_encode_batch": (st, [st, vp, i32, u32, vp, sz, vp]),
         "zc_merkle_commit_batch": (st, [vp, vp, i32, vp, sz, vp]),
+        "zc_eval_poly_workspace_bytes": (sz, [i64]),
+        "zc_eval_poly": (st, [st, vp, i64, vp, i32, vp, vp, sz, vp]),
+        "zc_deep_quotient": (st, [st, vp, i64, vp, i32, vp, u32, u32, i32, vp, vp]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(lib, name)

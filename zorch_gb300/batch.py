@@ -66,6 +66,22 @@ class CommittedMatrix:
         return self.layers.root
 
 
+@dataclass
+class CommittedPolys:
+    """The columns of a [w, n] codeword committed as w polynomials, each with
+    its own pair-leaf tree: `roots` [w, 8] (what FriProver.commit returns,
+    stacked) and, when kept, every tree's digest layers `flat` [w, n-1, 8]."""
+
+    codeword: torch.Tensor
+    roots: torch.Tensor
+    flat: torch.Tensor | None = None
+
+    def layers(self, c: int) -> DigestLayers:
+        if self.flat is None:
+            raise ValueError("the digest layers of this commitment were not kept")
+        return DigestLayers(self.flat[c], self.codeword.shape[1] // 2)
+
+
 def _bucket(log_n: int, width: int) -> str:
     return f"{log_n}:{max(width, 1).bit_length() - 1}"
 
@@ -221,6 +237,65 @@ class BatchCommitter:
         cws = self.encode(jobs)
         layers = self.merkle(cws)
         return [CommittedMatrix(c, l) for c, l in zip(cws, layers)]
+
+    # -- per-polynomial pair-leaf trees (FriProver.commit's output) ----------
+    def pair_trees(self, codewords: list[torch.Tensor], flats: list[torch.Tensor] | None = None,
+                   counters: torch.Tensor | None = None) -> list[torch.Tensor]:
+        """Every column of every [w, n] codeword committed as its own pair-leaf
+        tree (leaf p = (cw[c, p], cw[c, p + n/2]), the _commit_one of
+        zorch/pcs/fri/prover.py:141-148), all in one batched commit: one
+        tree-family job per codeword. Returns per codeword its digest layers
+        [w, n-1, 8] (column c's tree at [c], root at [c, n-2])."""
+        if flats is None:
+            flats = [torch.empty((cw.shape[0], cw.shape[1] - 1, 8), dtype=torch.int32,
+                                 device=cw.device) for cw in codewords]
+        arr = (_lib.MerkleJob * len(codewords))()
+        for i, (cw, fl) in enumerate(zip(codewords, flats)):
+            w, n = cw.shape
+            if n < 2 or n & (n - 1):
+                raise ValueError(f"codeword length must be a power of two >= 2, got {n}")
+            top = self._choice(n.bit_length() - 1, w)["top"]
+            half = n // 2
+            arr[i] = _lib.MerkleJob(_lib.Leaves(ptr(cw), half, 2, 1, half), ptr(fl), top, w, n,
+                                    8 * (n - 1))
+        if counters is None:
+            counters = torch.empty(64, dtype=torch.int32, device=codewords[0].device)
+        _lib.check(_lib.lib().zc_merkle_commit_batch(self.perm.handle, arr, len(codewords),
+                                                     ptr(counters), counters.numel() * 4,
+                                                     stream_handle()), "merkle_commit_batch")
+        return flats
+
+    def commit_polys(self, jobs: list[MatrixJob], keep_layers: list[bool] | None = None,
+                     layer_cap: int = 16 << 30) -> list[CommittedPolys]:
+        """FriProver.commit (zorch/pcs/fri/prover.py:92-99) of every column of
+        every job, batched: the LDEs in two persistent launches, every
+        column's pair-leaf tree in one batched tree commit (a tree family per
+        job). Each column's root and digest layers are byte-identical to a
+        per-polynomial commit. A job whose layers are not kept
+        (keep_layers[i] False) and would exceed `layer_cap` bytes has its
+        trees committed in column chunks through one reused buffer, keeping
+        only the roots."""
+        keep = keep_layers if keep_layers is not None else [True] * len(jobs)
+        cws = self.encode(jobs)
+        whole = [i for i, cw in enumerate(cws)
+                 if keep[i] or 32 * cw.shape[0] * cw.shape[1] <= layer_cap]
+        flats = self.pair_trees([cws[i] for i in whole]) if whole else []
+        out: list[CommittedPolys | None] = [None] * len(jobs)
+        for i, fl in zip(whole, flats):
+            out[i] = CommittedPolys(cws[i], fl[:, -1, :].contiguous(), fl if keep[i] else None)
+        for i, cw in enumerate(cws):
+            if out[i] is not None:
+                continue
+            w, n = cw.shape
+            per = max(1, layer_cap // (32 * n))
+            buf = torch.empty((min(per, w), n - 1, 8), dtype=torch.int32, device=cw.device)
+            roots = torch.empty((w, 8), dtype=torch.int32, device=cw.device)
+            for c0 in range(0, w, per):
+                cnt = min(per, w - c0)
+                self.pair_trees([cw[c0:c0 + cnt]], flats=[buf[:cnt]])
+                roots[c0:c0 + cnt].copy_(buf[:cnt, -1, :])
+            out[i] = CommittedPolys(cw, roots, None)
+        return out
 
 
 class GraphedBatch:

@@ -1,6 +1,6 @@
 """Build the CUDA library libzc.so in-tree for sm_103a (GB300).
 
-Four translation units compiled in parallel with nvcc, then linked into
+Five translation units compiled in parallel with nvcc, then linked into
 zorch_gb300/_build/libzc.so. No cmake, no torch extension machinery: the
 library exposes a plain C ABI (include/zc.h) that Python reaches via ctypes.
 """
@@ -18,7 +18,7 @@ ROOT = PKG.parent
 CSRC = PKG / "csrc"
 OUT_DIR = PKG / "_build"
 LIB = OUT_DIR / "libzc.so"
-SOURCES = ["zc_core.cu", "zc_ntt.cu", "zc_merkle.cu", "zc_sumcheck.cu"]
+SOURCES = ["zc_core.cu", "zc_ntt.cu", "zc_merkle.cu", "zc_sumcheck.cu", "zc_deep.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 
@@ -77,6 +77,51 @@ def build(force: bool = False, verbose: bool = False, extra: list[str] | None = 
     os.replace(tmp, LIB)
     stamp.write_text(flags_id)
     return LIB
+
+
+# ------------------------------------------------------------ XLA FFI ----
+XLA_SRC = CSRC / "zc_xla.cc"
+XLA_LIB = OUT_DIR / "libzc_xla.so"
+
+
+def xla_ffi_include_dir() -> Path | None:
+    """The directory holding xla/ffi/api/ffi.h: XLA_FFI_INCLUDE_DIR, else an
+    installed jaxlib's (or jax's) include directory; None when absent."""
+    cands = []
+    if os.environ.get("XLA_FFI_INCLUDE_DIR"):
+        cands.append(Path(os.environ["XLA_FFI_INCLUDE_DIR"]))
+    for mod in ("jaxlib", "jax"):
+        try:
+            m = __import__(mod)
+        except Exception:  # noqa: BLE001 - absent or broken install: not a build error
+            continue
+        cands.append(Path(m.__file__).resolve().parent / "include")
+    for c in cands:
+        if (c / "xla" / "ffi" / "api" / "ffi.h").exists():
+            return c
+    return None
+
+
+def build_xla(force: bool = False) -> Path | None:
+    """libzc_xla.so, the XLA FFI handlers of zc_xla.cc over libzc.so, built
+    only where the XLA FFI headers are found; None (and nothing built)
+    otherwise."""
+    inc = xla_ffi_include_dir()
+    if inc is None:
+        return None
+    lib = build()
+    if XLA_LIB.exists() and not force and XLA_LIB.stat().st_mtime >= max(
+            XLA_SRC.stat().st_mtime, lib.stat().st_mtime):
+        return XLA_LIB
+    cuda = Path(os.environ.get("CUDA_HOME", "/usr/local/cuda"))
+    cmd = ["g++", "-O2", "-std=c++17", "-shared", "-fPIC", "-I", str(inc),
+           "-I", str(ROOT / "include"), "-I", str(cuda / "include"), str(XLA_SRC),
+           "-o", str(XLA_LIB), "-L", str(OUT_DIR), "-lzc", f"-Wl,-rpath,{OUT_DIR}",
+           "-L", str(cuda / "lib64"), "-lcudart"]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError(f"zc_xla.cc failed to build:\n{r.stderr}")
+    return XLA_LIB
 
 
 if __name__ == "__main__":

@@ -84,6 +84,8 @@ class ReedSolomon:
     """Reed-Solomon code; implements the reference's FoldableCode seam
     (zorch/coding/foldable_code.py:27-70) for the binary natural-order fold."""
 
+    bit_reversed = False
+
     def __init__(self, message_len: int, blowup: int, field=BABYBEAR, *,
                  coset_shift: int | None = None, fold_factor: int = 2,
                  generator: int | None = None) -> None:
@@ -292,6 +294,8 @@ class BitReversedReedSolomon:
     sits at (2p, 2p+1), and folding a bit-reversed layer yields the next
     layer, again bit-reversed. The fold math is ReedSolomon's."""
 
+    bit_reversed = True
+
     def __init__(self, message_len: int, blowup: int, field=BABYBEAR, *,
                  coset_shift: int | None = None) -> None:
         self._natural = ReedSolomon(message_len, blowup, field, coset_shift=coset_shift)
@@ -300,6 +304,8 @@ class BitReversedReedSolomon:
         self.block_len = self._natural.block_len
         self.field = self._natural.field
         self.coset_shift = coset_shift
+        self.generator = None
+        self._shift_mont = self._natural._shift_mont
 
     def __eq__(self, other) -> bool:
         return isinstance(other, BitReversedReedSolomon) and self._natural == other._natural

@@ -196,12 +196,30 @@ class MerkleTree:
         q = idx.numel()
         rows = torch.empty((q, width), dtype=torch.int32, device=idx.device)
         paths = torch.empty((layers.depth, q, 8), dtype=torch.int32, device=idx.device)
-        flag = torch.zeros(1, dtype=torch.int32, device=idx.device)
+        check = check and not torch.cuda.is_current_stream_capturing()
+        # the flag is only zeroed (a fill launch) when it is read back
+        flag = torch.zeros(1, dtype=torch.int32, device=idx.device) if check else None
         _lib.check(_lib.lib().zc_merkle_open(lv, ptr(layers.flat), ptr(idx), q, ptr(rows),
                                              ptr(paths), ptr(flag), stream_handle()),
                    "merkle_open")
-        if check and not torch.cuda.is_current_stream_capturing() and int(flag.item()):
+        if check and int(flag.item()):
             raise IndexError(f"leaf index out of range [0, {lv.num_leaves})")
+        return Opening(rows, paths)
+
+    def open_layout_reduced(self, lv: _lib.Leaves, layers: DigestLayers,
+                            indices: torch.Tensor, width: int, shift: int = 0) -> Opening:
+        """Openings at leaf (indices[i] >> shift) mod num_leaves, reduced by the
+        kernel: a fold layer's opening at the layer position of the query
+        positions -- q mod (n >> (i+1)) in natural order (shift 0), q >> (i+1)
+        in bit-reversed order (zorch/coding/reed_solomon.py:320-329, 521-528).
+        No host synchronisation."""
+        idx = indices.to(torch.int32).contiguous()
+        q = idx.numel()
+        rows = torch.empty((q, width), dtype=torch.int32, device=idx.device)
+        paths = torch.empty((layers.depth, q, 8), dtype=torch.int32, device=idx.device)
+        _lib.check(_lib.lib().zc_merkle_open_reduced(lv, ptr(layers.flat), ptr(idx), q, shift,
+                                                     ptr(rows), ptr(paths), stream_handle()),
+                   "merkle_open_reduced")
         return Opening(rows, paths)
 
     def open_rows(self, matrix: torch.Tensor, layers: DigestLayers,

@@ -168,4 +168,22 @@ ZC_HD ef4 ef_mul(const ef4& a, const ef4& b) {
   return r;
 }
 
+// EF4 inverse through the norm. With y = x^2, a = e(y) + x o(y) for
+// e = a0 + a2 y, o = a1 + a3 y, and a(x) a(-x) = e^2 - y o^2 = c0 + c1 y in
+// F[y]/(y^2 - W); (c0 + c1 y)(c0 - c1 y) = c0^2 - W c1^2 = n lies in F. So
+// a^-1 = a(-x) (c0 - c1 x^2) / n, one base-field inversion; zero maps to zero.
+template <class F>
+ZC_HD ef4 ef_inv(const ef4& a) {
+  const uint32_t a0 = a.c[0], a1 = a.c[1], a2 = a.c[2], a3 = a.c[3];
+  const uint32_t a13 = mmul<F>(a1, a3), a02 = mmul<F>(a0, a2);
+  const uint32_t c0 = msub<F>(madd<F>(mmul<F>(a0, a0), mmul<F>(F::W, mmul<F>(a2, a2))),
+                              mmul<F>(F::W, madd<F>(a13, a13)));
+  const uint32_t c1 = msub<F>(madd<F>(a02, a02),
+                              madd<F>(mmul<F>(a1, a1), mmul<F>(F::W, mmul<F>(a3, a3))));
+  const uint32_t n = msub<F>(mmul<F>(c0, c0), mmul<F>(F::W, mmul<F>(c1, c1)));
+  const ef4 conj{{a0, mneg<F>(a1), a2, mneg<F>(a3)}};
+  const ef4 d{{c0, 0u, mneg<F>(c1), 0u}};
+  return ef_scale<F>(ef_mul<F>(conj, d), minv<F>(n));
+}
+
 }  // namespace zc

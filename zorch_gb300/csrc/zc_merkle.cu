@@ -354,10 +354,17 @@ zc_status commit_tree(const Leaf& leaf, uint32_t* layers, int64_t L, const P2Par
   return finish_tree<K>(layers, L, ilog2(T0), rt, st);
 }
 
+// Rows and sibling paths of q leaves. reduce != 0: leaf = (idx >> shift) mod
+// num_leaves (a power of two) -- the layer positions of
+// zorch/coding/reed_solomon.py:320-329 (natural order, shift 0: a_i = q mod
+// (n >> (i+1))) and :521-528 (bit-reversed order, shift i+1: a_i = q >> (i+1))
+// computed here rather than by the caller.
 __global__ void k_open(zc_leaves lv, const uint32_t* layers, const int32_t* idx, int q, int depth,
-                       uint32_t* rows, uint32_t* paths, uint32_t* oob) {
+                       uint32_t* rows, uint32_t* paths, uint32_t* oob, int reduce, int shift) {
   const int qi = blockIdx.x;
   int64_t i = idx[qi];
+  if (reduce)
+    i = (int64_t)(((uint64_t)(uint32_t)idx[qi] >> shift) & (uint64_t)(lv.num_leaves - 1));
   if (i < 0 || i >= lv.num_leaves) {
     if (threadIdx.x == 0 && oob) atomicOr(oob, 1u);
     i = i < 0 ? 0 : lv.num_leaves - 1;
@@ -531,20 +538,27 @@ __global__ void __launch_bounds__(32) k_bind_root(const P2Params* rt, const uint
 constexpr int kMaxTreeJobs = 48;
 constexpr int kTopLog = 8;
 
+// One job is `count` trees of the same shape: tree t reads its leaves at
+// base + t * bstride and writes its layers at layers + t * lstride (the columns
+// of one request, each committed as its own polynomial).
 struct TreeJobDev {
   const uint32_t* base;
   uint32_t* layers;
   int64_t L;
   int64_t gs;
+  int64_t bstride, lstride;
+  int64_t chunks;  // 256-node chunks per tree at the level being produced
   int32_t G, g;
   int32_t depth, top;
+  int32_t count;
 };
 
 struct TreeBatch {
   int32_t njobs;
   int32_t level;  // level phase: the level being produced
   int64_t total;
-  int64_t prefix[kMaxTreeJobs + 1];
+  int64_t prefix[kMaxTreeJobs + 1];       // work items before job j
+  int64_t tree_prefix[kMaxTreeJobs + 1];  // trees before job j (top launch)
   TreeJobDev job[kMaxTreeJobs];
 };
 
@@ -574,20 +588,23 @@ __global__ void __launch_bounds__(kMaxT) k_tree_batch(const __grid_constant__ Tr
     if (it >= B.total) break;
     const int j = find_tree(B.prefix, B.njobs, it);
     const TreeJobDev& J = B.job[j];
-    const int64_t p = (it - B.prefix[j]) * kMaxT + threadIdx.x;
+    const int64_t local = it - B.prefix[j];
+    const int64_t tree = local / J.chunks;
+    const int64_t p = (local - tree * J.chunks) * kMaxT + threadIdx.x;
+    uint32_t* lay = J.layers + tree * J.lstride;
     uint32_t d[8];
     if (LEVEL == 0) {
       if (p < J.L) {
-        LayoutLeaf leaf{J.base, J.G, J.g, J.gs};
+        LayoutLeaf leaf{J.base + tree * J.bstride, J.G, J.g, J.gs};
         leaf.digest(p, d, k);
-        store_digest(J.layers + 8 * p, d);
+        store_digest(lay + 8 * p, d);
       }
     } else {
       const int l = B.level;
       if (p < (J.L >> l)) {
-        NodeLeaf nl{J.layers + 8 * level_offset(J.L, l - 1)};
+        NodeLeaf nl{lay + 8 * level_offset(J.L, l - 1)};
         nl.digest(p, d, k);
-        store_digest(J.layers + 8 * (level_offset(J.L, l) + p), d);
+        store_digest(lay + 8 * (level_offset(J.L, l) + p), d);
       }
     }
   }
@@ -605,17 +622,19 @@ __global__ void __launch_bounds__(8 * kSubT) k_tree_top(const __grid_constant__ 
   __shared__ uint32_t sm[2][8 * S];
   KIn<K>::make(rt, &s_rt);
   const P2Params* hp = KIn<K>::half(rt, &s_rt);
-  const TreeJobDev& J = B.job[blockIdx.x];
+  const int j = find_tree(B.tree_prefix, B.njobs, (int64_t)blockIdx.x);
+  const TreeJobDev& J = B.job[j];
+  uint32_t* lay = J.layers + ((int64_t)blockIdx.x - B.tree_prefix[j]) * J.lstride;
   int lvl = J.top;
   int width = (int)(J.L >> lvl);
-  const uint32_t* src = J.layers + 8 * level_offset(J.L, lvl);
+  const uint32_t* src = lay + 8 * level_offset(J.L, lvl);
   for (int i = threadIdx.x; i < width * 8; i += blockDim.x) sm[0][(i & 7) * S + (i >> 3)] = src[i];
   int cur = 0;
   while (width > 1) {
     __syncthreads();
     width >>= 1;
     lvl++;
-    subtree_level<F>(sm[cur], sm[cur ^ 1], S, J.layers + 8 * level_offset(J.L, lvl), width, hp);
+    subtree_level<F>(sm[cur], sm[cur ^ 1], S, lay + 8 * level_offset(J.L, lvl), width, hp);
     cur ^= 1;
   }
 }
@@ -627,6 +646,7 @@ zc_status tree_batch_wave(const zc_merkle_job* jobs, int n, unsigned long long* 
   memset(&B, 0, sizeof(B));
   B.njobs = n;
   int max_top = 0;
+  int64_t trees = 0;
   for (int i = 0; i < n; i++) {
     TreeJobDev& d = B.job[i];
     d.base = jobs[i].leaves.base;
@@ -635,11 +655,17 @@ zc_status tree_batch_wave(const zc_merkle_job* jobs, int n, unsigned long long* 
     d.gs = jobs[i].leaves.group_stride;
     d.G = jobs[i].leaves.groups;
     d.g = jobs[i].leaves.group_len;
+    d.count = jobs[i].count > 1 ? jobs[i].count : 1;
+    d.bstride = jobs[i].leaf_stride;
+    d.lstride = jobs[i].layer_stride;
     d.depth = ilog2(d.L);
     const int tl = jobs[i].top_log ? jobs[i].top_log : kTopLog;
     d.top = d.depth > tl ? d.depth - tl : 0;
     max_top = d.top > max_top ? d.top : max_top;
+    B.tree_prefix[i] = trees;
+    trees += d.count;
   }
+  B.tree_prefix[n] = trees;
   int dev = 0, sms = 0;
   ZC_CUDA(cudaGetDevice(&dev));
   ZC_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
@@ -650,8 +676,10 @@ zc_status tree_batch_wave(const zc_merkle_job* jobs, int n, unsigned long long* 
   for (int l = 0; l <= max_top; l++) {
     int64_t tot = 0;
     for (int i = 0; i < n; i++) {
+      TreeJobDev& d = B.job[i];
       B.prefix[i] = tot;
-      if (l == 0 || l <= B.job[i].top) tot += ((B.job[i].L >> l) + kMaxT - 1) / kMaxT;
+      d.chunks = ((d.L >> l) + kMaxT - 1) / kMaxT;
+      if (l == 0 || l <= d.top) tot += d.chunks * d.count;
     }
     B.prefix[n] = tot;
     B.total = tot;
@@ -665,7 +693,8 @@ zc_status tree_batch_wave(const zc_merkle_job* jobs, int n, unsigned long long* 
       k_tree_batch<K, 1><<<(unsigned)grid, kMaxT, 0, st>>>(B, ctr + l, rt);
     ZC_TRY(launch_check());
   }
-  k_tree_top<K><<<n, 8 * kSubT, 0, st>>>(B, rt);
+  if (trees > 0x7fffffff) return ZC_BAD_SHAPE;
+  k_tree_top<K><<<(unsigned)trees, 8 * kSubT, 0, st>>>(B, rt);
   return launch_check();
 }
 
@@ -807,7 +836,21 @@ zc_status zc_merkle_open(zc_leaves lv, const uint32_t* layers, const int32_t* id
   if (!is_pow2(lv.num_leaves)) return ZC_NOT_POW2;
   if (q == 0) return ZC_OK;
   const int depth = ilog2(lv.num_leaves);
-  k_open<<<q, 128, 0, (cudaStream_t)stream>>>(lv, layers, idx, q, depth, rows, paths, oob_flag);
+  k_open<<<q, 128, 0, (cudaStream_t)stream>>>(lv, layers, idx, q, depth, rows, paths, oob_flag,
+                                              0, 0);
+  return launch_check();
+}
+
+zc_status zc_merkle_open_reduced(zc_leaves lv, const uint32_t* layers, const int32_t* idx,
+                                 int32_t q, int32_t shift, uint32_t* rows, uint32_t* paths,
+                                 void* stream) {
+  if (q < 0 || !layers || !idx || (q > 0 && (!rows || !paths))) return ZC_BAD_ARG;
+  if (shift < 0 || shift > 31) return ZC_BAD_ARG;
+  if (!is_pow2(lv.num_leaves) || lv.num_leaves > (1ll << 32)) return ZC_NOT_POW2;
+  if (q == 0) return ZC_OK;
+  const int depth = ilog2(lv.num_leaves);
+  k_open<<<q, 128, 0, (cudaStream_t)stream>>>(lv, layers, idx, q, depth, rows, paths, nullptr,
+                                              1, shift);
   return launch_check();
 }
 
@@ -911,6 +954,13 @@ zc_status zc_merkle_commit_batch(const zc_poseidon2* p, const zc_merkle_job* job
       return ZC_BAD_ARG;
     if (j.top_log < 0 || j.top_log > kTopLog) {
       set_error("top_log must be 0 (default) or 1..8");
+      return ZC_BAD_ARG;
+    }
+    if (j.count < 0) return ZC_BAD_ARG;
+    if (j.count > 1 && (j.layer_stride < 8 * (2 * j.leaves.num_leaves - 1) ||
+                        j.layer_stride % 4 || j.leaf_stride < 0)) {
+      set_error("a tree family needs layer_stride >= (2L-1)*8 words (a multiple of 4) "
+                "and leaf_stride >= 0");
       return ZC_BAD_ARG;
     }
     if (ilog2(j.leaves.num_leaves) - (j.top_log ? j.top_log : kTopLog) + 1 > 30)

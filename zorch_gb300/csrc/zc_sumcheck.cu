@@ -292,24 +292,6 @@ __global__ void k_rlc_values(const uint32_t* values, int w, const uint32_t* chal
 
 constexpr int kReduceBlocks = 256;
 
-// EF4 inverse through the norm. With y = x^2, a = e(y) + x o(y) for
-// e = a0 + a2 y, o = a1 + a3 y, and a(x) a(-x) = e^2 - y o^2 = c0 + c1 y in
-// F[y]/(y^2 - W); (c0 + c1 y)(c0 - c1 y) = c0^2 - W c1^2 = n lies in F. So
-// a^-1 = a(-x) (c0 - c1 x^2) / n, one base-field inversion; zero maps to zero.
-template <class F>
-__device__ ef4 ef_inv(const ef4& a) {
-  const uint32_t a0 = a.c[0], a1 = a.c[1], a2 = a.c[2], a3 = a.c[3];
-  const uint32_t a13 = mmul<F>(a1, a3), a02 = mmul<F>(a0, a2);
-  const uint32_t c0 = msub<F>(madd<F>(mmul<F>(a0, a0), mmul<F>(F::W, mmul<F>(a2, a2))),
-                              mmul<F>(F::W, madd<F>(a13, a13)));
-  const uint32_t c1 = msub<F>(madd<F>(a02, a02),
-                              madd<F>(mmul<F>(a1, a1), mmul<F>(F::W, mmul<F>(a3, a3))));
-  const uint32_t n = msub<F>(mmul<F>(c0, c0), mmul<F>(F::W, mmul<F>(c1, c1)));
-  const ef4 conj{{a0, mneg<F>(a1), a2, mneg<F>(a3)}};
-  const ef4 d{{c0, 0u, mneg<F>(c1), 0u}};
-  return ef_scale<F>(ef_mul<F>(conj, d), minv<F>(n));
-}
-
 template <class F>
 __global__ void k_ef4_inv(const uint32_t* in, uint32_t* out, int64_t count) {
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < count;

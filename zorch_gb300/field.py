@@ -144,6 +144,30 @@ def to_host(t: torch.Tensor) -> np.ndarray:
     return t.detach().contiguous().cpu().numpy().view(np.uint32)
 
 
+def parts_to_pinned(parts: list[torch.Tensor]) -> torch.Tensor:
+    """Concatenate device tensors into one page-locked host buffer with one
+    asynchronous device->host copy per part on the current stream (copy
+    engine only, no gather kernel). The result is valid once the stream has
+    reached the copies (synchronise or record an event)."""
+    flat = [p.reshape(-1) for p in parts]
+    total = sum(p.numel() for p in flat)
+    host = torch.empty(total, dtype=torch.int32, pin_memory=True)
+    off = 0
+    for p in flat:
+        if p.numel():
+            host[off: off + p.numel()].copy_(p, non_blocking=True)
+        off += p.numel()
+    return host
+
+
+def parts_to_bytes(parts: list[torch.Tensor]) -> bytes:
+    """Mont-u32 little-endian bytes of the parts in order (one device->host
+    copy per part, then one stream synchronisation)."""
+    host = parts_to_pinned(parts)
+    torch.cuda.current_stream().synchronize()
+    return host.numpy().view(np.uint32).astype("<u4").tobytes()
+
+
 def to_mont(field, t: torch.Tensor, out: torch.Tensor | None = None) -> torch.Tensor:
     """Canonical -> Montgomery on the device (zc_to_mont)."""
     f = field_of(field)

@@ -20,7 +20,9 @@ import torch
 from . import _lib
 from .coding import ReedSolomon
 from .commit import DigestLayers, MerkleTree, Opening, leaves_layout
-from .field import ptr, stream_handle, to_host
+from .field import parts_to_bytes, ptr, stream_handle, to_host
+from .stage import (OpeningClaim, OpeningProof, OpeningWitness, ProveResult, TrivialClaim,
+                    VerifyResult)
 from .transcript import DuplexTranscript
 
 
@@ -35,9 +37,14 @@ def to_base_field(leaves: torch.Tensor) -> torch.Tensor:
     return leaves
 
 
-def pair_layout(layer: torch.Tensor) -> _lib.Leaves:
+def pair_layout(layer: torch.Tensor, bit_reversed: bool = False) -> _lib.Leaves:
+    """A layer's pair leaves in place: (cw[p], cw[p + n/2]) in natural order,
+    the adjacent (cw[2p], cw[2p+1]) in bit-reversed order
+    (zorch/coding/reed_solomon.py:303-307, 512-515)."""
     n = layer.shape[0]
     limbs = limbs_of(layer)
+    if bit_reversed:
+        return leaves_layout(layer, n // 2, 1, 2 * limbs, 0)
     return leaves_layout(layer, n // 2, 2, limbs, (n // 2) * limbs)
 
 
@@ -66,6 +73,7 @@ class FoldState:
     codeword: torch.Tensor
     layers: tuple = ()
     pending: CommittedLayer | None = None
+    betas: tuple = ()  # the challenge sampled in each round so far
 
 
 @dataclass
@@ -83,8 +91,7 @@ class PreFoldPairCommitRound:
     last_round: int | None = None  # index of the final round (no commit after it)
 
     def commit_layer(self, cw: torch.Tensor) -> CommittedLayer:
-        n = cw.shape[0]
-        _, layers = self.tree.commit_layout(pair_layout(cw), cw.device)
+        _, layers = self.tree.commit_layout(pair_layout(cw, self.code.bit_reversed), cw.device)
         return CommittedLayer(cw, layers)
 
     def __call__(self, state: FoldState, t: DuplexTranscript):
@@ -99,7 +106,8 @@ class PreFoldPairCommitRound:
             out, pending = self.fold_commit(cw, beta, level)
         else:
             out, pending = self.code.fold(cw, beta), None
-        return FoldState(out, state.layers + (layer,), pending), t, layer.root
+        return FoldState(out, state.layers + (layer,), pending, state.betas + (beta,)), t, \
+            layer.root
 
     def fold_commit(self, cw: torch.Tensor, beta: torch.Tensor, level: int):
         n = cw.shape[0]
@@ -110,7 +118,9 @@ class PreFoldPairCommitRound:
                           device=cw.device)
         L = n // 4
         flat = torch.empty((2 * L - 1, 8), dtype=torch.int32, device=cw.device)
-        _lib.check(_lib.lib().zc_fri_fold_commit(
+        fn = (_lib.lib().zc_fri_fold_commit_bitrev if self.code.bit_reversed
+              else _lib.lib().zc_fri_fold_commit)
+        _lib.check(fn(
             self.tree.perm.handle, ptr(cw), n, int(ef_in), ptr(beta), int(ef_beta),
             self.code.level_shift_mont(level), self.code.generator or 0, ptr(out), ptr(flat),
             stream_handle()), "fri_fold_commit")
@@ -193,11 +203,16 @@ def fold_rounds(rnd, state, transcript, rounds: int):
     return state, transcript, msgs
 
 
-def open_layer(tree: MerkleTree, layer: CommittedLayer, indices: torch.Tensor) -> Opening:
-    """open_rows over a layer's pair leaves (zorch/pcs/fold.py:142-149); the
-    indices are reduced mod the layer's leaf count, so no range check."""
-    return tree.open_layout(pair_layout(layer.codeword), layer.digest_layers, indices,
-                            2 * layer.limbs, check=False)
+def open_layer(tree: MerkleTree, layer: CommittedLayer, positions: torch.Tensor,
+               level: int = 0, bit_reversed: bool = False) -> Opening:
+    """open_rows over layer `level`'s pair leaves (zorch/pcs/fold.py:142-149)
+    at its layer positions -- positions mod the layer's leaf count in natural
+    order, positions >> (level + 1) in bit-reversed order
+    (code.layer_positions, zorch/coding/reed_solomon.py:320-329, 521-528) --
+    reduced by the opening kernel: no range check, no reduction launch."""
+    return tree.open_layout_reduced(pair_layout(layer.codeword, bit_reversed),
+                                    layer.digest_layers, positions, 2 * layer.limbs,
+                                    level + 1 if bit_reversed else 0)
 
 
 @dataclass
@@ -217,7 +232,7 @@ class CommitPhaseProof:
         parts = [self.roots.reshape(-1), self.final_layer.reshape(-1)]
         for op in self.openings:
             parts += [op.row.reshape(-1), op.path.reshape(-1)]
-        return to_host(torch.cat(parts)).astype("<u4").tobytes()
+        return parts_to_bytes(parts)
 
 
 @dataclass(frozen=True)
@@ -260,7 +275,7 @@ class FriProver:
         pair-leaf Merkle commit of the codeword."""
         code, tree = self.params.code, self.params.tree
         cw = code.encode(coeffs, out)
-        _, layers = tree.commit_layout(pair_layout(cw), cw.device)
+        _, layers = tree.commit_layout(pair_layout(cw, code.bit_reversed), cw.device)
         return FriCommittedPoly(coeffs, cw, layers)
 
     def commit(self, polys: Sequence[torch.Tensor]):
@@ -278,7 +293,6 @@ class FriProver:
                                      last_round=p.num_rounds - 1)
         state = FoldState(codeword, (), first_layer)
         t = transcript._copy()
-        betas = []
         roots = []
         for _ in range(p.num_rounds):
             state, t, root = rnd(state, t)
@@ -286,14 +300,279 @@ class FriProver:
         final = state.codeword
         n0 = codeword.shape[0]
         positions = t.sample_positions_(n0, p.num_queries, values=final)
-        openings = []
-        q = positions
-        for i, layer in enumerate(state.layers):
-            q = torch.remainder(q, n0 >> (i + 1))
-            openings.append(open_layer(p.tree, layer, q))
+        br = p.code.bit_reversed
+        openings = [open_layer(p.tree, layer, positions, i, br)
+                    for i, layer in enumerate(state.layers)]
         roots_t = torch.stack(roots) if roots else torch.empty((0, 8), dtype=torch.int32,
                                                                device=codeword.device)
-        return CommitPhaseProof(roots_t, betas, final, positions, openings), t, state
+        return CommitPhaseProof(roots_t, list(state.betas), final, positions, openings), t, state
+
+
+    # -- the open: ProverStage.prove (zorch/pcs/fri/prover.py:101-187) --------
+    def prove(self, claim: OpeningClaim, witness: OpeningWitness,
+              transcript: DuplexTranscript) -> ProveResult:
+        """Open the committed polynomials at the claim's points. Terminal: the
+        claim reduces to TrivialClaim(); the reduction proof is
+        OpeningProof(values, [FriProof per polynomial])."""
+        values, proofs, t = self._open(witness.prover_data, claim.points, transcript)
+        return ProveResult(TrivialClaim(), OpeningProof(values, proofs), t)
+
+    def _open(self, prover_data: FriProverData, points: Sequence, transcript: DuplexTranscript):
+        """One _open_one per polynomial, threading one transcript through them
+        in order (zorch/pcs/fri/prover.py:114-133). Returns (values [k] base /
+        [k, 4] EF4, proofs, transcript)."""
+        if len(prover_data.polys) != len(points):
+            raise ValueError(f"batch mismatch: {len(prover_data.polys)} polys vs "
+                             f"{len(points)} points")
+        t = transcript._copy()
+        values, proofs = [], []
+        for committed, z in zip(prover_data.polys, points):
+            proof, t = self._open_one(committed, fri_point(self.params.code.field, z), t)
+            values.append(proof.value)
+            proofs.append(proof)
+        if not values:
+            return torch.empty(0, dtype=torch.int32), proofs, t
+        return torch.stack(values), proofs, t
+
+    def _open_one(self, committed: FriCommittedPoly, z: torch.Tensor, t: DuplexTranscript):
+        """_open_one (zorch/pcs/fri/prover.py:151-187) on the device with no
+        host synchronisation: v = f(z) (zc_eval_poly), the layer-0 DEEP
+        quotient (cw - v) / (domain - z) (zc_deep_quotient), observe f's root,
+        the pre-fold pair commit rounds, the final layer and the query
+        positions (commit_phase), and f's pair leaf at each layer-0 position."""
+        code, tree = self.params.code, self.params.tree
+        f = code.field
+        dev = committed.codeword.device
+        zl = z.numel()
+        L = _lib.lib()
+        st = stream_handle()
+        coeffs = committed.coeffs.contiguous()
+        k = coeffs.numel()
+        v = torch.empty(zl, dtype=torch.int32, device=dev)
+        nb = L.zc_eval_poly_workspace_bytes(k)
+        ws = torch.empty((nb + 15) // 4, dtype=torch.int32, device=dev)
+        _lib.check(L.zc_eval_poly(f.id, ptr(coeffs), k, ptr(z), zl, ptr(v), ptr(ws), nb, st),
+                   "eval_poly")
+        n = committed.codeword.shape[0]
+        q = torch.empty((n,) if zl == 1 else (n, 4), dtype=torch.int32, device=dev)
+        _lib.check(L.zc_deep_quotient(f.id, ptr(committed.codeword), n, ptr(z), zl, ptr(v),
+                                      code._shift_mont, code.generator or 0,
+                                      int(code.bit_reversed), ptr(q), st), "deep_quotient")
+        t = t._copy()
+        t.observe_(committed.root)
+        phase, t, _ = self.commit_phase(q, t)
+        br = code.bit_reversed
+        f_open = tree.open_layout_reduced(pair_layout(committed.codeword, br),
+                                          committed.digest_layers, phase.positions, 2,
+                                          1 if br else 0)
+        proof = FriProof(v.reshape(()) if zl == 1 else v, phase.roots, phase.final_layer,
+                         f_open, phase.openings, phase.positions)
+        return proof, t
+
+
+def point_words(field, z) -> np.ndarray:
+    """An opening point as host Montgomery words (see fri_point)."""
+    if torch.is_tensor(z) or isinstance(z, np.ndarray):
+        w = _host(z).reshape(-1)
+    else:
+        w = np.asarray([field.mont(int(x)) for x in (z if isinstance(z, (tuple, list)) else [z])],
+                       np.uint32)
+    if w.size not in (1, 4):
+        raise ValueError(f"an opening point has 1 (base) or 4 (EF4) limbs, got {w.size}")
+    return w
+
+
+def fri_point(field, z) -> torch.Tensor:
+    """An opening point as device Montgomery words: a tensor (1 word: base, 4:
+    EF4) passes through; a Python int is a canonical base element; a 4-tuple
+    of ints a canonical EF4 element."""
+    if torch.is_tensor(z):
+        if z.numel() not in (1, 4):
+            raise ValueError(f"an opening point has 1 (base) or 4 (EF4) limbs, got {z.numel()}")
+        return z.reshape(-1).to(torch.int32).contiguous()
+    words = [field.mont(int(x)) for x in (z if isinstance(z, (tuple, list)) else [z])]
+    if len(words) not in (1, 4):
+        raise ValueError(f"an opening point has 1 (base) or 4 (EF4) limbs, got {len(words)}")
+    return torch.tensor(np.asarray(words, np.uint32).view(np.int32), device="cuda")
+
+
+@dataclass
+class FriProof:
+    """zorch/pcs/fri/config.py:56-69: value = f(z); fri_roots = the quotient's
+    pre-fold layer roots [R, 8]; final_layer; f_opening = f's pair leaf at each
+    query's layer-0 position (rebuilds the quotient at layer 0);
+    query_openings = each fold layer's pair leaf. `positions` (the sampled
+    query positions) is derived by both sides and is not on the wire."""
+
+    value: torch.Tensor
+    fri_roots: torch.Tensor
+    final_layer: torch.Tensor
+    f_opening: Opening
+    query_openings: list[Opening]
+    positions: torch.Tensor | None = None
+
+    def parts(self) -> list[torch.Tensor]:
+        """The wire tensors in pytree flatten order: value, fri_roots,
+        final_layer, f_opening (row, path), query_openings (row, path each)."""
+        out = [self.value.reshape(-1), self.fri_roots, self.final_layer, self.f_opening.row,
+               self.f_opening.path]
+        for op in self.query_openings:
+            out += [op.row, op.path]
+        return out
+
+    def to_bytes(self) -> bytes:
+        """Mont-u32 little endian in pytree flatten order."""
+        return parts_to_bytes(self.parts())
+
+
+def _host(x) -> np.ndarray:
+    return to_host(x) if torch.is_tensor(x) else np.asarray(x, np.uint32)
+
+
+class FriVerifier:
+    """FRI verifier on the host (zorch/pcs/fri/verifier.py:31-140): replays the
+    transcript, checks the final layer is constant, every opened leaf against
+    its root, the layer-0 quotient pair rebuilt from f's opened leaf, and the
+    fold chain down to the final layer. A bad proof is a False verdict;
+    structural mismatches raise ValueError, as the reference does."""
+
+    def __init__(self, params: FriParams) -> None:
+        self.params = params
+
+    def verify(self, claim: OpeningClaim, reduction_proof: OpeningProof, transcript):
+        ok, t = self._verify_opening(claim.commitment, claim.points, reduction_proof.values,
+                                     reduction_proof.proof, transcript)
+        return VerifyResult(TrivialClaim(), t, ok)
+
+    def _verify_opening(self, commitment, points, values, proof, transcript):
+        from .transcript import HostDuplexTranscript
+
+        roots = _host(commitment).reshape(-1, 8)
+        vals = _host(values)
+        k = roots.shape[0]
+        nvals = vals.shape[0] if vals.ndim else 1
+        if not (len(points) == nvals == len(proof) == k):
+            raise ValueError(f"batch mismatch: commitment={k}, points={len(points)}, "
+                             f"values={nvals}, proof={len(proof)}")
+        rounds = self.params.num_rounds
+        for pf in proof:
+            if pf.fri_roots.shape[0] != rounds or len(pf.query_openings) != rounds:
+                raise ValueError(f"malformed proof: expected {rounds} fold layers, got "
+                                 f"{pf.fri_roots.shape[0]} roots / {len(pf.query_openings)} "
+                                 "openings")
+        t = host_transcript(self.params.tree.perm, transcript)
+        oks = []
+        vals = vals.reshape(k, -1)
+        for f_root, z, v, pf in zip(roots, points, vals, proof):
+            t, ok = self._verify_one(f_root, z, v, pf, t)
+            oks.append(ok)
+        return all(oks), t
+
+    def _verify_one(self, f_root, z, v, pf: FriProof, t):
+        p = self.params
+        code, tree = p.code, p.tree
+        f = code.field
+        n = code.block_len
+        zw = point_words(f, z)
+        zl = zw.size
+        vw = np.asarray(v, np.uint32).reshape(-1)
+        if vw.size != zl:
+            return t, False
+        pad = lambda w: tuple(f.ef_from_mont(list(w) + [0] * (4 - len(w))))  # noqa: E731
+        zc, vc = pad(zw), pad(vw)
+        t = t.observe(f_root)
+        betas = []
+        for r in _host(pf.fri_roots).reshape(-1, 8):
+            t, b = t.observe_and_sample(r, p.challenge_limbs)
+            betas.append(pad(b))
+        final = _host(pf.final_layer)
+        t = t.observe(final.reshape(-1))
+        fin = final.reshape(final.shape[0], -1)
+        ok = bool((fin == fin[0]).all())
+        t, raw = t.sample(p.num_queries)
+        positions = [int(x) % n for x in raw]
+        br = code.bit_reversed
+
+        def leaf_index(q: int, level: int) -> int:
+            return q >> (level + 1) if br else q % (n >> (level + 1))
+
+        # Merkle: f's pair leaf at a_0, every fold layer's pair leaf at a_i
+        f_rows = _host(pf.f_opening.row)
+        for qi, q in enumerate(positions):
+            ok &= tree.verify(torch.as_tensor(np.asarray(f_root, np.uint32).view(np.int32)),
+                              leaf_index(q, 0),
+                              Opening(pf.f_opening.row[qi], pf.f_opening.path[:, qi]))
+            for i, op in enumerate(pf.query_openings):
+                ok &= tree.verify(torch.as_tensor(_host(pf.fri_roots)[i].view(np.int32)),
+                                  leaf_index(q, i), Opening(op.row[qi], op.path[:, qi]))
+        if not ok:
+            return t, False
+        shift = code.coset_shift
+        gen = code.generator or None
+
+        def point(level: int, j: int) -> int:
+            """Layer `level`'s domain point at natural index j."""
+            nl = n >> level
+            sh = pow(shift, 1 << level, f.p) if shift is not None else 1
+            return sh * pow(f.root_of_unity(nl.bit_length() - 1, gen), j, f.p) % f.p
+
+        def pair_points(level: int, a: int) -> tuple:
+            """(lo, hi) codeword indices of the pair at leaf a and the lo
+            point's natural index (hi's point is its negation)."""
+            nl = n >> level
+            if br:
+                bits = nl.bit_length() - 1
+                j = int(format(2 * a, f"0{bits}b")[::-1], 2) if bits else 0
+                return 2 * a, 2 * a + 1, j
+            return a, a + nl // 2, a
+
+        layer0 = [_host(op.row) for op in pf.query_openings]
+        inv2 = pow(2, f.p - 2, f.p)
+        for qi, q in enumerate(positions):
+            a0 = leaf_index(q, 0)
+            _, _, j0 = pair_points(0, a0)
+            x_lo = point(0, j0)
+            x_hi = (f.p - x_lo) % f.p
+            f_lo, f_hi = f.canon(int(f_rows[qi, 0])), f.canon(int(f_rows[qi, 1]))
+            # the quotient pair rebuilt from f's opened leaf == the committed layer-0 leaf
+            for fx, x, slot in ((f_lo, x_lo, 0), (f_hi, x_hi, 1)):
+                num = f.ef_sub((fx, 0, 0, 0), vc)
+                den = f.ef_sub((x, 0, 0, 0), zc)
+                g = (0, 0, 0, 0) if den == (0, 0, 0, 0) else f.ef_mul(num, f.ef_inv(den))
+                lw = layer0[0][qi].reshape(2, -1)[slot] if p.num_rounds else None
+                if lw is not None:
+                    ok &= g == pad(lw)
+            # fold chain
+            for i in range(p.num_rounds):
+                a = leaf_index(q, i)
+                leaf = layer0[i][qi].reshape(2, -1)
+                lo, hi = pad(leaf[0]), pad(leaf[1])
+                _, _, j = pair_points(i, a)
+                x = point(i, j)
+                inv2x = pow(2 * x % f.p, f.p - 2, f.p)
+                folded = f.ef_add(f.ef_scale(f.ef_add(lo, hi), inv2),
+                                  f.ef_mul(f.ef_scale(f.ef_sub(lo, hi), inv2x), betas[i]))
+                if i + 1 < p.num_rounds:
+                    a_next = leaf_index(q, i + 1)
+                    lo_n, _, _ = pair_points(i + 1, a_next)
+                    nxt = layer0[i + 1][qi].reshape(2, -1)
+                    expected = pad(nxt[0] if a == lo_n else nxt[1])
+                else:
+                    expected = pad(fin[a])
+                ok &= folded == expected
+        return t, bool(ok)
+
+
+def host_transcript(perm, transcript=None):
+    """The verifier's host transcript: fresh (None), a HostDuplexTranscript
+    as is, or a device DuplexTranscript's state read back."""
+    from .transcript import HostDuplexTranscript
+
+    if transcript is None:
+        return HostDuplexTranscript(perm)
+    if isinstance(transcript, HostDuplexTranscript):
+        return transcript
+    return HostDuplexTranscript(perm, to_host(transcript.state).copy())
 
 
 @dataclass
@@ -329,7 +608,7 @@ class BasefoldProof:
                  self.final_poly.reshape(-1)]
         for op in list(self.component_openings) + list(self.query_openings):
             parts += [op.row.reshape(-1), op.path.reshape(-1)]
-        return to_host(torch.cat(parts)).astype("<u4").tobytes()
+        return parts_to_bytes(parts)
 
 
 def _ceil_log2(x: int) -> int:
@@ -449,11 +728,7 @@ class BasefoldProver:
         final = cw
         positions = t.sample_positions_(n, self.num_queries, values=final)
         comp = [self.open_rows(pd, positions, check=False) for pd in rounds]
-        queries = []
-        q = positions
-        for i, layer in enumerate(layers):
-            q = torch.remainder(q, n >> (i + 1))
-            queries.append(open_layer(tree, layer, q))
+        queries = [open_layer(tree, layer, positions) for layer in layers]
         proof = BasefoldProof(msgs, torch.stack([ly.root for ly in layers]), final, comp,
                               queries, positions)
         return values, proof, t

@@ -1,22 +1,31 @@
-"""Continuous-batching commit server and the plain per-polynomial path beside it.
+"""Continuous-batching commit server and the plain per-call path beside it.
 
 Requests (a BabyBear matrix of 2^log_h rows x width columns, a blowup, and
 for some a fold-and-open) arrive over time. `Server.run` admits arrived
-requests by their HBM footprint against a budget, batches every admitted
-request into one batched LDE + batched Merkle commit (zorch_gb300.batch) on
-one of several CUDA streams, so batches formed while others are still on the
-GPU overlap on the device; fold requests then run their fold-and-commit
-rounds and query openings on the same stream. A request's codeword and
-digest layers stay resident until its openings are taken. Latency =
-completion time - arrival time.
+requests by their HBM footprint against a budget and commits every admitted
+request in one batched commit (zorch_gb300.batch) on one of several CUDA
+streams, so batches formed while others are still on the GPU overlap on the
+device; fold requests then run their fold-and-commit rounds and query
+openings on the same stream. A request's codeword and digest layers stay
+resident until its openings are taken. Latency = completion - arrival.
 
-`run_plain` serves the same stream one request at a time through the
-drop-in API with one call per polynomial (FriProver.commit, zorch/pcs/fri/
-prover.py:92-99: encode one column, commit its pair-leaf tree) and a host
-synchronisation per call, as the reference's eager loop does.
+Two commitment modes, each with its plain counterpart producing the same
+bytes:
 
-A request's result bytes do not depend on what it was batched with; the
-tests check each one alone and in the mix.
+- "fri": every column is its own polynomial with its own pair-leaf tree, the
+  commitment is the stacked roots -- FriProver.commit
+  (zorch/pcs/fri/prover.py:92-99, 141-148). The server commits all columns of
+  all admitted requests in one batched LDE and one batched tree commit (a
+  tree family per request); `run_plain` makes one call per polynomial
+  (FriProver.commit_one).
+- "matrix": one row-leaf tree per request, the commitment is its root --
+  BasefoldProver.commit (zorch/pcs/basefold/prover.py:437-455). The server
+  batches the requests' matrices; `run_plain` makes one commit call per
+  request.
+
+A request's result bytes do not depend on what it was batched with or on
+which path made them: the tests compare every request served, alone and in
+the mix, with the plain path's bytes and with the oracle.
 """
 
 from __future__ import annotations
@@ -24,6 +33,7 @@ from __future__ import annotations
 import time
 from collections import deque
 from dataclasses import dataclass, field as dc_field
+from typing import Callable
 
 import numpy as np
 import torch
@@ -31,10 +41,15 @@ import torch
 from . import _lib
 from .batch import BatchCommitter, MatrixJob
 from .coding import ReedSolomon
-from .commit import MerkleTree, Poseidon2, leaves_layout
-from .field import BABYBEAR, ptr, stream_handle, to_mont, to_mont_from_host
-from .pcs import FriParams, FriProver
+from .commit import DigestLayers, MerkleTree, Opening, Poseidon2, leaves_layout
+from .field import BABYBEAR, parts_to_pinned, ptr, stream_handle, to_mont, to_mont_from_host
+from .pcs import BasefoldProver, FriParams, FriProver, pair_layout
 from .transcript import DuplexTranscript
+
+MODES = ("fri", "matrix")
+# Digest layers of a "fri" request whose trees are not opened are committed in
+# column chunks of at most this many bytes (only the roots are kept).
+FRI_LAYER_CAP = 16 << 30
 
 
 @dataclass
@@ -57,13 +72,19 @@ class Request:
     def log_n(self) -> int:
         return self.log_h + self.log_blowup
 
-    def footprint(self) -> int:
+    def footprint(self, mode: str = "fri") -> int:
         """HBM bytes held while the request is in flight."""
         n = 1 << self.log_n
-        b = 4 * self.elements          # input (converted to Montgomery in place)
+        b = 4 * self.elements          # input in Montgomery form
         b += 4 * self.width * n         # LDE
         b += min(4 * self.width * n, 1 << 30)  # four-step intermediate share
-        b += 64 * n                     # digest layers (2n - 1 digests of 32 B)
+        if mode == "fri":
+            # one pair-leaf tree (n - 1 digests) per column; only opened
+            # requests keep every column's tree, the others one chunk's worth
+            layers = 32 * self.width * n
+            b += layers if self.fold else min(layers, FRI_LAYER_CAP)
+        else:
+            b += 64 * n                 # one row-leaf tree (2n - 1 digests)
         if self.fold:
             b += 16 * n + 48 * n        # RLC codeword + fold layers and their trees
         return b
@@ -127,59 +148,63 @@ def batch_columns(cw: torch.Tensor, t: DuplexTranscript) -> torch.Tensor:
     return out
 
 
-def fold_and_open(req: Request, cw: torch.Tensor, root: torch.Tensor, perm: Poseidon2,
-                  tree: MerkleTree, layers=None) -> tuple:
-    """Open a committed matrix the Basefold way without the sumcheck: observe
-    the root, batch the columns into one EF4 codeword, observe the fold-round
+def fold_parts(req: Request, cw: torch.Tensor, commitment: torch.Tensor, perm: Poseidon2,
+               tree: MerkleTree, open_commitment: Callable[[torch.Tensor], list[Opening]]
+               ) -> list[torch.Tensor]:
+    """Fold-and-open of a committed request, the Basefold way without the
+    sumcheck: observe the commitment (the matrix root, or the stacked column
+    roots), batch the columns into one EF4 codeword, observe the fold-round
     count (the domain separation of zorch/pcs/jagged/open.py:262-263), fold
     with EF4 challenges down to 2^8 committing every layer, observe the final
-    layer, sample 64 positions, and open the matrix rows and every fold layer
-    there."""
-    n = cw.shape[1]
+    layer, sample 64 positions, and open the commitment and every fold layer
+    there. Returns the proof's parts in wire order: fold roots, final layer,
+    positions, the commitment's openings (row, path), the fold layers'
+    openings (row, path)."""
     t = DuplexTranscript.new(perm, device=cw.device)
-    t.observe_(root)
+    t.observe_(commitment.reshape(-1))
     rlc = batch_columns(cw, t)
     rounds = max(req.log_n - FOLD_FINAL_LOG, 0)
-    # a fill kernel, not a host->device copy: the copy would block this thread
-    # until the batch's stream drained
+    # a fill kernel, not a host->device copy: a pageable copy would block the
+    # calling thread until the stream drained
     t.observe_(torch.full((1,), BABYBEAR.mont(rounds), dtype=torch.int32, device=cw.device))
     code = ReedSolomon(1 << req.log_h, 1 << req.log_blowup, BABYBEAR, coset_shift=31,
                        generator=31)
     prover = FriProver(FriParams(code, tree, rounds, FOLD_QUERIES, 4))
-    proof, t, _ = prover.commit_phase(rlc, t)
-    layers = layers if layers is not None else _ResidentLayers.get(req.rid)
-    # positions are drawn below n on the device: no range read-back (a sync)
-    rows = tree.open_layout(leaves_layout(cw, n, cw.shape[0], 1, n), layers, proof.positions,
-                            cw.shape[0], check=False)
-    return proof, rows
+    proof, _, _ = prover.commit_phase(rlc, t)
+    parts = [proof.roots, proof.final_layer, proof.positions]
+    for op in open_commitment(proof.positions):
+        parts += [op.row, op.path]
+    for op in proof.openings:
+        parts += [op.row, op.path]
+    return parts
 
 
-class _ResidentLayers:
-    """Digest layers of committed matrices kept on the device until opened."""
+def open_matrix(tree: MerkleTree, cw: torch.Tensor, layers: DigestLayers):
+    """Opening of a row-leaf matrix commitment at the query positions."""
+    w, n = cw.shape
+    return lambda pos: [tree.open_layout(leaves_layout(cw, n, w, 1, n), layers, pos, w,
+                                         check=False)]
+
+
+def open_columns(tree: MerkleTree, cw: torch.Tensor, layers: Callable[[int], DigestLayers]):
+    """Openings of every column's pair-leaf tree at the query positions mod
+    n/2 (each column's layer-0 position, zorch/coding/reed_solomon.py:320-329)."""
+    return lambda pos: [tree.open_layout_reduced(pair_layout(cw[c]), layers(c), pos, 2)
+                        for c in range(cw.shape[0])]
+
+
+class _Resident:
+    """Committed requests kept on the device until their openings are taken."""
 
     _table: dict = {}
 
     @classmethod
-    def put(cls, rid: int, layers) -> None:
-        cls._table[rid] = layers
-
-    @classmethod
-    def get(cls, rid: int):
-        return cls._table[rid]
+    def put(cls, rid: int, obj) -> None:
+        cls._table[rid] = obj
 
     @classmethod
     def drop(cls, rid: int) -> None:
         cls._table.pop(rid, None)
-
-
-def _proof_bytes(root: torch.Tensor, proof, rows) -> torch.Tensor:
-    parts = [root.reshape(-1)]
-    if proof is not None:
-        parts += [proof.roots.reshape(-1), proof.final_layer.reshape(-1),
-                  proof.positions.reshape(-1), rows.row.reshape(-1), rows.path.reshape(-1)]
-        for op in proof.openings:
-            parts += [op.row.reshape(-1), op.path.reshape(-1)]
-    return torch.cat(parts)
 
 
 @dataclass
@@ -190,13 +215,14 @@ class _Batch:
     keep: list = dc_field(default_factory=list)
 
 
-def admit(pending: deque, now: float, in_use: int, budget: float, max_batch: int):
+def admit(pending: deque, now: float, in_use: int, budget: float, max_batch: int,
+          mode: str = "fri"):
     """Admission rule, FIFO by arrival: take arrived requests while their HBM
     footprint fits the budget, up to max_batch; a request larger than the
     whole budget is rejected. Returns (admitted, rejected, in_use)."""
     ready, rejected = [], []
     while pending and pending[0].arrival <= now and len(ready) < max_batch:
-        fp = pending[0].footprint()
+        fp = pending[0].footprint(mode)
         if fp > budget:
             rejected.append(pending.popleft())
             continue
@@ -207,11 +233,20 @@ def admit(pending: deque, now: float, in_use: int, budget: float, max_batch: int
     return ready, rejected, in_use
 
 
+def _input(r: Request, host_fed: bool) -> torch.Tensor:
+    if host_fed:  # the conversion kernel reads the pinned input over the host link
+        return to_mont_from_host(BABYBEAR, r.host)
+    return to_mont(BABYBEAR, r.resident)
+
+
 class Server:
     """Continuous batching under an HBM admission budget."""
 
     def __init__(self, budget_bytes: float = 150e9, max_batch: int = 32, streams: int = 3,
-                 perm: Poseidon2 | None = None, tuner=None) -> None:
+                 perm: Poseidon2 | None = None, tuner=None, mode: str = "fri") -> None:
+        if mode not in MODES:
+            raise ValueError(f"mode must be one of {MODES}, got {mode!r}")
+        self.mode = mode
         self.budget = budget_bytes
         self.max_batch = max_batch
         self.perm = perm if perm is not None else Poseidon2.builtin(BABYBEAR)
@@ -222,26 +257,28 @@ class Server:
 
     def _launch(self, reqs: list[Request], host_fed: bool, stream: torch.cuda.Stream) -> _Batch:
         with torch.cuda.stream(stream):
-            jobs, keep = [], []
-            for r in reqs:
-                if host_fed:  # read the pinned input over the host link
-                    x = to_mont_from_host(BABYBEAR, r.host)
-                else:
-                    x = to_mont(BABYBEAR, r.resident)
-                jobs.append(MatrixJob(x, r.log_blowup, 31))
-                keep.append(x)
-            committed = self.committer.commit(jobs)
+            xs = [_input(r, host_fed) for r in reqs]
+            jobs = [MatrixJob(x, r.log_blowup, 31) for x, r in zip(xs, reqs)]
+            keep = list(xs)
             outs = []
+            if self.mode == "fri":
+                committed = self.committer.commit_polys(jobs, [r.fold for r in reqs],
+                                                        FRI_LAYER_CAP)
+            else:
+                committed = self.committer.commit(jobs)
             for r, c in zip(reqs, committed):
-                _ResidentLayers.put(r.rid, c.layers)
-                proof = rows = None
+                _Resident.put(r.rid, c)
+                if self.mode == "fri":
+                    commitment = c.roots
+                    opener = open_columns(self.tree, c.codeword, c.layers)
+                else:
+                    commitment = c.root
+                    opener = open_matrix(self.tree, c.codeword, c.layers)
+                parts = [commitment]
                 if r.fold:
-                    proof, rows = fold_and_open(r, c.codeword, c.root, self.perm, self.tree)
-                flat = _proof_bytes(c.root, proof, rows)
-                host = torch.empty(flat.shape, dtype=flat.dtype, pin_memory=True)
-                host.copy_(flat, non_blocking=True)
-                outs.append(host)
-                keep += [c, flat]
+                    parts += fold_parts(r, c.codeword, commitment, self.perm, self.tree, opener)
+                outs.append(parts_to_pinned(parts))
+                keep += [c, parts]
             ev = torch.cuda.Event()
             ev.record(stream)
         self.batches_launched += 1
@@ -265,13 +302,14 @@ class Server:
                         words = host.numpy().view(np.uint32)
                         results.append(Result(r.rid, words[:8].copy(), words.tobytes(),
                                               r.arrival, done))
-                        in_use -= r.footprint()
-                        _ResidentLayers.drop(r.rid)
+                        in_use -= r.footprint(self.mode)
+                        _Resident.drop(r.rid)
                 else:
                     still.append(b)
             inflight = still
             # admit arrived requests that fit the budget
-            ready, rejected, in_use = admit(pending, now, in_use, self.budget, self.max_batch)
+            ready, rejected, in_use = admit(pending, now, in_use, self.budget, self.max_batch,
+                                            self.mode)
             for r in rejected:
                 results.append(Result(r.rid, np.zeros(8, np.uint32), b"", r.arrival, now))
             if ready:
@@ -290,11 +328,42 @@ class Server:
         return sorted(results, key=lambda r: r.rid)
 
 
+def plain_request(r: Request, x: torch.Tensor, perm: Poseidon2, tree: MerkleTree,
+                  mode: str = "fri") -> list[torch.Tensor]:
+    """One request through the drop-in API, one commit call per polynomial
+    ("fri": FriProver.commit_one per column, roots stacked) or per matrix
+    ("matrix": BasefoldProver.commit); returns the proof parts."""
+    code = ReedSolomon(1 << r.log_h, 1 << r.log_blowup, BABYBEAR, coset_shift=31, generator=31)
+    if mode == "fri":
+        prover = FriProver(FriParams(code, tree, 0, 0))
+        cw = torch.empty((r.width, 1 << r.log_n), dtype=torch.int32, device=x.device)
+        commitment = torch.empty((r.width, 8), dtype=torch.int32, device=x.device)
+        kept = []  # digest layers are kept only when the request opens them
+        for c in range(r.width):
+            cp = prover.commit_one(x[c], out=cw[c])
+            commitment[c].copy_(cp.root)
+            if r.fold:
+                kept.append(cp.digest_layers)
+        opener = open_columns(tree, cw, lambda c: kept[c])
+    else:
+        root, data = BasefoldProver(code, tree).commit_columns(x)
+        cw, commitment = data.codeword, root
+        opener = open_matrix(tree, cw, data.digest_layers)
+    parts = [commitment]
+    if r.fold:
+        parts += fold_parts(r, cw, commitment, perm, tree, opener)
+    return parts
+
+
 def run_plain(requests: list[Request], host_fed: bool = False,
-              perm: Poseidon2 | None = None) -> list[Result]:
-    """One request at a time, one call per polynomial (FriProver.commit), a
-    host synchronisation per call; fold requests run the same fold-and-open as
-    the server on their batched columns."""
+              perm: Poseidon2 | None = None, mode: str = "fri",
+              budget_bytes: float = 150e9) -> list[Result]:
+    """One request at a time, as arrivals allow, through the drop-in API
+    (plain_request); a request's result is read back (a host
+    synchronisation) before the next one starts. A request whose footprint
+    exceeds the budget is rejected (empty result), as the server does."""
+    if mode not in MODES:
+        raise ValueError(f"mode must be one of {MODES}, got {mode!r}")
     perm = perm if perm is not None else Poseidon2.builtin(BABYBEAR)
     tree = MerkleTree(perm)
     results = []
@@ -303,35 +372,14 @@ def run_plain(requests: list[Request], host_fed: bool = False,
         now = time.perf_counter() - t0
         if r.arrival > now:
             time.sleep(r.arrival - now)
-        if host_fed:
-            x = to_mont_from_host(BABYBEAR, r.host)
-        else:
-            x = to_mont(BABYBEAR, r.resident)
-        code = ReedSolomon(1 << r.log_h, 1 << r.log_blowup, BABYBEAR, coset_shift=31,
-                           generator=31)
-        prover = FriProver(FriParams(code, tree, 0, 0))
-        n = 1 << r.log_n
-        cw = torch.empty((r.width, n), dtype=torch.int32, device=x.device)
-        roots = []
-        for c in range(r.width):
-            cp = prover.commit_one(x[c], out=cw[c])
-            roots.append(cp.root)
-            torch.cuda.synchronize()
-        stacked = torch.stack(roots)
-        parts = [stacked.reshape(-1)]
-        if r.fold:
-            t = DuplexTranscript.new(perm, device=x.device)
-            t.observe_(stacked)
-            rlc = batch_columns(cw, t)
-            rounds = max(r.log_n - FOLD_FINAL_LOG, 0)
-            t.observe_(torch.tensor([BABYBEAR.mont(rounds)], dtype=torch.int32, device=x.device))
-            fri = FriProver(FriParams(code, tree, rounds, FOLD_QUERIES, 4))
-            proof, t, _ = fri.commit_phase(rlc, t)
-            parts += [proof.roots.reshape(-1), proof.final_layer.reshape(-1),
-                      proof.positions.reshape(-1)]
-            for op in proof.openings:
-                parts += [op.row.reshape(-1), op.path.reshape(-1)]
-        words = torch.cat(parts).cpu().numpy().view(np.uint32)
+        if r.footprint(mode) > budget_bytes:
+            results.append(Result(r.rid, np.zeros(8, np.uint32), b"", r.arrival,
+                                  time.perf_counter() - t0))
+            continue
+        parts = plain_request(r, _input(r, host_fed), perm, tree, mode)
+        host = parts_to_pinned(parts)
+        torch.cuda.current_stream().synchronize()
+        words = host.numpy().view(np.uint32)
         results.append(Result(r.rid, words[:8].copy(), words.tobytes(), r.arrival,
                               time.perf_counter() - t0))
     return results
