@@ -386,10 +386,12 @@ def served_hash_roofline(reqs, server, mode):
     """LDE and hash device time of the served stream's commits, one request at
     a time on the current stream with CUDA events around each phase (the
     server overlaps requests on several streams, so per-kernel times are
-    taken on this serial replay of the same commits): returns (lde_ms,
-    hash_ms, permutations, lde_bytes)."""
+    taken on this serial replay of the same commits). Every buffer is
+    allocated before the first event, so the timed regions hold kernels only.
+    Returns (lde_ms, hash_ms, permutations, lde_bytes)."""
     import torch
 
+    from zorch_gb300 import _lib
     from zorch_gb300.batch import MatrixJob
     from zorch_gb300.field import BABYBEAR, to_mont
     from zorch_gb300.serve import FRI_LAYER_CAP
@@ -400,41 +402,39 @@ def served_hash_roofline(reqs, server, mode):
     perms = lde_bytes = 0
     for r in reqs:
         x = to_mont(BABYBEAR, r.resident)
+        w, n = r.width, 1 << r.log_n
+        job = MatrixJob(x, r.log_blowup, 31)
+        cw = torch.empty((w, n), dtype=torch.int32, device=x.device)
+        arr = bc._lde_jobs([job], [cw])
+        ws = torch.empty((_lib.lib().zc_rs_encode_batch_workspace_bytes(arr, 1) + 3) // 4 + 64,
+                         dtype=torch.int32, device=x.device)
+        ws = ws[(-ws.data_ptr() % 256) // 4:]  # 256-byte aligned view
+        if mode == "fri":
+            per = w if 32 * w * n <= FRI_LAYER_CAP else max(1, FRI_LAYER_CAP // (32 * n))
+            buf = torch.empty((min(per, w), n - 1, 8), dtype=torch.int32, device=x.device)
+        else:
+            per, buf = w, torch.empty((2 * n - 1, 8), dtype=torch.int32, device=x.device)
+        ctr = torch.empty(64, dtype=torch.int32, device=x.device)
+        torch.cuda.synchronize()
         e = [torch.cuda.Event(enable_timing=True) for _ in range(3)]
         e[0].record(stream)
-        cws = bc.encode([MatrixJob(x, r.log_blowup, 31)])
+        bc.encode([job], [cw], ws)
         e[1].record(stream)
-        w, n = cws[0].shape
         if mode == "fri":
-            if 32 * w * n <= FRI_LAYER_CAP:
-                bc.pair_trees(cws)
-            else:
-                per = max(1, FRI_LAYER_CAP // (32 * n))
-                buf = torch.empty((min(per, w), n - 1, 8), dtype=torch.int32, device=x.device)
-                for c0 in range(0, w, per):
-                    cnt = min(per, w - c0)
-                    bc.pair_trees([cws[0][c0:c0 + cnt]], flats=[buf[:cnt]])
+            for c0 in range(0, w, per):
+                cnt = min(per, w - c0)
+                bc.pair_trees([cw[c0:c0 + cnt]], flats=[buf[:cnt]], counters=ctr)
             perms += w * (n - 1)
         else:
-            bc.merkle(cws)
+            bc.merkle([cw], flats=[buf], counters=ctr)
             perms += n * ((w + 7) // 8) + n - 1
         e[2].record(stream)
         torch.cuda.synchronize()
         lde_ms += e[0].elapsed_time(e[1])
         hash_ms += e[1].elapsed_time(e[2])
         lde_bytes += 4 * r.elements + 4 * w * n
-        del cws, x
+        del cw, x, buf, ws
     return lde_ms, hash_ms, perms, lde_bytes
-
-
-def request_perms(r, mode):
-    """Poseidon2 permutations of a request's commit and fold-and-open (the
-    work model used to set the calibrated arrival rate)."""
-    n = 1 << r.log_n
-    perms = r.width * (n - 1) if mode == "fri" else n * ((r.width + 7) // 8) + n - 1
-    if r.fold:
-        perms += n  # fold layers' pair-leaf trees: n/2 + n/4 + ... leaves and nodes
-    return perms
 
 
 def calibrated_stream(args, n, seed, rate, device):
@@ -1008,15 +1008,17 @@ def main():
         # request rate, a long stream, both arms on the same stream
         del reqs
         torch.cuda.empty_cache()
+        from zorch_gb300.serve import request_work
+
         cal = {}
         for mode in ("fri", "matrix"):
             # the plain path's capacity in permutations/s on the 24-request
             # stream, over the mean permutations of a request of the longer
             # stream (hashing is most of a request's device time)
             shapes = make_stream_for(args)
-            rate = sum(request_perms(q, mode) for q in shapes) / modes[mode]["plain_dt"]
+            rate = sum(request_work(q, mode) for q in shapes) / modes[mode]["plain_dt"]
             probe = calibrated_stream(args, args.cal_requests, args.seed + 1, 1.0, None)
-            mean = sum(request_perms(q, mode) for q in probe) / len(probe)
+            mean = sum(request_work(q, mode) for q in probe) / len(probe)
             lam = 0.8 * rate / mean
             stream_c = calibrated_stream(args, args.cal_requests, args.seed + 1, lam, device)
             served(mode, stream=stream_c[:8])  # warm the shapes' kernels
@@ -1063,6 +1065,9 @@ def main():
                                       "queries; headline: per-polynomial commitments "
                                       "(FriProver.commit bytes)", "budget_gb": args.budget_gb,
                           "max_batch": args.max_batch, "streams": args.streams,
+                          "policy": "shortest work first within a size class, 2 s aging bound; "
+                                    f"{args.streams - 1} high-priority streams for batches of "
+                                    "<= 2^25 permutations, 1 low-priority stream for larger",
                           "field": "babybear", "hash": "poseidon2-16 (built-in)",
                           "l2": "inputs larger than L2"}
 

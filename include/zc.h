@@ -164,7 +164,7 @@ zc_status zc_rs_encode_noalloc(zc_field field, const uint32_t* coeffs, int64_t b
                                uint32_t* out, void* stream);
 
 /* Batched LDE: many jobs (matrices of different heights, widths, blowups) in
- * two persistent launches over a (job, tile) work list -- the batched form of
+ * two launches over a (job, tile) work list -- the batched form of
  * the one-call-per-matrix encode of zorch/pcs/basefold/prover.py:437-447.
  * tile_log selects the shared-memory tile (2^tile_log words; 0 = default),
  * the knob the autotuner sets per (log_n, width) bucket. The workspace holds

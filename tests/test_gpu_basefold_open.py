@@ -20,6 +20,12 @@ from zorch_gb300.field import BABYBEAR, KOALABEAR, to_device, to_host  # noqa: E
 
 
 @pytest.fixture(scope="module", autouse=True)
+
+def _verdict(verifier, *args) -> bool:
+    """The boolean of BasefoldVerifier.verify_batch's (ok, transcript)."""
+    ok, _ = verifier.verify_batch(*args)
+    return ok
+
 def _cuda():
     if not torch.cuda.is_available():
         pytest.skip("no CUDA device")
@@ -94,31 +100,31 @@ def test_basefold_open_matches_oracle(orc, case):
         assert np.array_equal(to_host(op.row), rows) and np.array_equal(to_host(op.path), paths)
     for op, (rows, paths) in zip(proof.query_openings, want["query_openings"]):
         assert np.array_equal(to_host(op.row), rows) and np.array_equal(to_host(op.path), paths)
-    assert verifier.verify(roots, z, values, proof)
+    assert _verdict(verifier, roots, [z], values, proof)
 
 
 def test_basefold_verifier_rejects_tampering(orc):
     verifier, roots, z, values, proof, _ = _open(orc, *CASES[1])
-    assert verifier.verify(roots, z, values, proof)
+    assert _verdict(verifier, roots, [z], values, proof)
     bad_msgs = proof.uni_msgs.clone()
     bad_msgs[0, 0] ^= 1
-    assert not verifier.verify(roots, z, values, dataclasses.replace(proof, uni_msgs=bad_msgs))
+    assert not _verdict(verifier, roots, [z], values, dataclasses.replace(proof, uni_msgs=bad_msgs))
     comp = proof.component_openings[0]
     bad_row = comp.row.clone()
     bad_row[0, 0] ^= 1
     bad_comp = dataclasses.replace(comp, row=bad_row)
-    assert not verifier.verify(roots, z, values, dataclasses.replace(
+    assert not _verdict(verifier, roots, [z], values, dataclasses.replace(
         proof, component_openings=[bad_comp, *proof.component_openings[1:]]))
     bad_vals = [values[0].clone(), *values[1:]]
     bad_vals[0][0, 1] ^= 1
-    assert not verifier.verify(roots, z, bad_vals, proof)
+    assert not _verdict(verifier, roots, [z], bad_vals, proof)
     bad_final = proof.final_poly.clone()
     bad_final[0, 0] ^= 1
-    assert not verifier.verify(roots, z, values, dataclasses.replace(proof, final_poly=bad_final))
+    assert not _verdict(verifier, roots, [z], values, dataclasses.replace(proof, final_poly=bad_final))
     q = proof.query_openings[2]
     bad_q = dataclasses.replace(q, row=q.row.clone())
     bad_q.row[1, 3] ^= 1
-    assert not verifier.verify(roots, z, values, dataclasses.replace(
+    assert not _verdict(verifier, roots, [z], values, dataclasses.replace(
         proof, query_openings=[*proof.query_openings[:2], bad_q, *proof.query_openings[3:]]))
 
 
@@ -191,3 +197,31 @@ def test_graphed_open_replays_the_eager_open(orc):
                         g_proof.component_openings + g_proof.query_openings):
             assert torch.equal(a.row, b.row) and torch.equal(a.path, b.path)
         assert torch.equal(t_out.state, g_t.state)
+
+
+def test_basefold_prove_stage_form(orc):
+    """BasefoldProver.prove / BasefoldVerifier.verify, the reference's stage
+    seam (zorch/pcs/basefold/prover.py:195-209, verifier.py:99-113): the
+    single-matrix open equals open_batch on that matrix, and verifies."""
+    from zorch_gb300.coding import ReedSolomon
+    from zorch_gb300.commit import MerkleTree
+    from zorch_gb300.field import BABYBEAR
+    from zorch_gb300.pcs import BasefoldProver, BasefoldVerifier
+    from zorch_gb300.stage import OpeningClaim, OpeningWitness, TrivialClaim
+    from zorch_gb300.transcript import DuplexTranscript
+
+    gperm, _ = _perms(orc, 0)
+    v, w, q = 10, 6, 12
+    code = ReedSolomon(1 << v, 2, BABYBEAR, coset_shift=31)
+    tree = MerkleTree(gperm, column_major=True)
+    prover = BasefoldProver(code, tree, num_queries=q)
+    root, data = prover.commit_columns(dev(rand_mont(orc, 0, (w, 1 << v), 5)).reshape(w, 1 << v))
+    z = dev(rand_mont(orc, 0, (v, 4), 6)).reshape(v, 4)
+    res = prover.prove(OpeningClaim(root, [z]), OpeningWitness(data), DuplexTranscript.new(gperm))
+    assert res.reduced_claim == TrivialClaim()
+    vals, proof, _ = prover.open_batch([data], [z], DuplexTranscript.new(gperm))
+    assert torch.equal(res.reduction_proof.values, vals[0])
+    assert res.reduction_proof.proof.to_bytes() == proof.to_bytes()
+    vr = BasefoldVerifier(code, tree, num_queries=q).verify(OpeningClaim(root, [z]),
+                                                            res.reduction_proof)
+    assert vr.ok

@@ -49,6 +49,37 @@ def test_admission_fifo_budget_and_rejection():
     assert len(ready) == 3 and len(q) == 7
 
 
+def test_admission_shortest_work_first_with_aging():
+    from zorch_gb300.serve import Request, admit_sjf, request_work
+
+    def req(i, arrival, log_h, width, fold=False):
+        return Request(i, arrival, log_h, width, 1, fold, i)
+
+    big, mid, tiny = req(0, 0.0, 20, 64), req(1, 0.1, 16, 8), req(2, 0.2, 12, 1)
+    assert request_work(tiny) < request_work(mid) < request_work(big)
+    # the least work first; one size class per batch (big is not batched with tiny)
+    q = deque([big, mid, tiny, req(3, 9.0, 10, 1)])
+    ready, rej, used = admit_sjf(q, 1.0, 0, 1e18, 8)
+    assert [r.rid for r in ready] == [2] and not rej
+    assert [r.rid for r in q] == [0, 1, 3]
+    ready, _, _ = admit_sjf(q, 1.0, 0, 1e18, 8)
+    assert [r.rid for r in ready] == [1]
+    # a request that has waited longer than max_wait goes first
+    q = deque([big, req(4, 2.5, 12, 1)])
+    ready, _, _ = admit_sjf(q, 3.0, 0, 1e18, 8, max_wait=2.0)
+    assert [r.rid for r in ready] == [0]
+    # the head does not fit the budget: nothing is admitted, nothing overtakes it
+    q = deque([big, req(5, 0.0, 12, 1)])
+    ready, _, used = admit_sjf(q, 3.0, 0, big.footprint() + 1, 8, max_wait=2.0, )
+    assert [r.rid for r in ready] == [0]
+    ready, _, _ = admit_sjf(q, 3.0, used, big.footprint() + 1, 8, max_wait=0.0)
+    assert not ready
+    # larger than the whole budget: rejected
+    q = deque([req(6, 0.0, 30, 256), req(7, 0.0, 10, 1)])
+    ready, rej, _ = admit_sjf(q, 1.0, 0, 1e12, 8)
+    assert [r.rid for r in rej] == [6] and [r.rid for r in ready] == [7] and not q
+
+
 def _worker(rank, world, port, out):
     import torch.distributed as dist
 

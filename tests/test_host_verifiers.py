@@ -16,6 +16,12 @@ import pytest
 torch = pytest.importorskip("torch")
 
 
+
+def _verdict(verifier, *args) -> bool:
+    """The boolean of BasefoldVerifier.verify_batch's (ok, transcript)."""
+    ok, _ = verifier.verify_batch(*args)
+    return ok
+
 def _t(a) -> torch.Tensor:
     return torch.from_numpy(np.ascontiguousarray(np.asarray(a, np.uint32)).view(np.int32))
 
@@ -70,7 +76,24 @@ def _basefold_case(orc, widths=(3, 2), v=8, queries=6):
 
 def test_basefold_verifier_accepts_the_oracle_proof_on_cpu(orc):
     verifier, roots, z, values, proof = _basefold_case(orc)
-    assert verifier.verify(roots, z, values, proof)
+    assert _verdict(verifier, roots, [z], values, proof)
+
+
+def test_basefold_stage_form_on_cpu(orc):
+    """The reference's stage seam (zorch/pcs/basefold/verifier.py:99-113):
+    verify(OpeningClaim(commitment, [z]), OpeningProof(values, proof),
+    transcript) on a single committed matrix -> VerifyResult(TrivialClaim(),
+    transcript, ok); a wrong value is a False verdict; two points raise."""
+    from zorch_gb300.stage import OpeningClaim, OpeningProof, TrivialClaim
+
+    verifier, roots, z, values, proof = _basefold_case(orc, widths=(5,))
+    vr = verifier.verify(OpeningClaim(roots[0], [z]), OpeningProof(values[0], proof))
+    assert vr.ok and vr.reduced_claim == TrivialClaim()
+    bad = values[0].clone()
+    bad.view(-1)[0] ^= 1
+    assert not verifier.verify(OpeningClaim(roots[0], [z]), OpeningProof(bad, proof)).ok
+    with pytest.raises(ValueError):
+        verifier.verify(OpeningClaim(roots[0], [z, z]), OpeningProof(values[0], proof))
 
 
 def test_basefold_verifier_rejects_tampering_on_cpu(orc):
@@ -81,16 +104,16 @@ def test_basefold_verifier_rejects_tampering_on_cpu(orc):
         t.view(-1)[i] ^= 1
         return t
 
-    assert not verifier.verify(roots, z, values,
+    assert not _verdict(verifier, roots, [z], values,
                                dataclasses.replace(proof, uni_msgs=flip(proof.uni_msgs, 2)))
-    assert not verifier.verify(roots, z, values,
+    assert not _verdict(verifier, roots, [z], values,
                                dataclasses.replace(proof, final_poly=flip(proof.final_poly, 0)))
-    assert not verifier.verify(roots, z, [flip(values[0], 1), *values[1:]], proof)
+    assert not _verdict(verifier, roots, [z], [flip(values[0], 1), *values[1:]], proof)
     q = proof.query_openings[1]
     bad = dataclasses.replace(q, row=flip(q.row, 3))
-    assert not verifier.verify(roots, z, values, dataclasses.replace(
+    assert not _verdict(verifier, roots, [z], values, dataclasses.replace(
         proof, query_openings=[proof.query_openings[0], bad, *proof.query_openings[2:]]))
-    assert not verifier.verify([flip(roots[0], 5), *roots[1:]], z, values, proof)
+    assert not _verdict(verifier, [flip(roots[0], 5), *roots[1:]], [z], values, proof)
 
 
 def test_stacked_verifier_accepts_the_oracle_proof_on_cpu(orc):

@@ -1,7 +1,7 @@
 """Batched matrix commits: many polynomial matrices per launch.
 
 `BatchCommitter.commit(jobs)` runs the coset LDE of every matrix in two
-persistent launches over a (matrix, NTT tile) work list (zc_rs_encode_batch)
+launches over a (matrix, NTT tile) work list (zc_rs_encode_batch)
 and all their row-leaf Merkle trees in 1 + (max depth - 8) + 1 launches over
 (matrix, subtree chunk) work lists (zc_merkle_commit_batch). Each matrix gets
 exactly the root a per-matrix BasefoldProver.commit would produce
@@ -268,7 +268,7 @@ class BatchCommitter:
     def commit_polys(self, jobs: list[MatrixJob], keep_layers: list[bool] | None = None,
                      layer_cap: int = 16 << 30) -> list[CommittedPolys]:
         """FriProver.commit (zorch/pcs/fri/prover.py:92-99) of every column of
-        every job, batched: the LDEs in two persistent launches, every
+        every job, batched: the LDEs in two work-list launches, every
         column's pair-leaf tree in one batched tree commit (a tree family per
         job). Each column's root and digest layers are byte-identical to a
         per-polynomial commit. A job whose layers are not kept

@@ -666,13 +666,7 @@ zc_status tree_batch_wave(const zc_merkle_job* jobs, int n, unsigned long long* 
     trees += d.count;
   }
   B.tree_prefix[n] = trees;
-  int dev = 0, sms = 0;
-  ZC_CUDA(cudaGetDevice(&dev));
-  ZC_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
   ZC_CUDA(cudaMemsetAsync(ctr, 0, sizeof(unsigned long long) * (max_top + 1), st));
-  int occ = 0;
-  ZC_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_tree_batch<K, 0>, kMaxT, 0));
-  if (occ < 1) occ = 1;
   for (int l = 0; l <= max_top; l++) {
     int64_t tot = 0;
     for (int i = 0; i < n; i++) {
@@ -685,8 +679,11 @@ zc_status tree_batch_wave(const zc_merkle_job* jobs, int n, unsigned long long* 
     B.total = tot;
     B.level = l;
     if (tot == 0) continue;
-    int64_t grid = (int64_t)occ * sms;
-    if (grid > tot) grid = tot;
+    // one CTA per work item (each claims items from the counter until none
+    // is left): CTAs retire as their items finish, so the block scheduler can
+    // start blocks of a higher-priority stream between them -- a batch of
+    // small served requests then does not wait for a large one to drain
+    const int64_t grid = tot < 0x7fffffff ? tot : 0x7fffffff;
     if (l == 0)
       k_tree_batch<K, 0><<<(unsigned)grid, kMaxT, 0, st>>>(B, ctr + l, rt);
     else

@@ -486,8 +486,8 @@ zc_status lde_launch(const uint32_t* x, int64_t batch, int log_k, int log_b, uin
 // Many LDE jobs (matrices of different heights, widths and blowups) in two
 // launches: phase A runs every single-pass column and every pass-1 tile of
 // every job, phase B every pass-2 tile. The job table is a __grid_constant__
-// kernel parameter; persistent CTAs claim (job, tile) items from an atomic
-// counter in the workspace, so large and small jobs share the machine.
+// kernel parameter; CTAs claim (job, tile) items from an atomic counter in the
+// workspace, so large and small jobs share the machine.
 constexpr int kMaxLdeJobs = 48;
 
 struct LdeJobDev {
@@ -599,9 +599,6 @@ zc_status lde_batch_wave(const zc_lde_job* jobs, int n, uint32_t* zbase, unsigne
   }
   B.prefix[n] = totA;
   prefB[n] = totB;
-  int dev = 0, sms = 0;
-  ZC_CUDA(cudaGetDevice(&dev));
-  ZC_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
   ZC_CUDA(cudaMemsetAsync(ctr, 0, 2 * sizeof(unsigned long long), st));
   for (int phase = 0; phase < 2; phase++) {
     const int64_t total = phase ? totB : totA;
@@ -612,11 +609,9 @@ zc_status lde_batch_wave(const zc_lde_job* jobs, int n, uint32_t* zbase, unsigne
     if (phase) memcpy(B.prefix, prefB, sizeof(prefB));
     ZC_CUDA(cudaFuncSetAttribute(k_lde_batch<F>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                  (int)smem));
-    int occ = 0;
-    ZC_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_lde_batch<F>, kThreads, smem));
-    if (occ < 1) occ = 1;
-    int64_t grid = (int64_t)occ * sms;
-    if (grid > total) grid = total;
+    // one CTA per work item (see tree_batch_wave): CTAs retire per item, so
+    // blocks of a higher-priority stream can start between them
+    const int64_t grid = total < 0x7fffffff ? total : 0x7fffffff;
     k_lde_batch<F><<<(unsigned)grid, kThreads, smem, st>>>(B, ctr + phase);
     ZC_TRY(launch_check());
   }

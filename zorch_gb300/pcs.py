@@ -633,14 +633,31 @@ class BasefoldProver:
         _, layers = self.tree.commit_layout(leaves_layout(cw, n, K, 1, n), cw.device)
         return layers.root, BasefoldProverData(layers, cw, (K,), columns.contiguous())
 
-    def open_batch(self, rounds: Sequence[BasefoldProverData], z: torch.Tensor,
+    def prove(self, claim: OpeningClaim, witness: OpeningWitness,
+              transcript: DuplexTranscript) -> ProveResult:
+        """Open a single committed matrix, the degenerate one-matrix batch
+        (zorch/pcs/basefold/prover.py:195-209): the claim's points are one
+        shared EF4 point; the reduction proof is OpeningProof(values [w, 4],
+        proof) and the claim reduces to TrivialClaim()."""
+        values, proof, t = self.open_batch([witness.prover_data], claim.points, transcript)
+        return ProveResult(TrivialClaim(), OpeningProof(values[0], proof), t)
+
+    def open_batch(self, rounds: Sequence[BasefoldProverData], points,
                    transcript: DuplexTranscript):
-        """Batch-open the committed matrices at the shared EF4 point z [v, 4]
-        (Montgomery words on the device; _open_batch_body,
-        zorch/pcs/basefold/prover.py:503-547, and _fold_and_query, :419-480):
-        returns (values: per matrix [w, 4], proof, transcript). The whole open
-        runs on the device with no host synchronisation, so it can be captured
-        in a CUDA graph (GraphedBasefoldOpen)."""
+        """Batch-open the committed matrices at the shared EF4 point
+        (zorch/pcs/basefold/prover.py:211-244; _open_batch_body, :503-547, and
+        _fold_and_query, :419-480). `points` is the one-point sequence of the
+        reference ([z], z of shape [v, 4], Montgomery words on the device) or
+        z itself. Returns (values: per matrix [w, 4], proof, transcript). The
+        whole open runs on the device with no host synchronisation, so it can
+        be captured in a CUDA graph (GraphedBasefoldOpen)."""
+        if torch.is_tensor(points):
+            z = points
+        else:
+            if len(points) != 1:
+                raise ValueError(f"BaseFold opens the matrices at one shared point, got "
+                                 f"{len(points)}")
+            z = points[0]
         if not rounds:
             raise ValueError("BaseFold opens at least one committed matrix, got none")
         if z.dim() != 2 or z.shape[1] != 4 or z.shape[0] < 1:
@@ -756,8 +773,28 @@ class BasefoldVerifier:
         self.tree = tree
         self.num_queries = num_queries
 
-    def verify(self, commitments, z, values, proof: BasefoldProof) -> bool:
-        from .transcript import HostDuplexTranscript
+    def verify(self, claim: OpeningClaim, reduction_proof: OpeningProof, transcript=None):
+        """A single-matrix open, the degenerate one-matrix batch
+        (zorch/pcs/basefold/verifier.py:99-113): VerifyResult(TrivialClaim(),
+        transcript, ok)."""
+        ok, t = self.verify_batch([claim.commitment], claim.points, [reduction_proof.values],
+                                  reduction_proof.proof, transcript)
+        return VerifyResult(TrivialClaim(), t, ok)
+
+    def verify_batch(self, commitments, points, values, proof: BasefoldProof, transcript=None):
+        """(ok, transcript) for a batch open at one shared point
+        (zorch/pcs/basefold/verifier.py:115-151). `points` is [z] (or z);
+        `transcript` the verifier's starting transcript (None: fresh)."""
+        if torch.is_tensor(points) or isinstance(points, np.ndarray):
+            z = points
+        else:
+            if len(points) != 1:
+                raise ValueError(f"BaseFold opens the matrices at one shared point, got "
+                                 f"{len(points)}")
+            z = points[0]
+        if not (len(commitments) == len(values) == len(proof.component_openings)):
+            raise ValueError(f"batch mismatch: {len(commitments)} commitments, {len(values)} "
+                             f"value vectors, {len(proof.component_openings)} component openings")
         f, code, tree = self.code.field, self.code, self.tree
         host = lambda x: to_host(x) if torch.is_tensor(x) else np.asarray(x, np.uint32)  # noqa: E731
         ef = lambda words: f.ef_from_mont(words)  # noqa: E731
@@ -766,9 +803,9 @@ class BasefoldVerifier:
         n = code.block_len
         msgs = host(proof.uni_msgs).reshape(-1, 8)
         roots = host(proof.fri_roots).reshape(-1, 8)
+        t = host_transcript(tree.perm, transcript)
         if msgs.shape[0] != v or roots.shape[0] != v or code.message_len != 1 << v:
-            return False
-        t = HostDuplexTranscript(tree.perm)
+            return False, t
         for c in commitments:
             t = t.observe(host(c).reshape(-1))
         vals = [host(x).reshape(-1, 4) for x in values]
@@ -811,7 +848,7 @@ class BasefoldVerifier:
         t, raw = t.sample(self.num_queries)
         positions = [int(x) % n for x in raw]
         if [int(x) for x in host(proof.positions).view(np.int32)] != positions:
-            return False
+            return False, t
         # Merkle openings
         for pos_i, q in enumerate(positions):
             for r, (c, op) in enumerate(zip(commitments, proof.component_openings)):
@@ -823,7 +860,7 @@ class BasefoldVerifier:
                 ok &= tree.verify(torch.as_tensor(roots[i].view(np.int32)), a,
                                   Opening(op.row[pos_i], op.path[:, pos_i]))
         if not ok:
-            return False
+            return False, t
         # batched component rows == fold layer 0's leg at the position
         shift = code.coset_shift
         for pos_i, q in enumerate(positions):
@@ -858,7 +895,7 @@ class BasefoldVerifier:
                 else:
                     expected = ef(final[a])
                 ok &= folded == expected
-        return bool(ok)
+        return bool(ok), t
 
 
 class GraphedBasefoldOpen:

@@ -118,6 +118,17 @@ def make_stream(n: int, seed: int, rate_hz: float, *, log_h=(14, 24), log_w=(0.0
                     int(seed * 1000003 + i)) for i in range(n)]
 
 
+def request_work(r: Request, mode: str = "fri") -> int:
+    """Poseidon2 permutations of a request's commit and fold-and-open -- the
+    hashing that is most of its device time: the cost model of the server's
+    admission order and of the calibrated arrival rate."""
+    n = 1 << r.log_n
+    perms = r.width * (n - 1) if mode == "fri" else n * ((r.width + 7) // 8) + n - 1
+    if r.fold:
+        perms += n  # the fold layers' pair-leaf trees: n/2 + n/4 + ... leaves and nodes
+    return perms
+
+
 def fill_request(req: Request, device="cuda", pinned: bool = False) -> None:
     """Seeded synthetic canonical data for the request (device fill; copied to
     pinned host memory when `pinned`)."""
@@ -210,9 +221,10 @@ class _Resident:
 @dataclass
 class _Batch:
     reqs: list
-    event: torch.cuda.Event
+    events: list   # one per request: its proof bytes are in `outs` once it fires
     outs: list
     keep: list = dc_field(default_factory=list)
+    done: list = dc_field(default_factory=list)
 
 
 def admit(pending: deque, now: float, in_use: int, budget: float, max_batch: int,
@@ -233,6 +245,47 @@ def admit(pending: deque, now: float, in_use: int, budget: float, max_batch: int
     return ready, rejected, in_use
 
 
+def admit_sjf(pending: deque, now: float, in_use: int, budget: float, max_batch: int,
+              mode: str = "fri", max_wait: float = 2.0, class_ratio: float = 8.0):
+    """Admission rule, shortest work first within one size class: among the
+    arrived requests, those that have waited longer than max_wait go first
+    (oldest first), then the rest by ascending work (request_work). The batch
+    takes requests in that order whose work is within class_ratio of the
+    first one's (so a small request never waits on a large one's batch),
+    while their footprints fit the budget, up to max_batch. If the first
+    request does not fit, nothing is admitted (a large request that has
+    waited is not overtaken forever). A request larger than the whole budget
+    is rejected. Returns (admitted, rejected, in_use)."""
+    arrived = [r for r in pending if r.arrival <= now]
+    rejected = [r for r in arrived if r.footprint(mode) > budget]
+    cand = [r for r in arrived if r.footprint(mode) <= budget]
+    old = [r for r in cand if now - r.arrival > max_wait]
+    young = sorted((r for r in cand if now - r.arrival <= max_wait),
+                   key=lambda r: (request_work(r, mode), r.arrival))
+    order = old + young
+    ready = []
+    if order:
+        w0 = request_work(order[0], mode)
+        for r in order:
+            if len(ready) >= max_batch:
+                break
+            w = request_work(r, mode)
+            if ready and not (w0 / class_ratio <= w <= w0 * class_ratio):
+                continue
+            fp = r.footprint(mode)
+            if in_use + fp > budget:
+                if not ready:
+                    break
+                continue
+            in_use += fp
+            ready.append(r)
+    gone = {id(r) for r in ready + rejected}
+    keep = [r for r in pending if id(r) not in gone]
+    pending.clear()
+    pending.extend(keep)
+    return ready, rejected, in_use
+
+
 def _input(r: Request, host_fed: bool) -> torch.Tensor:
     if host_fed:  # the conversion kernel reads the pinned input over the host link
         return to_mont_from_host(BABYBEAR, r.host)
@@ -240,27 +293,56 @@ def _input(r: Request, host_fed: bool) -> torch.Tensor:
 
 
 class Server:
-    """Continuous batching under an HBM admission budget."""
+    """Continuous batching under an HBM admission budget.
+
+    policy "sjf" (default): admit_sjf -- shortest work first within a size
+    class, with an aging bound; batches whose work is at most priority_work
+    permutations run on high-priority streams (streams - 1 of them, round
+    robin), larger ones in order on one low-priority stream. The batched
+    kernels retire their CTAs per work item, so the GPU's block scheduler
+    starts a small batch's blocks while a large batch is still running.
+    policy "fifo": admit (arrival order), every batch on the streams in turn.
+    A request's result is taken as soon as its own bytes are copied back."""
 
     def __init__(self, budget_bytes: float = 150e9, max_batch: int = 32, streams: int = 3,
-                 perm: Poseidon2 | None = None, tuner=None, mode: str = "fri") -> None:
+                 perm: Poseidon2 | None = None, tuner=None, mode: str = "fri",
+                 policy: str = "sjf", priority_work: int = 1 << 25,
+                 max_wait: float = 2.0) -> None:
         if mode not in MODES:
             raise ValueError(f"mode must be one of {MODES}, got {mode!r}")
+        if policy not in ("sjf", "fifo"):
+            raise ValueError(f"policy must be 'sjf' or 'fifo', got {policy!r}")
         self.mode = mode
+        self.policy = policy
         self.budget = budget_bytes
         self.max_batch = max_batch
+        self.priority_work = priority_work
+        self.max_wait = max_wait
         self.perm = perm if perm is not None else Poseidon2.builtin(BABYBEAR)
         self.committer = BatchCommitter(self.perm, BABYBEAR, tuner=tuner)
         self.tree = MerkleTree(self.perm)
-        self.streams = [torch.cuda.Stream() for _ in range(streams)]
+        if policy == "sjf":
+            # a lower number is a higher priority; out-of-range values are clamped
+            self.fast = [torch.cuda.Stream(priority=-10) for _ in range(max(streams - 1, 1))]
+            self.slow = [torch.cuda.Stream(priority=0)]
+        else:
+            self.fast = []
+            self.slow = [torch.cuda.Stream() for _ in range(streams)]
         self.batches_launched = 0
+        self._rr = 0
+
+    def _stream_for(self, reqs: list[Request]) -> torch.cuda.Stream:
+        work = sum(request_work(r, self.mode) for r in reqs)
+        pool = self.fast if self.fast and work <= self.priority_work else self.slow
+        self._rr += 1
+        return pool[self._rr % len(pool)]
 
     def _launch(self, reqs: list[Request], host_fed: bool, stream: torch.cuda.Stream) -> _Batch:
         with torch.cuda.stream(stream):
             xs = [_input(r, host_fed) for r in reqs]
             jobs = [MatrixJob(x, r.log_blowup, 31) for x, r in zip(xs, reqs)]
             keep = list(xs)
-            outs = []
+            outs, events = [], []
             if self.mode == "fri":
                 committed = self.committer.commit_polys(jobs, [r.fold for r in reqs],
                                                         FRI_LAYER_CAP)
@@ -278,43 +360,46 @@ class Server:
                 if r.fold:
                     parts += fold_parts(r, c.codeword, commitment, self.perm, self.tree, opener)
                 outs.append(parts_to_pinned(parts))
+                ev = torch.cuda.Event()
+                ev.record(stream)
+                events.append(ev)
                 keep += [c, parts]
-            ev = torch.cuda.Event()
-            ev.record(stream)
         self.batches_launched += 1
-        return _Batch(reqs, ev, outs, keep)
+        return _Batch(reqs, events, outs, keep, [False] * len(reqs))
 
     def run(self, requests: list[Request], host_fed: bool = False) -> list[Result]:
         pending = deque(sorted(requests, key=lambda r: r.arrival))
         inflight: deque[_Batch] = deque()
         results: list[Result] = []
         in_use = 0
-        si = 0
         t0 = time.perf_counter()
         while pending or inflight:
             now = time.perf_counter() - t0
-            # retire finished batches (in launch order per stream is not required)
+            # retire each request as soon as its own bytes are back
             still = deque()
             for b in inflight:
-                if b.event.query():
-                    done = time.perf_counter() - t0
-                    for r, host in zip(b.reqs, b.outs):
+                for i, (r, host, ev) in enumerate(zip(b.reqs, b.outs, b.events)):
+                    if not b.done[i] and ev.query():
+                        b.done[i] = True
                         words = host.numpy().view(np.uint32)
                         results.append(Result(r.rid, words[:8].copy(), words.tobytes(),
-                                              r.arrival, done))
+                                              r.arrival, time.perf_counter() - t0))
                         in_use -= r.footprint(self.mode)
                         _Resident.drop(r.rid)
-                else:
+                if not all(b.done):
                     still.append(b)
             inflight = still
             # admit arrived requests that fit the budget
-            ready, rejected, in_use = admit(pending, now, in_use, self.budget, self.max_batch,
-                                            self.mode)
+            if self.policy == "sjf":
+                ready, rejected, in_use = admit_sjf(pending, now, in_use, self.budget,
+                                                    self.max_batch, self.mode, self.max_wait)
+            else:
+                ready, rejected, in_use = admit(pending, now, in_use, self.budget,
+                                                self.max_batch, self.mode)
             for r in rejected:
                 results.append(Result(r.rid, np.zeros(8, np.uint32), b"", r.arrival, now))
             if ready:
-                inflight.append(self._launch(ready, host_fed, self.streams[si % len(self.streams)]))
-                si += 1
+                inflight.append(self._launch(ready, host_fed, self._stream_for(ready)))
                 continue
             if inflight:
                 # blocked by the budget / batch size, or waiting for the next arrival:
