@@ -373,6 +373,12 @@ zc_status zc_sumcheck_fold(zc_field field, const uint32_t* mle, int64_t M, const
  * zorch/pcs/basefold/batching.py:66-80). w <= 4096. */
 zc_status zc_rlc_columns(zc_field field, const uint32_t* cw, int64_t n, int32_t w,
                          const uint32_t* challenges, uint32_t* out, void* stream);
+/* out[i] = value for i < n, on the stream (zero through a memset): device
+ * constants such as a zeroed transcript state or a round count to observe,
+ * made without a host copy or a framework kernel, so fold loops stay free of
+ * host synchronisation. No reference counterpart (the reference builds these
+ * as jitted array constants). */
+zc_status zc_fill_u32(uint32_t* out, int64_t n, uint32_t value, void* stream);
 /* Synthetic benchmark data (no reference counterpart): out[i] =
  * SplitMix64(seed * 0x100000001B3 + i) mod p, canonical form. */
 zc_status zc_fill_uniform(zc_field field, uint32_t* out, int64_t n, uint64_t seed, void* stream);

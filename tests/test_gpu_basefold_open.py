@@ -20,12 +20,6 @@ from zorch_gb300.field import BABYBEAR, KOALABEAR, to_device, to_host  # noqa: E
 
 
 @pytest.fixture(scope="module", autouse=True)
-
-def _verdict(verifier, *args) -> bool:
-    """The boolean of BasefoldVerifier.verify_batch's (ok, transcript)."""
-    ok, _ = verifier.verify_batch(*args)
-    return ok
-
 def _cuda():
     if not torch.cuda.is_available():
         pytest.skip("no CUDA device")
@@ -85,6 +79,12 @@ def _open(orc, field, widths, v, log_blowup, shift, queries):
     sh = f.mont(shift) if shift else 0
     want = orc.basefold_open(cperm, field, mats, z, log_blowup, sh, queries, orc.Transcript(cperm))
     return verifier, roots, dev(z).reshape(v, 4), values, proof, want
+
+
+def _verdict(verifier, *args) -> bool:
+    """The boolean of BasefoldVerifier.verify_batch's (ok, transcript)."""
+    ok, _ = verifier.verify_batch(*args)
+    return ok
 
 
 @pytest.mark.parametrize("case", CASES)

@@ -134,6 +134,55 @@ struct HalfPerm {
   }
 };
 
+// duplex_observe on the device (same result): full rate blocks are absorbed
+// with the sponge kept one word per lane (lane l of each half holds word l),
+// each block's eight values loaded straight into lanes 0..7 -- the next
+// block's loads issued before the current permutation -- so a long observe
+// (a final fold layer, a sponge chain of hundreds of blocks) costs one
+// half-warp permutation per block and no per-word state shuffling. The
+// pending prefix and the tail take the generic path.
+template <class F>
+__device__ void duplex_observe(Duplex& t, const uint32_t* v, int64_t m, const HalfPerm<F>& perm) {
+  if (m <= 0) return;
+  int pos = t.in_pos & 7;
+  int64_t i = 0;
+  for (; pos != 0 && i < m; i++) {  // complete a pending block first
+    t.in_buf[pos++] = v[i];
+    if (pos == 8) {
+      for (int j = 0; j < 8; j++) t.sponge[j] = t.in_buf[j];
+      perm(t.sponge);
+      pos = 0;
+    }
+  }
+  if (m - i >= 8) {
+    const int lane = threadIdx.x & 31, l = lane & 15;
+    uint32_t x = 0;
+#pragma unroll
+    for (int j = 0; j < 16; j++) x = l == j ? t.sponge[j] : x;
+    uint32_t nxt = l < 8 ? v[i + l] : 0u;
+    for (; m - i >= 8; i += 8) {
+      const uint32_t cur = nxt;
+      if (m - i >= 16 && l < 8) nxt = v[i + 8 + l];  // issued before the permutation
+      if (l < 8) x = cur;
+      x = p2_permute_half<F>(x, perm.p);
+    }
+#pragma unroll
+    for (int j = 0; j < 16; j++) t.sponge[j] = __shfl_sync(kFullMask, x, (lane & 16) | j);
+  }
+  for (; i < m; i++) {  // the tail stays pending (m - i < 8)
+    t.in_buf[pos++] = v[i];
+  }
+  for (int j = pos; j < 8; j++) t.in_buf[j] = 0;
+  t.in_pos = pos;
+  if (pos == 0) {
+    for (int j = 0; j < 8; j++) t.out_buf[j] = t.sponge[j];
+    t.out_pos = 8;
+  } else {
+    for (int j = 0; j < 8; j++) t.out_buf[j] = 0;
+    t.out_pos = 0;
+  }
+}
+
 // One warp; lane 0 writes the results.
 template <class K>
 __global__ void __launch_bounds__(32) k_duplex_step(const P2Params* rt, uint32_t* state,

@@ -195,11 +195,23 @@ struct FoldLeaf {
   }
 };
 
-// Nodes per subtree CTA at its first level, and its threads: 8 per node, so
-// each level above the first is one round of half-warp permutations (T/2
-// halves); at least a warp.
+// Nodes per tree-top CTA of the batched commit (k_tree_top) at its first
+// level; its threads: 8 per node, so each level above is one round of
+// half-warp permutations.
 constexpr int kSubT = 128;
-inline int subtree_threads(int T) { return 8 * T > 32 ? 8 * T : 32; }
+// Nodes per fused-subtree CTA (k_subtree) at its first level, and its
+// threads: 8 per node up to 1024 (64 half-warps), at least a warp. With 256
+// first-level nodes a launch fuses 9 levels.
+#ifndef ZC_SUBTREE_T
+#define ZC_SUBTREE_T 256
+#endif
+constexpr int kSubMaxT = ZC_SUBTREE_T;
+static_assert(kSubMaxT >= 2 && kSubMaxT <= 256 && (kSubMaxT & (kSubMaxT - 1)) == 0,
+              "subtree width must be a power of two in [2, 256]");
+inline int subtree_threads(int T) {
+  const int t = 8 * T > 32 ? 8 * T : 32;
+  return t < 1024 ? t : 1024;
+}
 
 // Half-warp permutation of the caller's field (lane l passes state word l).
 template <class F>
@@ -236,11 +248,11 @@ __device__ __forceinline__ void subtree_level(const uint32_t* src, uint32_t* dst
 // compressed by half-warps out of ping-pong shared-memory slots, each level
 // written to `layers`.
 template <class K, class Leaf>
-__global__ void __launch_bounds__(8 * kSubT) k_subtree(Leaf leaf, uint32_t* layers, int64_t L,
+__global__ void __launch_bounds__(1024) k_subtree(Leaf leaf, uint32_t* layers, int64_t L,
                                                        int l0, int T, const P2Params* rt) {
   using F = typename K::F;
   __shared__ P2Params s_rt;
-  __shared__ uint32_t sm[2][8 * kSubT];  // [word][node] digest slots
+  __shared__ uint32_t sm[2][8 * kSubMaxT];  // [word][node] digest slots
   K k = KIn<K>::make(rt, &s_rt);
   const P2Params* hp = KIn<K>::half(rt, &s_rt);
   const int t = threadIdx.x;
@@ -256,7 +268,7 @@ __global__ void __launch_bounds__(8 * kSubT) k_subtree(Leaf leaf, uint32_t* laye
       x = half_perm<F>(x, hp);
       if (on && l < 8) {
         lay0[8 * node + l] = x;
-        sm[0][l * kSubT + node] = x;
+        sm[0][l * kSubMaxT + node] = x;
       }
     }
   } else {
@@ -265,7 +277,7 @@ __global__ void __launch_bounds__(8 * kSubT) k_subtree(Leaf leaf, uint32_t* laye
       leaf.digest(base + t, d, k);
       store_digest(lay0 + 8 * t, d);
 #pragma unroll
-      for (int i = 0; i < 8; i++) sm[0][i * kSubT + t] = d[i];
+      for (int i = 0; i < 8; i++) sm[0][i * kSubMaxT + t] = d[i];
     }
   }
   int cur = 0, lvl = l0, width = T;
@@ -273,7 +285,7 @@ __global__ void __launch_bounds__(8 * kSubT) k_subtree(Leaf leaf, uint32_t* laye
     __syncthreads();
     width >>= 1;
     lvl++;
-    subtree_level<F>(sm[cur], sm[cur ^ 1], kSubT,
+    subtree_level<F>(sm[cur], sm[cur ^ 1], kSubMaxT,
                      layers + 8 * (level_offset(L, lvl) + (int64_t)blockIdx.x * width), width, hp);
     cur ^= 1;
   }
@@ -309,10 +321,16 @@ __global__ void __launch_bounds__(kMaxT, HashOcc<K>::v) k_leaf(Leaf leaf, uint32
 }
 
 // Levels with more than this many nodes run one thread per node (k_leaf with
-// NodeLeaf, fully occupied, throughput-bound); the narrow top of the tree is
-// latency-bound and runs as fused CTA subtrees of half-warp permutations
-// (k_subtree with NodeLeaf), log2(T)+1 levels per launch.
-constexpr int64_t kLevelWiseMin = 1 << 13;
+// NodeLeaf, throughput-bound: a level this wide fills the GPU); the narrower
+// top of the tree is latency-bound and runs as fused CTA subtrees of
+// half-warp permutations (k_subtree with NodeLeaf), log2(T)+1 levels per
+// launch. A level of 2^16 nodes as single-thread permutations occupies a
+// fifth of the GPU's threads and takes one permutation's latency (~9 us); as
+// 256 subtree CTAs it takes nine half-warp rounds for nine levels.
+#ifndef ZC_LEVELWISE_MIN_LOG
+#define ZC_LEVELWISE_MIN_LOG 16
+#endif
+constexpr int64_t kLevelWiseMin = (int64_t)1 << ZC_LEVELWISE_MIN_LOG;
 
 // Launches the levels above `l_done` (all levels <= l_done already stored).
 template <class K>
@@ -330,7 +348,7 @@ zc_status finish_tree(uint32_t* layers, int64_t L, int l_done, const P2Params* r
       l += 1;
       continue;
     }
-    const int T = parents < kSubT ? (int)parents : kSubT;
+    const int T = parents < kSubMaxT ? (int)parents : kSubMaxT;
     k_subtree<K, NodeLeaf><<<(unsigned)(parents / T), subtree_threads(T), 0, st>>>(
         nl, layers, L, l + 1, T, rt);
     ZC_TRY(launch_check());
@@ -347,7 +365,7 @@ zc_status commit_tree(const Leaf& leaf, uint32_t* layers, int64_t L, const P2Par
     ZC_TRY(launch_check());
     return finish_tree<K>(layers, L, 0, rt, st);
   }
-  const int T0 = L < kSubT ? (int)L : kSubT;
+  const int T0 = L < kSubMaxT ? (int)L : kSubMaxT;
   k_subtree<K, Leaf><<<(unsigned)(L / T0), subtree_threads(T0), 0, st>>>(leaf, layers, L, 0, T0,
                                                                          rt);
   ZC_TRY(launch_check());
@@ -742,6 +760,12 @@ __host__ __device__ __forceinline__ uint64_t splitmix64(uint64_t x) {
   return x ^ (x >> 31);
 }
 
+__global__ void k_fill_u32(uint32_t* out, int64_t n, uint32_t value) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x)
+    out[i] = value;
+}
+
 __global__ void k_fill_uniform(uint32_t* out, int64_t n, uint64_t seed, uint32_t p) {
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
        i += (int64_t)gridDim.x * blockDim.x)
@@ -990,6 +1014,19 @@ zc_status zc_rlc_columns(zc_field field, const uint32_t* cw, int64_t n, int32_t 
     k_rlc<F><<<(unsigned)blocks, 256, ((size_t)16) << nbv, st>>>(cw, n, w, challenges, nbv, out);
     return launch_check();
   });
+}
+
+zc_status zc_fill_u32(uint32_t* out, int64_t n, uint32_t value, void* stream) {
+  if ((!out && n > 0) || n < 0) return ZC_BAD_ARG;
+  if (n == 0) return ZC_OK;
+  if (value == 0) {
+    ZC_CUDA(cudaMemsetAsync(out, 0, (size_t)n * 4, (cudaStream_t)stream));
+    return ZC_OK;
+  }
+  int64_t blocks = (n + 255) / 256;
+  if (blocks > 152 * 16) blocks = 152 * 16;
+  k_fill_u32<<<(unsigned)blocks, 256, 0, (cudaStream_t)stream>>>(out, n, value);
+  return launch_check();
 }
 
 zc_status zc_fill_uniform(zc_field field, uint32_t* out, int64_t n, uint64_t seed, void* stream) {

@@ -144,6 +144,16 @@ def to_host(t: torch.Tensor) -> np.ndarray:
     return t.detach().contiguous().cpu().numpy().view(np.uint32)
 
 
+def full_u32(shape, value: int = 0, device="cuda") -> torch.Tensor:
+    """An int32 device tensor with every word set to `value` (a u32 bit
+    pattern) on the current stream by zc_fill_u32: a memset for zero, else
+    the library's fill kernel -- no framework kernel and no host copy."""
+    t = torch.empty(shape, dtype=torch.int32, device=device)
+    _lib.check(_lib.lib().zc_fill_u32(ptr(t), t.numel(), int(value) & 0xFFFFFFFF,
+                                      stream_handle()), "fill_u32")
+    return t
+
+
 def parts_to_pinned(parts: list[torch.Tensor]) -> torch.Tensor:
     """Concatenate device tensors into one page-locked host buffer with one
     asynchronous device->host copy per part on the current stream (copy

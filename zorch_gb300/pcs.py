@@ -20,10 +20,21 @@ import torch
 from . import _lib
 from .coding import ReedSolomon
 from .commit import DigestLayers, MerkleTree, Opening, leaves_layout
-from .field import parts_to_bytes, ptr, stream_handle, to_host
+from .field import full_u32, parts_to_bytes, ptr, stream_handle, to_host
 from .stage import (OpeningClaim, OpeningProof, OpeningWitness, ProveResult, TrivialClaim,
                     VerifyResult)
 from .transcript import DuplexTranscript
+
+
+def stack_rows(rows: Sequence[torch.Tensor], shape=None, device=None) -> torch.Tensor:
+    """torch.stack of equally shaped device tensors by one device-to-device
+    copy per row into a preallocated tensor (copy engine, no gather kernel)."""
+    if not rows:
+        return torch.empty((0, *(shape or ())), dtype=torch.int32, device=device)
+    out = torch.empty((len(rows), *rows[0].shape), dtype=rows[0].dtype, device=rows[0].device)
+    for i, r in enumerate(rows):
+        out[i].copy_(r, non_blocking=True)
+    return out
 
 
 def limbs_of(layer: torch.Tensor) -> int:
@@ -281,7 +292,7 @@ class FriProver:
     def commit(self, polys: Sequence[torch.Tensor]):
         """One call per polynomial, roots stacked (zorch/pcs/fri/prover.py:92-99)."""
         committed = [self.commit_one(p) for p in polys]
-        return torch.stack([c.root for c in committed]), FriProverData(tuple(committed))
+        return stack_rows([c.root for c in committed]), FriProverData(tuple(committed))
 
     def commit_phase(self, codeword: torch.Tensor, transcript: DuplexTranscript,
                      first_layer: CommittedLayer | None = None):
@@ -303,8 +314,7 @@ class FriProver:
         br = p.code.bit_reversed
         openings = [open_layer(p.tree, layer, positions, i, br)
                     for i, layer in enumerate(state.layers)]
-        roots_t = torch.stack(roots) if roots else torch.empty((0, 8), dtype=torch.int32,
-                                                               device=codeword.device)
+        roots_t = stack_rows(roots, (8,), codeword.device)
         return CommitPhaseProof(roots_t, list(state.betas), final, positions, openings), t, state
 
 
@@ -332,7 +342,7 @@ class FriProver:
             proofs.append(proof)
         if not values:
             return torch.empty(0, dtype=torch.int32), proofs, t
-        return torch.stack(values), proofs, t
+        return stack_rows(values), proofs, t
 
     def _open_one(self, committed: FriCommittedPoly, z: torch.Tensor, t: DuplexTranscript):
         """_open_one (zorch/pcs/fri/prover.py:151-187) on the device with no
@@ -945,7 +955,7 @@ class GraphedFriCommitPhase:
     def __init__(self, prover: FriProver, device="cuda") -> None:
         self.prover = prover
         code = prover.params.code
-        self.coeffs = torch.zeros(code.message_len, dtype=torch.int32, device=device)
+        self.coeffs = full_u32(code.message_len, 0, device)
         self._run()  # kernel attributes, allocator warm-up
         torch.cuda.synchronize()
         self.graph = torch.cuda.CUDAGraph()

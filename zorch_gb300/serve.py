@@ -42,7 +42,8 @@ from . import _lib
 from .batch import BatchCommitter, MatrixJob
 from .coding import ReedSolomon
 from .commit import DigestLayers, MerkleTree, Opening, Poseidon2, leaves_layout
-from .field import BABYBEAR, parts_to_pinned, ptr, stream_handle, to_mont, to_mont_from_host
+from .field import (BABYBEAR, full_u32, parts_to_pinned, ptr, stream_handle, to_mont,
+                    to_mont_from_host)
 from .pcs import BasefoldProver, FriParams, FriProver, pair_layout
 from .transcript import DuplexTranscript
 
@@ -175,9 +176,9 @@ def fold_parts(req: Request, cw: torch.Tensor, commitment: torch.Tensor, perm: P
     t.observe_(commitment.reshape(-1))
     rlc = batch_columns(cw, t)
     rounds = max(req.log_n - FOLD_FINAL_LOG, 0)
-    # a fill kernel, not a host->device copy: a pageable copy would block the
+    # a device fill, not a host->device copy: a pageable copy would block the
     # calling thread until the stream drained
-    t.observe_(torch.full((1,), BABYBEAR.mont(rounds), dtype=torch.int32, device=cw.device))
+    t.observe_(full_u32(1, BABYBEAR.mont(rounds), cw.device))
     code = ReedSolomon(1 << req.log_h, 1 << req.log_blowup, BABYBEAR, coset_shift=31,
                        generator=31)
     prover = FriProver(FriParams(code, tree, rounds, FOLD_QUERIES, 4))

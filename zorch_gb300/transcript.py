@@ -20,7 +20,7 @@ import torch
 
 from . import _lib
 from .commit import Poseidon2
-from .field import ptr, stream_handle
+from .field import full_u32, ptr, stream_handle
 
 
 class DuplexTranscript:
@@ -36,7 +36,7 @@ class DuplexTranscript:
         if rate != 8:
             raise NotImplementedError("only rate 8 (width 16) is built")
         perm = perm if perm is not None else Poseidon2.builtin()
-        return cls(perm, torch.zeros(_lib.DUPLEX_WORDS, dtype=torch.int32, device=device))
+        return cls(perm, full_u32(_lib.DUPLEX_WORDS, 0, device))
 
     @property
     def field(self):
