@@ -109,6 +109,33 @@ __device__ void root_table(uint32_t* tab, int count, int log_m) {
 // butterfly (u, v) -> (u + v, (u - v) * w_{2H}^pos) with pos the offset in the
 // 2H-block. Consecutive threads take consecutive rows (row-major tiles) so a
 // warp's shared-memory accesses fall on distinct banks.
+// The R stages of one radix-2^R group held in registers: members j at
+// positions base + j S (S = 2^lS, off = base mod S); stage r's twiddle is
+// tw[pos << (sh0 + r)] with pos = off + (j mod 2^hb) S.
+template <class F, int R>
+__device__ __forceinline__ void dif_group(uint32_t (&v)[1 << R], const uint32_t* tw, int off,
+                                          int lS, int sh0) {
+  constexpr int G = 1 << R;
+#pragma unroll
+  for (int r = 0; r < R; r++) {
+    const int hb = R - 1 - r;  // local bit of this stage
+    // pos = off + jm S with jm = j mod 2^hb: index = (off << sh) + jm (S << sh)
+    const int sh = sh0 + r;
+    const int tb = off << sh, ts = 1 << (lS + sh);
+#pragma unroll
+    for (int j = 0; j < G; j++) {
+      if (!(j & (1 << hb))) {
+        const int j2 = j | (1 << hb);
+        const uint32_t w = tw[tb + (j & ((1 << hb) - 1)) * ts];
+        const uint32_t u = v[j], t = v[j2];
+        v[j] = madd<F>(u, t);
+        // u - t in (-p, p) feeds the signed product directly
+        v[j2] = snorm<F>(smul<F>((int32_t)(u - t), (int32_t)w));
+      }
+    }
+  }
+}
+
 template <class F, int R>
 __device__ __forceinline__ void dif_pass(uint32_t* a, int log_rows, int logm, int rs,
                                          const uint32_t* tw, int h0) {
@@ -131,24 +158,7 @@ __device__ __forceinline__ void dif_pass(uint32_t* a, int log_rows, int logm, in
     uint32_t v[G];
 #pragma unroll
     for (int j = 0; j < G; j++) v[j] = ar[pad(j << lS)];
-#pragma unroll
-    for (int r = 0; r < R; r++) {
-      const int hb = R - 1 - r;  // local bit of this stage
-      // pos = off + jm S with jm = j mod 2^hb: index = (off << sh) + jm (S << sh)
-      const int sh = sh0 + r;
-      const int tb = off << sh, ts = 1 << (lS + sh);
-#pragma unroll
-      for (int j = 0; j < G; j++) {
-        if (!(j & (1 << hb))) {
-          const int j2 = j | (1 << hb);
-          const uint32_t w = tw[tb + (j & ((1 << hb) - 1)) * ts];
-          const uint32_t u = v[j], t = v[j2];
-          v[j] = madd<F>(u, t);
-          // u - t in (-p, p) feeds the signed product directly
-          v[j2] = snorm<F>(smul<F>((int32_t)(u - t), (int32_t)w));
-        }
-      }
-    }
+    dif_group<F, R>(v, tw, off, lS, sh0);
 #pragma unroll
     for (int j = 0; j < G; j++) ar[pad(j << lS)] = v[j];
   }
@@ -181,7 +191,7 @@ __device__ void smem_ntt_dif(uint32_t* a, int log_rows, int logm, int rs, const 
 }
 
 constexpr int kThreads = 512;
-constexpr int kLogThreads = 9;
+[[maybe_unused]] constexpr int kLogThreads = 9;
 
 // Asynchronous 4-byte global -> shared copies (cp.async): a tile's loads are
 // all in flight at once, overlapping the twiddle-table set-up, instead of one
@@ -301,13 +311,261 @@ __device__ void lde_pass1_body(const uint32_t* x, uint32_t* z, int log_k1, int l
   for (int p = i2_0; p < k2; p += di) zd[(uint32_t)brev(p, log_k2) << log_k1] = wd[pad(p)];
 }
 
+// ---------------------------------------------------------- fused passes --
+// The four-step passes with the first radix pass fed straight from global
+// memory and the last radix pass writing straight to global memory: each
+// thread loads its group's 2^R members into registers (coalesced across the
+// warp, all loads in flight at once), applies the coset / four-step scale
+// there, runs the R stages and writes shared memory; the middle passes are
+// dif_pass; the last pass reads shared memory, runs its stages and stores the
+// outputs at their final positions. Compared with staging the tile through
+// per-word cp.async copies, a separate scale loop and a separate output loop,
+// this removes one shared-memory round trip and two barrier-separated loops
+// per pass (the words, products and results are the same).
+#ifndef ZC_LDE_FUSED
+#define ZC_LDE_FUSED 1
+#endif
+
+// Balanced radix of pass q of `passes` over the stages left (h0 + 1).
+__host__ __device__ __forceinline__ int pass_radix(int h0, int passes, int q) {
+  return (h0 + 1 + (passes - q) - 1) / (passes - q);
+}
+__host__ __device__ __forceinline__ int pass_count(int logm, int max_r) {
+  return (logm + max_r - 1) / max_r;
+}
+// log2 of the first pass's member stride S (= its number of groups per row).
+__host__ __device__ __forceinline__ int first_stride_log(int logm, int max_r) {
+  return logm - pass_radix(logm - 1, pass_count(logm, max_r), 0);
+}
+
+// Pass 1, one radix pass: rows d < TI (the i1 columns of the tile), row length
+// k2 (the i2 index). first: the members come from x, scaled by
+// gs^(i1 + k1 i2) = gi[d] * G^off * (G^S)^j; last: the outputs go to z at the
+// bit-reversed position brev(p) << log_k1.
+template <class F, int R>
+__device__ __forceinline__ void p1_pass(uint32_t* work, int rs, int log_ti, int log_k1,
+                                        int log_k2, int h0, bool first, bool last,
+                                        const uint32_t* xs, const uint32_t* gi, const uint32_t* Gt,
+                                        uint32_t GS, const uint32_t* tw, uint32_t* zd) {
+  constexpr int G = 1 << R;
+  const int lS = h0 - R + 1;
+  const int total = 1 << (log_ti + log_k2 - R);
+  const int rmask = (1 << log_ti) - 1;
+  const int sh0 = log_k2 - 1 - h0;
+  for (int it = threadIdx.x; it < total; it += blockDim.x) {
+    const int d = it & rmask, g = it >> log_ti;
+    const int off = g & ((1 << lS) - 1), blk = g >> lS;
+    const int base = (blk << (h0 + 1)) | off;  // first pass: blk == 0, base == off
+    uint32_t* ar = work + d * rs + pad(base);
+    uint32_t v[G];
+    if (first) {
+      const uint32_t* src = xs + d + ((int64_t)off << log_k1);
+#pragma unroll
+      for (int j = 0; j < G; j++) v[j] = __ldg(src + ((int64_t)j << (lS + log_k1)));
+      int32_t f = smul<F>((int32_t)gi[d], (int32_t)Gt[off]);
+#pragma unroll
+      for (int j = 0; j < G; j++) {
+        v[j] = snorm<F>(smul<F>((int32_t)v[j], f));
+        if (j + 1 < G) f = smul<F>(f, (int32_t)GS);
+      }
+    } else {
+#pragma unroll
+      for (int j = 0; j < G; j++) v[j] = ar[pad(j << lS)];
+    }
+    dif_group<F, R>(v, tw, off, lS, sh0);
+    if (last) {  // lS == 0: members are the positions base + j
+#pragma unroll
+      for (int j = 0; j < G; j++) zd[d + ((uint32_t)brev(base + j, log_k2) << log_k1)] = v[j];
+    } else {
+#pragma unroll
+      for (int j = 0; j < G; j++) ar[pad(j << lS)] = v[j];
+    }
+  }
+}
+
+// Pass-1 item with fused load and store. Layout: work[TI][rs] | tw[k2/2] |
+// gi[TI] | Gt[S] (S = the first pass's member stride).
+template <class F>
+__device__ void lde_pass1_fused(const uint32_t* x, uint32_t* z, int log_k1, int log_k2, int log_b,
+                                int log_ti, uint32_t h, int s, int tile, int64_t c, uint32_t* sm,
+                                int max_r) {
+  const int k1 = 1 << log_k1, k2 = 1 << log_k2, TI = 1 << log_ti;
+  const int log_k = log_k1 + log_k2, log_n = log_k + log_b;
+  const int rs = row_stride(k2);
+  const int lS0 = first_stride_log(log_k2, max_r);
+  uint32_t* work = sm;
+  uint32_t* tw = work + TI * rs;
+  uint32_t* gi = tw + (k2 > 1 ? k2 / 2 : 1);
+  uint32_t* Gt = gi + TI;
+  const int i1_0 = tile * TI;
+  const uint32_t gs = mmul<F>(h, s ? omega_pow<F>(log_n, (uint32_t)s) : F::ONE);
+  const uint32_t G = mpow<F>(gs, (uint64_t)k1);
+  root_table<F>(tw, k2 > 1 ? k2 / 2 : 1, log_k2);
+  for (int i = threadIdx.x; i < TI; i += blockDim.x) gi[i] = mpow<F>(gs, (uint64_t)(i1_0 + i));
+  for (int i = threadIdx.x; i < (1 << lS0); i += blockDim.x) Gt[i] = mpow<F>(G, (uint64_t)i);
+  const uint32_t GS = mpow<F>(G, (uint64_t)1 << lS0);
+  __syncthreads();
+  const uint32_t* xs = x + (c << log_k) + i1_0;
+  uint32_t* zd = z + ((c << log_b) + s) * ((int64_t)1 << log_k) + i1_0;
+  const int passes = pass_count(log_k2, max_r);
+  int h0 = log_k2 - 1;
+  for (int q = 0; q < passes; q++) {
+    const int R = pass_radix(h0, passes, q);
+    const bool first = q == 0, last = q == passes - 1;
+    switch (R) {
+      case 4: p1_pass<F, 4>(work, rs, log_ti, log_k1, log_k2, h0, first, last, xs, gi, Gt, GS, tw, zd); break;
+      case 3: p1_pass<F, 3>(work, rs, log_ti, log_k1, log_k2, h0, first, last, xs, gi, Gt, GS, tw, zd); break;
+      case 2: p1_pass<F, 2>(work, rs, log_ti, log_k1, log_k2, h0, first, last, xs, gi, Gt, GS, tw, zd); break;
+      default: p1_pass<F, 1>(work, rs, log_ti, log_k1, log_k2, h0, first, last, xs, gi, Gt, GS, tw, zd); break;
+    }
+    if (!last) __syncthreads();
+    h0 -= R;
+  }
+}
+
+// Pass 2, first radix pass from z: a thread takes one group position `off` of
+// row dt for every coset s in turn (consecutive threads on consecutive off:
+// coalesced loads), the scale w_k^(t i1) = w_k^(t off) (w_k^(t S))^j computed
+// once for the b rows. Shared rows are ordered r = dt * b + s.
+template <class F, int R>
+__device__ __forceinline__ void p2_first(uint32_t* work, int rs, int log_b, int log_tt, int log_k1,
+                                         int log_k, int t2_0, const uint32_t* zc_,
+                                         const uint32_t* tw, bool last, uint32_t* oc,
+                                         int log_k2, int brev_out) {
+  constexpr int G = 1 << R;
+  const int h0 = log_k1 - 1, lS = h0 - R + 1;
+  const int total = 1 << (log_tt + lS);
+  const int b = 1 << log_b;
+  const uint32_t kmask = (1u << log_k) - 1;
+  for (int it = threadIdx.x; it < total; it += blockDim.x) {
+    const int off = it & ((1 << lS) - 1), dt = it >> lS;
+    const uint32_t t = (uint32_t)(t2_0 + dt);
+    int32_t f[G];
+    f[0] = (int32_t)omega_pow<F>(log_k, (t * (uint32_t)off) & kmask);
+    const int32_t step = (int32_t)omega_pow<F>(log_k, (t << lS) & kmask);
+#pragma unroll
+    for (int j = 1; j < G; j++) f[j] = smul<F>(f[j - 1], step);
+    for (int s = 0; s < b; s++) {
+      const uint32_t* src = zc_ + ((int64_t)s << log_k) + ((int64_t)t << log_k1) + off;
+      uint32_t v[G];
+#pragma unroll
+      for (int j = 0; j < G; j++) v[j] = __ldg(src + (j << lS));
+#pragma unroll
+      for (int j = 0; j < G; j++) v[j] = snorm<F>(smul<F>((int32_t)v[j], f[j]));
+      dif_group<F, R>(v, tw, off, lS, 0);
+      if (last) {  // a single pass (k1 <= 16): off == 0, positions j
+#pragma unroll
+        for (int j = 0; j < G; j++) {
+          if (brev_out)
+            oc[((int64_t)brev(s, log_b) << log_k) + ((int64_t)brev((int)t, log_k2) << log_k1) + j] = v[j];
+          else
+            oc[((int64_t)t << log_b) + s + ((int64_t)brev(j, log_k1) << (log_k2 + log_b))] = v[j];
+        }
+      } else {
+        uint32_t* ar = work + ((dt << log_b) + s) * rs + pad(off);
+#pragma unroll
+        for (int j = 0; j < G; j++) ar[pad(j << lS)] = v[j];
+      }
+    }
+  }
+}
+
+// Pass 2, last radix pass to `out`: consecutive threads on consecutive rows
+// r = dt * b + s, so natural-order stores out[b (t2 + k2 t1) + s] are
+// coalesced and the shared-memory reads fall on distinct banks.
+template <class F, int R>
+__device__ __forceinline__ void p2_last(uint32_t* work, int rs, int log_b, int log_tt, int log_k1,
+                                        int log_k2, int log_k, int t2_0, int h0,
+                                        const uint32_t* tw, uint32_t* oc, int brev_out) {
+  constexpr int G = 1 << R;
+  const int log_rows = log_b + log_tt;
+  const int total = 1 << (log_rows + log_k1 - R);
+  const int rmask = (1 << log_rows) - 1;
+  const int sh0 = log_k1 - 1 - h0;  // h0 == R - 1: lS == 0
+  for (int it = threadIdx.x; it < total; it += blockDim.x) {
+    const int r = it & rmask, g = it >> log_rows;
+    const int s = r & ((1 << log_b) - 1), dt = r >> log_b;
+    const int base = g << R;
+    uint32_t* ar = work + r * rs + pad(base);
+    uint32_t v[G];
+#pragma unroll
+    for (int j = 0; j < G; j++) v[j] = ar[pad(j)];
+    dif_group<F, R>(v, tw, 0, 0, sh0);
+    const int t = t2_0 + dt;
+    if (brev_out) {
+      uint32_t* orow = oc + ((int64_t)brev(s, log_b) << log_k) +
+                       ((int64_t)brev(t, log_k2) << log_k1) + base;
+#pragma unroll
+      for (int j = 0; j < G; j++) orow[j] = v[j];
+    } else {
+      uint32_t* ob = oc + ((int64_t)t << log_b) + s;
+      const int sh = log_k2 + log_b;
+#pragma unroll
+      for (int j = 0; j < G; j++) ob[(int64_t)brev(base + j, log_k1) << sh] = v[j];
+    }
+  }
+}
+
+// Pass-2 item with fused load and store. Layout: work[b*TT][rs] | tw[k1/2].
+template <class F>
+__device__ void lde_pass2_fused(const uint32_t* z, uint32_t* out, int log_k1, int log_k2,
+                                int log_b, int log_tt, int tile, int64_t c, uint32_t* sm,
+                                int brev_out, int max_r) {
+  const int k1 = 1 << log_k1;
+  const int log_k = log_k1 + log_k2, log_n = log_k + log_b;
+  const int log_rows = log_b + log_tt;
+  const int rs = row_stride(k1);
+  uint32_t* work = sm;
+  uint32_t* tw = work + (rs << log_rows);
+  const int t2_0 = tile << log_tt;
+  const uint32_t* zc_ = z + (c << log_n);
+  uint32_t* oc = out + (c << log_n);
+  root_table<F>(tw, k1 > 1 ? k1 / 2 : 1, log_k1);
+  __syncthreads();
+  const int passes = pass_count(log_k1, max_r);
+  int h0 = log_k1 - 1;
+  for (int q = 0; q < passes; q++) {
+    const int R = pass_radix(h0, passes, q);
+    const bool first = q == 0, last = q == passes - 1;
+    if (first) {
+      switch (R) {
+        case 4: p2_first<F, 4>(work, rs, log_b, log_tt, log_k1, log_k, t2_0, zc_, tw, last, oc, log_k2, brev_out); break;
+        case 3: p2_first<F, 3>(work, rs, log_b, log_tt, log_k1, log_k, t2_0, zc_, tw, last, oc, log_k2, brev_out); break;
+        case 2: p2_first<F, 2>(work, rs, log_b, log_tt, log_k1, log_k, t2_0, zc_, tw, last, oc, log_k2, brev_out); break;
+        default: p2_first<F, 1>(work, rs, log_b, log_tt, log_k1, log_k, t2_0, zc_, tw, last, oc, log_k2, brev_out); break;
+      }
+    } else if (last) {
+      switch (R) {
+        case 4: p2_last<F, 4>(work, rs, log_b, log_tt, log_k1, log_k2, log_k, t2_0, h0, tw, oc, brev_out); break;
+        case 3: p2_last<F, 3>(work, rs, log_b, log_tt, log_k1, log_k2, log_k, t2_0, h0, tw, oc, brev_out); break;
+        case 2: p2_last<F, 2>(work, rs, log_b, log_tt, log_k1, log_k2, log_k, t2_0, h0, tw, oc, brev_out); break;
+        default: p2_last<F, 1>(work, rs, log_b, log_tt, log_k1, log_k2, log_k, t2_0, h0, tw, oc, brev_out); break;
+      }
+    } else {
+      switch (R) {
+        case 4: dif_pass<F, 4>(work, log_rows, log_k1, rs, tw, h0); break;
+        case 3: dif_pass<F, 3>(work, log_rows, log_k1, rs, tw, h0); break;
+        case 2: dif_pass<F, 2>(work, log_rows, log_k1, rs, tw, h0); break;
+        default: dif_pass<F, 1>(work, log_rows, log_k1, rs, tw, h0); break;
+      }
+    }
+    if (!last) __syncthreads();
+    h0 -= R;
+  }
+}
+
 template <class F>
 __global__ void __launch_bounds__(kThreads, 2) k_lde_pass1(const uint32_t* x, uint32_t* z, int log_k1,
                                                         int log_k2, int log_b, int log_ti,
                                                         uint32_t h) {
   extern __shared__ uint32_t sm[];
+#if ZC_LDE_FUSED
+  lde_pass1_fused<F>(x, z, log_k1, log_k2, log_b, log_ti, h, blockIdx.x, blockIdx.y, blockIdx.z,
+                     sm, kMaxRadixLog);
+#else
   lde_pass1_body<F>(x, z, log_k1, log_k2, log_b, log_ti, h, blockIdx.x, blockIdx.y, blockIdx.z,
                     sm);
+#endif
 }
 
 // Pass 2 item (t2 tile, column c): rows (s, t2) for all b cosets and TT
@@ -394,7 +652,12 @@ __global__ void __launch_bounds__(kThreads, 2) k_lde_pass2(const uint32_t* z, ui
                                                         int log_k1, int log_k2, int log_b,
                                                         int log_tt, int brev_out) {
   extern __shared__ uint32_t sm[];
+#if ZC_LDE_FUSED
+  lde_pass2_fused<F>(z, out, log_k1, log_k2, log_b, log_tt, blockIdx.x, blockIdx.y, sm, brev_out,
+                     kMaxRadixLog);
+#else
   lde_pass2_body<F>(z, out, log_k1, log_k2, log_b, log_tt, blockIdx.x, blockIdx.y, sm, brev_out);
+#endif
 }
 
 struct LdePlan {
@@ -407,7 +670,7 @@ constexpr int kSmallMaxLogK = 12;
 constexpr int kSmallMaxLogN = 14;
 constexpr int kTileLog = 14;  // elements per shared-memory tile (2^14 = 64 KB)
 
-inline LdePlan plan_lde(int log_k, int log_b, int tile_log = 0) {
+inline LdePlan plan_lde(int log_k, int log_b, int tile_log = 0, int max_r = kMaxRadixLog) {
   LdePlan p{};
   const int k = 1 << log_k, b = 1 << log_b;
   const int tl = tile_log > 0 ? tile_log : kTileLog;
@@ -427,6 +690,9 @@ inline LdePlan plan_lde(int log_k, int log_b, int tile_log = 0) {
   const int k1 = 1 << p.log_k1, k2 = 1 << p.log_k2;
   p.smem1 = 4 * ((size_t)(1 << p.log_ti) * row_stride(k2) + (k2 > 1 ? k2 / 2 : 1) +
                  (1 << p.log_ti));
+#if ZC_LDE_FUSED
+  p.smem1 += (size_t)4 << first_stride_log(p.log_k2, max_r);  // the G^off table
+#endif
   p.smem2 = 4 * ((size_t)(b << p.log_tt) * row_stride(k1) + (k1 > 1 ? k1 / 2 : 1));
   return p;
 }
@@ -537,13 +803,23 @@ __global__ void __launch_bounds__(kThreads, 2) k_lde_batch(const __grid_constant
       const int64_t per_col = (int64_t)b << (J.log_k1 - J.log_ti);
       const int64_t c = local / per_col;
       const int r = (int)(local - c * per_col);
+#if ZC_LDE_FUSED
+      lde_pass1_fused<F>(J.x, J.z, J.log_k1, J.log_k2, J.log_b, J.log_ti, J.h, r & (b - 1),
+                         r >> J.log_b, c, sm, J.max_r);
+#else
       lde_pass1_body<F>(J.x, J.z, J.log_k1, J.log_k2, J.log_b, J.log_ti, J.h, r & (b - 1),
                         r >> J.log_b, c, sm, J.max_r);
+#endif
     } else {
       const int64_t tiles = (int64_t)1 << (J.log_k2 - J.log_tt);
       const int64_t c = local / tiles;
+#if ZC_LDE_FUSED
+      lde_pass2_fused<F>(J.z, J.out, J.log_k1, J.log_k2, J.log_b, J.log_tt,
+                         (int)(local - c * tiles), c, sm, J.brev_out, J.max_r);
+#else
       lde_pass2_body<F>(J.z, J.out, J.log_k1, J.log_k2, J.log_b, J.log_tt,
                         (int)(local - c * tiles), c, sm, J.brev_out, J.max_r);
+#endif
     }
     __syncthreads();  // the item's shared memory is free again
   }
@@ -568,7 +844,8 @@ zc_status lde_batch_wave(const zc_lde_job* jobs, int n, uint32_t* zbase, unsigne
   int64_t prefB[kMaxLdeJobs + 1];
   for (int i = 0; i < n; i++) {
     const zc_lde_job& j = jobs[i];
-    const LdePlan p = plan_lde(j.log_k, j.log_blowup, j.tile_log);
+    const LdePlan p = plan_lde(j.log_k, j.log_blowup, j.tile_log,
+                               j.radix_log ? j.radix_log : kMaxRadixLog);
     LdeJobDev& d = B.job[i];
     d.x = j.coeffs;
     d.out = j.out;
@@ -799,7 +1076,8 @@ zc_status zc_rs_encode_batch(zc_field field, const zc_lde_job* jobs, int32_t njo
         return ZC_BAD_ARG;
       }
       if (j.log_k + j.log_blowup > F::TWO_ADICITY || j.log_k > 24) return ZC_BAD_SHAPE;
-      const LdePlan p = plan_lde(j.log_k, j.log_blowup, j.tile_log);
+      const LdePlan p = plan_lde(j.log_k, j.log_blowup, j.tile_log,
+                                 j.radix_log ? j.radix_log : kMaxRadixLog);
       const size_t cap = 227 * 1024;
       if ((p.small && p.smem_small > cap) || (!p.small && (p.smem1 > cap || p.smem2 > cap)))
         return ZC_UNSUPPORTED;
