@@ -263,6 +263,23 @@ zc_status zc_fri_fold_commit(const zc_poseidon2* p, const uint32_t* cw, int64_t 
                              uint32_t generator, uint32_t* out, uint32_t* next_layers,
                              void* stream);
 
+/* zc_fri_fold_commit (bit_reversed = 0) or zc_fri_fold_commit_bitrev (1)
+ * followed, in the launch that computes the new tree's root, by the next
+ * round's transcript hop (PreFoldPairCommitRound, zorch/pcs/fold.py:106-113):
+ * observe the 8 root words into the packed 34-word duplex state `state`
+ * (read and advanced in place) and squeeze n_chal (0..64) words into `chal`
+ * -- the same state and words as zc_duplex_step(state, root, 8, n_chal), one
+ * launch fewer per fold round. */
+zc_status zc_fri_fold_commit_hop(const zc_poseidon2* p, const uint32_t* cw, int64_t n, int ef_in,
+                                 const uint32_t* beta, int ef_beta, uint32_t shift_mont,
+                                 uint32_t generator, int32_t bit_reversed, uint32_t* out,
+                                 uint32_t* next_layers, uint32_t* state, int32_t n_chal,
+                                 uint32_t* chal, void* stream);
+/* zc_merkle_commit followed, in the root's launch, by the same transcript hop
+ * (a first pre-fold round's commit, observe(root), sample). */
+zc_status zc_merkle_commit_hop(const zc_poseidon2* p, zc_leaves leaves, uint32_t* layers,
+                               uint32_t* state, int32_t n_chal, uint32_t* chal, void* stream);
+
 /* Replaces ReedSolomon.fold_group (zorch/coding/reed_solomon.py:357-381;
  * fri_fold_k :551-586): the k-ary fold, k = 2^log_k (log_k 1..4), of a
  * natural-order layer of n elements. Group p < n/k is

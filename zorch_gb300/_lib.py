@@ -82,6 +82,9 @@ def _declare(lib: C.CDLL) -> None:
         "zc_fri_fold_k": (st, [st, vp, i64, C.c_int, vp, C.c_int, C.c_int, u32, u32, vp, vp]),
         "zc_fri_fold_commit_bitrev": (st, [vp, vp, i64, C.c_int, vp, C.c_int, u32, u32, vp, vp,
                                            vp]),
+        "zc_fri_fold_commit_hop": (st, [vp, vp, i64, C.c_int, vp, C.c_int, u32, u32, i32, vp, vp,
+                                        vp, i32, vp, vp]),
+        "zc_merkle_commit_hop": (st, [vp, Leaves, vp, vp, i32, vp, vp]),
         "zc_smcs_bind_root": (st, [vp, vp, u32, u32, vp, vp]),
         "zc_eq_expand_workspace_bytes": (sz, [i32]),
         "zc_eq_expand": (st, [st, vp, i32, vp, vp, sz, vp]),

@@ -1,6 +1,6 @@
 """Build the CUDA library libzc.so in-tree for sm_103a (GB300).
 
-Five translation units compiled in parallel with nvcc, then linked into
+Seven translation units compiled in parallel with nvcc, then linked into
 zorch_gb300/_build/libzc.so. No cmake, no torch extension machinery: the
 library exposes a plain C ABI (include/zc.h) that Python reaches via ctypes.
 """
@@ -18,7 +18,8 @@ ROOT = PKG.parent
 CSRC = PKG / "csrc"
 OUT_DIR = PKG / "_build"
 LIB = OUT_DIR / "libzc.so"
-SOURCES = ["zc_core.cu", "zc_ntt.cu", "zc_merkle.cu", "zc_sumcheck.cu", "zc_deep.cu"]
+SOURCES = ["zc_core.cu", "zc_ntt.cu", "zc_merkle.cu", "zc_fold.cu", "zc_fold_bitrev.cu",
+           "zc_sumcheck.cu", "zc_deep.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 

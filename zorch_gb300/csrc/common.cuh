@@ -29,6 +29,25 @@ inline int ilog2(int64_t x) {
   return l;
 }
 
+// Work items a CTA of the batched (work-list) kernels takes before it retires
+// (0: CTAs stay resident until the list is empty). Retiring CTAs let the block
+// scheduler start blocks of a higher-priority stream in between, so a small
+// served batch does not wait for a large one to drain.
+#ifndef ZC_ITEMS_PER_CTA
+#define ZC_ITEMS_PER_CTA 8
+#endif
+constexpr int kItemsPerCta = ZC_ITEMS_PER_CTA;
+
+// Grid of a work-list launch over `total` items: every item is claimed (grid *
+// items per CTA >= total), never more CTAs than items; resident CTAs only
+// (occ per SM) when CTAs do not retire.
+inline int64_t batch_grid(int64_t total, int occ, int sms) {
+  int64_t grid = kItemsPerCta > 0 ? (total + kItemsPerCta - 1) / kItemsPerCta
+                                  : (int64_t)(occ > 0 ? occ : 1) * sms;
+  if (grid > total) grid = total;
+  return grid < 0x7fffffff ? grid : 0x7fffffff;
+}
+
 // log2 of a power of two, on the device.
 __device__ __forceinline__ int ilog2_dev(int64_t x) { return 63 - __clzll((long long)x); }
 

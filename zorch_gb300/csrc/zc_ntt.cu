@@ -788,7 +788,7 @@ __global__ void __launch_bounds__(kThreads, 2) k_lde_batch(const __grid_constant
                                                         unsigned long long* counter) {
   extern __shared__ uint32_t sm[];
   __shared__ long long s_item;
-  for (;;) {
+  for (int done = 0; kItemsPerCta == 0 || done < kItemsPerCta; done++) {
     if (threadIdx.x == 0) s_item = (long long)atomicAdd(counter, 1ull);
     __syncthreads();
     const int64_t it = s_item;
@@ -886,9 +886,11 @@ zc_status lde_batch_wave(const zc_lde_job* jobs, int n, uint32_t* zbase, unsigne
     if (phase) memcpy(B.prefix, prefB, sizeof(prefB));
     ZC_CUDA(cudaFuncSetAttribute(k_lde_batch<F>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                  (int)smem));
-    // one CTA per work item (see tree_batch_wave): CTAs retire per item, so
-    // blocks of a higher-priority stream can start between them
-    const int64_t grid = total < 0x7fffffff ? total : 0x7fffffff;
+    int dev = 0, sms = 0, occ = 0;
+    ZC_CUDA(cudaGetDevice(&dev));
+    ZC_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    ZC_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_lde_batch<F>, kThreads, smem));
+    const int64_t grid = batch_grid(total, occ, sms);
     k_lde_batch<F><<<(unsigned)grid, kThreads, smem, st>>>(B, ctr + phase);
     ZC_TRY(launch_check());
   }

@@ -85,6 +85,9 @@ class FoldState:
     layers: tuple = ()
     pending: CommittedLayer | None = None
     betas: tuple = ()  # the challenge sampled in each round so far
+    # the pending layer's challenge when the previous round's launch already
+    # ran this round's transcript hop (fuse_hop); the transcript is past it
+    pending_beta: torch.Tensor | None = None
 
 
 @dataclass
@@ -100,27 +103,56 @@ class PreFoldPairCommitRound:
     challenge_limbs: int = 1
     fused: bool = True
     last_round: int | None = None  # index of the final round (no commit after it)
+    # Run each round's observe(root) + sample(beta) inside the launch that
+    # computes the root (zc_merkle_commit_hop / zc_fri_fold_commit_hop): one
+    # launch fewer per round. The transcript a round returns is then already
+    # past the next round's hop, so this is only for rounds that follow each
+    # other directly on one transcript (FriProver.commit_phase).
+    fuse_hop: bool = False
 
     def commit_layer(self, cw: torch.Tensor) -> CommittedLayer:
         _, layers = self.tree.commit_layout(pair_layout(cw, self.code.bit_reversed), cw.device)
         return CommittedLayer(cw, layers)
 
+    def commit_layer_hop(self, cw: torch.Tensor, t: DuplexTranscript):
+        """commit_layer, then observe(root) + sample(beta) in the root's launch."""
+        L = cw.shape[0] // 2
+        flat = torch.empty((2 * L - 1, 8), dtype=torch.int32, device=cw.device)
+        beta = torch.empty(self.challenge_limbs, dtype=torch.int32, device=cw.device)
+        _lib.check(_lib.lib().zc_merkle_commit_hop(
+            self.tree.perm.handle, pair_layout(cw, self.code.bit_reversed), ptr(flat),
+            ptr(t.state), self.challenge_limbs, ptr(beta), stream_handle()), "merkle_commit_hop")
+        return CommittedLayer(cw, DigestLayers(flat, L)), beta
+
     def __call__(self, state: FoldState, t: DuplexTranscript):
         cw = state.codeword
-        layer = state.pending if state.pending is not None else self.commit_layer(cw)
         t = t._copy()
-        beta = t.observe_and_sample_(layer.root, self.challenge_limbs)
+        if state.pending is not None and state.pending_beta is not None:
+            layer, beta = state.pending, state.pending_beta
+        elif state.pending is None and self.fuse_hop:
+            layer, beta = self.commit_layer_hop(cw, t)
+        else:
+            layer = state.pending if state.pending is not None else self.commit_layer(cw)
+            beta = t.observe_and_sample_(layer.root, self.challenge_limbs)
         n = cw.shape[0]
         level = len(state.layers)
         is_last = self.last_round is not None and level >= self.last_round
+        next_beta = None
         if self.fused and not is_last and n >= 4:
-            out, pending = self.fold_commit(cw, beta, level)
+            if self.fuse_hop:
+                out, pending, next_beta = self.fold_commit(cw, beta, level, t)
+            else:
+                out, pending = self.fold_commit(cw, beta, level)
         else:
             out, pending = self.code.fold(cw, beta), None
-        return FoldState(out, state.layers + (layer,), pending, state.betas + (beta,)), t, \
-            layer.root
+        return FoldState(out, state.layers + (layer,), pending, state.betas + (beta,),
+                         next_beta), t, layer.root
 
-    def fold_commit(self, cw: torch.Tensor, beta: torch.Tensor, level: int):
+    def fold_commit(self, cw: torch.Tensor, beta: torch.Tensor, level: int,
+                    hop: DuplexTranscript | None = None):
+        """The fold of this round fused with the commit of the next layer;
+        with `hop`, also that layer's observe(root) + sample(beta) on `hop`
+        (in place), returning the sampled beta as a third value."""
         n = cw.shape[0]
         ef_in = cw.dim() == 2
         ef_beta = beta.numel() == 4
@@ -129,6 +161,14 @@ class PreFoldPairCommitRound:
                           device=cw.device)
         L = n // 4
         flat = torch.empty((2 * L - 1, 8), dtype=torch.int32, device=cw.device)
+        if hop is not None:
+            nxt = torch.empty(self.challenge_limbs, dtype=torch.int32, device=cw.device)
+            _lib.check(_lib.lib().zc_fri_fold_commit_hop(
+                self.tree.perm.handle, ptr(cw), n, int(ef_in), ptr(beta), int(ef_beta),
+                self.code.level_shift_mont(level), self.code.generator or 0,
+                int(self.code.bit_reversed), ptr(out), ptr(flat), ptr(hop.state),
+                self.challenge_limbs, ptr(nxt), stream_handle()), "fri_fold_commit_hop")
+            return out, CommittedLayer(out, DigestLayers(flat, L)), nxt
         fn = (_lib.lib().zc_fri_fold_commit_bitrev if self.code.bit_reversed
               else _lib.lib().zc_fri_fold_commit)
         _lib.check(fn(
@@ -301,7 +341,7 @@ class FriProver:
         of _open_one, zorch/pcs/fri/prover.py:151-187, on `codeword` itself)."""
         p = self.params
         rnd = PreFoldPairCommitRound(p.code, p.tree, p.challenge_limbs,
-                                     last_round=p.num_rounds - 1)
+                                     last_round=p.num_rounds - 1, fuse_hop=True)
         state = FoldState(codeword, (), first_layer)
         t = transcript._copy()
         roots = []
