@@ -396,6 +396,13 @@ zc_status zc_rlc_columns(zc_field field, const uint32_t* cw, int64_t n, int32_t 
  * host synchronisation. No reference counterpart (the reference builds these
  * as jitted array constants). */
 zc_status zc_fill_u32(uint32_t* out, int64_t n, uint32_t value, void* stream);
+/* Device-to-device copy of `rows` rows of `row_bytes` bytes, row i from
+ * src + i * src_pitch to dst + i * dst_pitch, as one 2D copy on the copy
+ * engine (no kernel): gathers strided rows such as each tree's root out of a
+ * stack of digest layers. Pitches >= row_bytes. No reference counterpart (the
+ * reference slices jitted arrays). */
+zc_status zc_copy_rows(void* dst, int64_t dst_pitch, const void* src, int64_t src_pitch,
+                       int64_t row_bytes, int64_t rows, void* stream);
 /* Synthetic benchmark data (no reference counterpart): out[i] =
  * SplitMix64(seed * 0x100000001B3 + i) mod p, canonical form. */
 zc_status zc_fill_uniform(zc_field field, uint32_t* out, int64_t n, uint64_t seed, void* stream);

@@ -114,7 +114,10 @@ def test_merkle_column_major_and_open(orc, perms, L, w):
 @pytest.mark.parametrize("log_k,log_b,batch", [(0, 1, 2), (1, 1, 1), (3, 2, 3), (6, 3, 2),
                                                (10, 2, 2), (12, 1, 1), (12, 2, 2), (12, 3, 1),
                                                (13, 1, 2), (14, 2, 1), (16, 1, 1), (17, 3, 1),
-                                               (20, 1, 1)])
+                                               (20, 1, 1),
+                                               # the wide (radix-2^5, 2^15-word tile) variant:
+                                               # >= two tiles per SM
+                                               (18, 1, 40), (15, 3, 80)])
 def test_rs_encode(orc, field, log_k, log_b, batch):
     from zorch_gb300.coding import rs_encode
     from zorch_gb300.field import field_of
@@ -415,3 +418,20 @@ def test_to_mont_reads_pinned_host_memory(orc):
     assert torch.equal(got, to_mont(BABYBEAR, host.cuda()))
     with pytest.raises(ValueError):
         to_mont_from_host(BABYBEAR, host)
+
+
+def test_copy_rows_gathers_strided_rows():
+    """copy_rows (zc_copy_rows, one 2D copy-engine transfer) gathers every
+    tree's root row out of a stack of digest layers, as the batched commits
+    use it, and refuses rows that are not contiguous."""
+    from zorch_gb300.field import copy_rows
+
+    layers = torch.arange(5 * 7 * 8, dtype=torch.int32, device="cuda").reshape(5, 7, 8)
+    out = torch.full((5, 8), -1, dtype=torch.int32, device="cuda")
+    copy_rows(out, layers[:, -1, :])
+    assert torch.equal(out, layers[:, -1, :])
+    one = torch.empty((1, 8), dtype=torch.int32, device="cuda")
+    copy_rows(one, layers[2:3, 3, :])
+    assert torch.equal(one, layers[2:3, 3, :])
+    with pytest.raises(ValueError):
+        copy_rows(torch.empty((8, 5), dtype=torch.int32, device="cuda"), layers[:, -1, :].t())

@@ -135,7 +135,8 @@ def test_bitrev_fold_matches_sp1_dump(orc, golden, i):
 
 @pytest.mark.parametrize("field", [0, 1])
 @pytest.mark.parametrize("log_k,log_b,batch", [(0, 1, 2), (3, 2, 3), (10, 2, 2), (12, 2, 2),
-                                               (13, 1, 2), (14, 2, 1), (16, 3, 1), (21, 2, 1)])
+                                               (13, 1, 2), (14, 2, 1), (16, 3, 1), (21, 2, 1),
+                                               (17, 2, 40)])  # the wide LDE variant
 def test_bitrev_encode_matches_oracle(orc, field, log_k, log_b, batch):
     from zorch_gb300.coding import rs_encode
     from zorch_gb300.field import field_of

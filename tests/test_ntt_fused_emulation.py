@@ -96,9 +96,11 @@ def pass1(x, z, c, s, tile, lk1, lk2, lb, lti, h, max_r, writes):
                 assert None not in v
             dif_group(v, tw, off, ls, lk2 - 1 - h0, r_)
             if last:
-                assert ls == 0
+                assert ls == 0 and base % (1 << r_) == 0
+                zp = zd + d + (brev(base, lk2) << lk1)
                 for j in range(1 << r_):
-                    pos = zd + d + (brev(base + j, lk2) << lk1)
+                    pos = zp + (brev(j, r_) << (lk1 + lk2 - r_))
+                    assert pos == zd + d + (brev(base + j, lk2) << lk1)
                     z[pos] = v[j]
                     writes[pos] = writes.get(pos, 0) + 1
             else:
@@ -142,8 +144,8 @@ def pass2(z, out, c, tile, lk1, lk2, lb, ltt, max_r, brev_out, writes):
                         for j in range(g_):
                             if brev_out:
                                 put(oc + (brev(s, lb) << lk) + (brev(t, lk2) << lk1) + j, v[j])
-                            else:
-                                put(oc + (t << lb) + s + (brev(j, lk1) << (lk2 + lb)), v[j])
+                            else:  # a single pass: r_ == lk1
+                                put(oc + (t << lb) + s + (brev(j, r_) << (lk2 + lb)), v[j])
                     else:
                         ar = ((dt << lb) + s) * rs + pad(off)
                         for j in range(g_):
@@ -158,11 +160,15 @@ def pass2(z, out, c, tile, lk1, lk2, lb, ltt, max_r, brev_out, writes):
                 assert None not in v
                 dif_group(v, tw, 0, 0, lk1 - 1 - h0, r_)
                 t = t2_0 + dt
+                sh = lk2 + lb
+                ob = oc + (t << lb) + s + (brev(base, lk1) << sh)
                 for j in range(g_):
                     if brev_out:
                         put(oc + (brev(s, lb) << lk) + (brev(t, lk2) << lk1) + base + j, v[j])
                     else:
-                        put(oc + (t << lb) + s + (brev(base + j, lk1) << (lk2 + lb)), v[j])
+                        pos = ob + (brev(j, r_) << (lk1 - r_ + sh))
+                        assert pos == oc + (t << lb) + s + (brev(base + j, lk1) << sh)
+                        put(pos, v[j])
         else:  # dif_pass over all rows
             ls = h0 - r_ + 1
             for gi in range(1 << (lrows + lk1 - r_)):
@@ -185,6 +191,10 @@ SHAPES = [
     (7, 6, 1, 4, 3, 3, False),   # first, middle and last passes
     (6, 6, 2, 3, 2, 4, True),    # bit-reversed output
     (7, 6, 1, 4, 3, 3, True),
+    (5, 5, 2, 3, 1, 5, False),   # radix-2^5 (the wide variant): single-pass rows
+    (7, 6, 1, 4, 3, 5, False),   # radix-2^5: 4 + 3 and 3 + 3 passes
+    (9, 5, 1, 2, 1, 5, False),   # radix-2^5: 5 (pass 1) and 5 + 4 (pass 2)
+    (5, 9, 1, 3, 1, 5, True),    # radix-2^5: 5 + 4 (pass 1) and 5, bit-reversed output
 ]
 
 

@@ -103,6 +103,7 @@ def _declare(lib: C.CDLL) -> None:
         "zc_rlc_columns": (st, [st, vp, i64, i32, vp, vp, vp]),
         "zc_fill_uniform": (st, [st, vp, i64, C.c_uint64, vp]),
         "zc_fill_u32": (st, [vp, i64, u32, vp]),
+        "zc_copy_rows": (st, [vp, i64, vp, i64, i64, i64, vp]),
         "zc_rs_encode_batch_workspace_bytes": (sz, [vp, i32]),
         "zc_rs_encode_batch": (st, [st, vp, i32, u32, vp, sz, vp]),
         "zc_merkle_commit_batch": (st, [vp, vp, i32, vp, sz, vp]),

@@ -25,7 +25,7 @@ import torch
 
 from . import _lib
 from .commit import DigestLayers, Poseidon2
-from .field import BABYBEAR, field_of, ptr, stream_handle
+from .field import BABYBEAR, copy_rows, field_of, ptr, stream_handle
 
 _TILE_CANDIDATES = (13, 14, 15)
 _RADIX_CANDIDATES = (3, 4)
@@ -282,7 +282,8 @@ class BatchCommitter:
         flats = self.pair_trees([cws[i] for i in whole]) if whole else []
         out: list[CommittedPolys | None] = [None] * len(jobs)
         for i, fl in zip(whole, flats):
-            out[i] = CommittedPolys(cws[i], fl[:, -1, :].contiguous(), fl if keep[i] else None)
+            roots = torch.empty((fl.shape[0], 8), dtype=torch.int32, device=fl.device)
+            out[i] = CommittedPolys(cws[i], copy_rows(roots, fl[:, -1, :]), fl if keep[i] else None)
         for i, cw in enumerate(cws):
             if out[i] is not None:
                 continue
@@ -293,7 +294,7 @@ class BatchCommitter:
             for c0 in range(0, w, per):
                 cnt = min(per, w - c0)
                 self.pair_trees([cw[c0:c0 + cnt]], flats=[buf[:cnt]])
-                roots[c0:c0 + cnt].copy_(buf[:cnt, -1, :])
+                copy_rows(roots[c0:c0 + cnt], buf[:cnt, -1, :])
             out[i] = CommittedPolys(cw, roots, None)
         return out
 

@@ -40,10 +40,13 @@ constexpr int kItemsPerCta = ZC_ITEMS_PER_CTA;
 
 // Grid of a work-list launch over `total` items: every item is claimed (grid *
 // items per CTA >= total), never more CTAs than items; resident CTAs only
-// (occ per SM) when CTAs do not retire.
+// (occ per SM) when CTAs do not retire. A list shorter than kItemsPerCta
+// resident waves gets one CTA per item up to a full wave, so that a small
+// batch still spreads over every SM.
 inline int64_t batch_grid(int64_t total, int occ, int sms) {
-  int64_t grid = kItemsPerCta > 0 ? (total + kItemsPerCta - 1) / kItemsPerCta
-                                  : (int64_t)(occ > 0 ? occ : 1) * sms;
+  const int64_t wave = (int64_t)(occ > 0 ? occ : 1) * sms;
+  int64_t grid = kItemsPerCta > 0 ? (total + kItemsPerCta - 1) / kItemsPerCta : wave;
+  if (kItemsPerCta > 0 && grid < wave) grid = total < wave ? total : wave;
   if (grid > total) grid = total;
   return grid < 0x7fffffff ? grid : 0x7fffffff;
 }

@@ -3,13 +3,15 @@
 // the tree driver, and the transcript hop run by a tree's root launch.
 //
 // Large trees: one thread per leaf (k_leaf, no barriers, full occupancy) writes
-// the leaf digests; each level wider than kLevelWiseMin nodes is one launch of
-// one thread per parent. The small top of a tree, and whole small trees, run
-// as fused CTA subtrees (k_subtree): the first level by one thread per leaf
-// (or a half-warp per parent), every level above by half-warps out of shared
-// memory, writing every level (the tree keeps all layers for openings,
-// zorch/commit/merkle.py:187-202) without reading a level back.
+// the leaf digests; each level wider than tree_shape().levelwise_min nodes is
+// one launch of one thread per parent. The small top of a tree, and whole
+// small trees, run as fused CTA subtrees (k_subtree): the first level by one
+// thread per leaf (or a quarter-warp per parent), every level above by
+// quarter- or half-warps out of shared memory, writing every level (the tree
+// keeps all layers for openings, zorch/commit/merkle.py:187-202) without
+// reading a level back.
 #pragma once
+#include <stdlib.h>
 #include <string.h>
 
 #include <type_traits>
@@ -227,22 +229,41 @@ struct FoldLeaf {
 };
 
 // Nodes per tree-top CTA of the batched commit (k_tree_top) at its first
-// level; its threads: 8 per node, so each level above is one round of
-// half-warp permutations.
+// level; its threads: 4 per node, so each level above is one round of
+// quarter-warp permutations.
 constexpr int kSubT = 128;
-// Nodes per fused-subtree CTA (k_subtree) at its first level, and its
-// threads: 8 per node up to 1024 (64 half-warps), at least a warp. 128
-// measured fastest on the GB300 (config 3's FRI commit phase: 6.21 ms graphed
-// at 128 against 6.37-6.72 ms at 256 with the level-wise threshold at
-// 2^14..2^16; the trace hash within 1 %).
-#ifndef ZC_SUBTREE_T
-#define ZC_SUBTREE_T 128
-#endif
-constexpr int kSubMaxT = ZC_SUBTREE_T;
-static_assert(kSubMaxT >= 2 && kSubMaxT <= 256 && (kSubMaxT & (kSubMaxT - 1)) == 0,
-              "subtree width must be a power of two in [2, 256]");
+// Largest number of nodes per fused-subtree CTA (k_subtree) at its first
+// level; its threads: 4 per node (a quarter-warp permutation per parent), at
+// least a warp.
+constexpr int kSubCap = 256;
+
+// The tree driver's shape: levels with more than `levelwise_min` nodes run one
+// thread per node; the top runs as fused subtrees of `subtree_t` first-level
+// nodes per CTA. Defaults 2^13 and 128; the environment variables
+// ZC_LEVELWISE_MIN_LOG (8..20) and ZC_SUBTREE_T (a power of two in 2..256)
+// override them for tuning (read once; no byte of any result depends on them).
+struct TreeShape {
+  int64_t levelwise_min;
+  int subtree_t;
+};
+inline const TreeShape& tree_shape() {
+  static const TreeShape shape = [] {
+    TreeShape t{(int64_t)1 << 13, 128};
+    if (const char* e = getenv("ZC_LEVELWISE_MIN_LOG")) {
+      const int v = atoi(e);
+      if (v >= 8 && v <= 20) t.levelwise_min = (int64_t)1 << v;
+    }
+    if (const char* e = getenv("ZC_SUBTREE_T")) {
+      const int v = atoi(e);
+      if (v >= 2 && v <= kSubCap && (v & (v - 1)) == 0) t.subtree_t = v;
+    }
+    return t;
+  }();
+  return shape;
+}
+
 inline int subtree_threads(int T) {
-  const int t = 8 * T > 32 ? 8 * T : 32;
+  const int t = 4 * T > 32 ? 4 * T : 32;
   return t < 1024 ? t : 1024;
 }
 
@@ -253,65 +274,74 @@ __device__ __forceinline__ uint32_t half_perm(uint32_t x, const P2Params* hp) {
 }
 
 // One level of a subtree: parent i (< width) = compress(children 2i, 2i+1)
-// read from the [word][node] slots `src` (row stride `stride`), written to the
-// `dst` slots and to the tree's level at `lay`. Half-warp h takes nodes
-// h, h + H, ... (H halves); a warp with no node in a round skips it (a
-// warp-uniform branch: the shuffles need every lane of a running warp).
+// read from the digest slots `src` ([node][8 words], 16-byte aligned),
+// written to the `dst` slots and to the tree's level at `lay`. A level with
+// more parents than the CTA has half-warps runs on quarter-warps (one round of
+// up to blockDim/4 parents; a quarter's permutation costs ~2.3x fewer thread
+// instructions, which is what counts when every warp is busy); a narrower
+// level runs on half-warps, whose permutation has the shorter dependency
+// chain (each lane issues a quarter of the instructions), which is what
+// counts when the level is a latency chain. Parents are taken round-robin by
+// quarter (half) g = g, g + Q, ...; a warp with no parent in a round skips it
+// (a warp-uniform branch: the shuffles need every lane of a running warp).
 template <class F>
-__device__ __forceinline__ void subtree_level(const uint32_t* src, uint32_t* dst, int stride,
-                                              uint32_t* lay, int width, const P2Params* hp) {
-  const int t = threadIdx.x, l = t & 15, H = blockDim.x >> 4;
-  const int child_off = l >> 3, word = l & 7;
-  for (int r = 0; r < width; r += H) {
-    if (r + 2 * (t >> 5) >= width) continue;
-    const int node = r + (t >> 4);
-    const bool on = node < width;
-    uint32_t x = on ? src[word * stride + 2 * node + child_off] : 0u;
-    x = half_perm<F>(x, hp);
-    if (on && l < 8) {
-      lay[8 * node + l] = x;
-      dst[l * stride + node] = x;
+__device__ __forceinline__ void subtree_level(const uint32_t* src, uint32_t* dst, uint32_t* lay,
+                                              int width, const P2Params* hp) {
+  const int t = threadIdx.x;
+  if (width > (int)(blockDim.x >> 4)) {  // quarter-warps: lane q holds words 4q .. 4q+3
+    const int q = t & 3, Q = blockDim.x >> 2;
+    for (int r = 0; r < width; r += Q) {
+      if (r + 8 * (t >> 5) >= width) continue;
+      const int node = r + (t >> 2);
+      const bool on = node < width;
+      uint4 v = on ? reinterpret_cast<const uint4*>(src)[4 * node + q] : make_uint4(0, 0, 0, 0);
+      uint32_t x[4] = {v.x, v.y, v.z, v.w};
+      p2_permute_quarter<F>(x, hp);
+      if (on && q < 2) {
+        const uint4 o = make_uint4(x[0], x[1], x[2], x[3]);
+        reinterpret_cast<uint4*>(lay)[2 * node + q] = o;
+        reinterpret_cast<uint4*>(dst)[2 * node + q] = o;
+      }
     }
+    return;
+  }
+  // half-warps (one round: width <= blockDim/16): lane l holds word l
+  const int l = t & 15, node = t >> 4;
+  if (2 * (t >> 5) >= width) return;
+  const bool on = node < width;
+  uint32_t x = on ? src[16 * node + l] : 0u;
+  x = half_perm<F>(x, hp);
+  if (on && l < 8) {
+    lay[8 * node + l] = x;
+    dst[8 * node + l] = x;
   }
 }
 
 // One subtree of T first-level nodes per CTA (blockDim = subtree_threads(T)):
-// the first level is T leaf digests (one thread each; for NodeLeaf, half-warps
-// compressing stored children), then every level up to the subtree root is
-// compressed by half-warps out of ping-pong shared-memory slots, each level
-// written to `layers`.
+// the first level is T leaf digests (one thread each; for NodeLeaf,
+// quarter-warps compressing stored children), then every level up to the
+// subtree root is compressed out of ping-pong shared-memory slots
+// (subtree_level), each level written to `layers`.
 template <class K, class Leaf>
 __global__ void __launch_bounds__(1024) k_subtree(Leaf leaf, uint32_t* layers, int64_t L,
                                                        int l0, int T, const P2Params* rt,
                                                        RootHop hop) {
   using F = typename K::F;
   __shared__ P2Params s_rt;
-  __shared__ uint32_t sm[2][8 * kSubMaxT];  // [word][node] digest slots
+  __shared__ __align__(16) uint32_t sm[2][8 * kSubCap];  // [node][word] digest slots
   K k = KIn<K>::make(rt, &s_rt);
   const P2Params* hp = KIn<K>::half(rt, &s_rt);
   const int t = threadIdx.x;
   const int64_t base = (int64_t)blockIdx.x * T;
   uint32_t* lay0 = layers + 8 * (level_offset(L, l0) + base);
   if constexpr (std::is_same<Leaf, NodeLeaf>::value) {
-    const int l = t & 15, H = blockDim.x >> 4;
-    for (int r = 0; r < T; r += H) {
-      if (r + 2 * (t >> 5) >= T) continue;
-      const int node = r + (t >> 4);
-      const bool on = node < T;
-      uint32_t x = on ? leaf.in[16 * (base + node) + l] : 0u;
-      x = half_perm<F>(x, hp);
-      if (on && l < 8) {
-        lay0[8 * node + l] = x;
-        sm[0][l * kSubMaxT + node] = x;
-      }
-    }
+    subtree_level<F>(leaf.in + 16 * base, sm[0], lay0, T, hp);
   } else {
     if (t < T) {
       uint32_t d[8];
       leaf.digest(base + t, d, k);
       store_digest(lay0 + 8 * t, d);
-#pragma unroll
-      for (int i = 0; i < 8; i++) sm[0][i * kSubMaxT + t] = d[i];
+      store_digest(sm[0] + 8 * t, d);
     }
   }
   int cur = 0, lvl = l0, width = T;
@@ -319,7 +349,7 @@ __global__ void __launch_bounds__(1024) k_subtree(Leaf leaf, uint32_t* layers, i
     __syncthreads();
     width >>= 1;
     lvl++;
-    subtree_level<F>(sm[cur], sm[cur ^ 1], kSubMaxT,
+    subtree_level<F>(sm[cur], sm[cur ^ 1],
                      layers + 8 * (level_offset(L, lvl) + (int64_t)blockIdx.x * width), width, hp);
     cur ^= 1;
   }
@@ -328,7 +358,7 @@ __global__ void __launch_bounds__(1024) k_subtree(Leaf leaf, uint32_t* layers, i
     if (threadIdx.x < 32) {
       uint32_t root[8];
 #pragma unroll
-      for (int i = 0; i < 8; i++) root[i] = sm[cur][i * kSubMaxT];
+      for (int i = 0; i < 8; i++) root[i] = sm[cur][i];
       root_hop<F>(hop, root, hp);
     }
   }
@@ -363,33 +393,28 @@ __global__ void __launch_bounds__(kMaxT, HashOcc<K>::v) k_leaf(Leaf leaf, uint32
   store_digest(out + 8 * p, d);
 }
 
-// Levels with more than this many nodes run one thread per node (k_leaf with
-// NodeLeaf, throughput-bound: a level this wide fills the GPU); the narrower
-// top of the tree is latency-bound and runs as fused CTA subtrees of
-// half-warp permutations (k_subtree with NodeLeaf), log2(T)+1 levels per
-// launch. 2^13 measured fastest (see ZC_SUBTREE_T).
-#ifndef ZC_LEVELWISE_MIN_LOG
-#define ZC_LEVELWISE_MIN_LOG 13
-#endif
-constexpr int64_t kLevelWiseMin = (int64_t)1 << ZC_LEVELWISE_MIN_LOG;
-
+// Levels with more than tree_shape().levelwise_min nodes run one thread per
+// node (k_leaf with NodeLeaf, throughput-bound: a level this wide fills the
+// GPU); the narrower top of the tree is latency-bound and runs as fused CTA
+// subtrees (k_subtree with NodeLeaf), log2(T)+1 levels per launch.
 // Launches the levels above `l_done` (all levels <= l_done already stored).
 template <class K>
 zc_status finish_tree(uint32_t* layers, int64_t L, int l_done, const P2Params* rt,
                       cudaStream_t st, RootHop hop = RootHop{nullptr, nullptr, 0}) {
   const int depth = ilog2(L);
+  const int sub_t = tree_shape().subtree_t;
   int l = l_done;
   while (l < depth) {
     const int64_t parents = (L >> l) >> 1;
     NodeLeaf nl{layers + 8 * level_offset(L, l)};
-    if (parents > kLevelWiseMin) {
+    if (parents > tree_shape().levelwise_min) {
       k_leaf<K, NodeLeaf><<<(unsigned)((parents + kMaxT - 1) / kMaxT), kMaxT, 0, st>>>(
           nl, layers + 8 * level_offset(L, l + 1), parents, rt);
       ZC_TRY(launch_check());
       l += 1;
       continue;
     }
-    const int T = parents < kSubMaxT ? (int)parents : kSubMaxT;
+    const int T = parents < sub_t ? (int)parents : sub_t;
     const bool top = parents == T;  // this launch's single CTA makes the root
     k_subtree<K, NodeLeaf><<<(unsigned)(parents / T), subtree_threads(T), 0, st>>>(
         nl, layers, L, l + 1, T, rt, top ? hop : RootHop{nullptr, nullptr, 0});
@@ -402,12 +427,13 @@ zc_status finish_tree(uint32_t* layers, int64_t L, int l_done, const P2Params* r
 template <class K, class Leaf>
 zc_status commit_tree(const Leaf& leaf, uint32_t* layers, int64_t L, const P2Params* rt,
                       cudaStream_t st, RootHop hop = RootHop{nullptr, nullptr, 0}) {
-  if (L > kLevelWiseMin) {
+  if (L > tree_shape().levelwise_min) {
     k_leaf<K, Leaf><<<(unsigned)((L + kMaxT - 1) / kMaxT), kMaxT, 0, st>>>(leaf, layers, L, rt);
     ZC_TRY(launch_check());
     return finish_tree<K>(layers, L, 0, rt, st, hop);
   }
-  const int T0 = L < kSubMaxT ? (int)L : kSubMaxT;
+  const int sub_t = tree_shape().subtree_t;
+  const int T0 = L < sub_t ? (int)L : sub_t;
   const bool top = L == T0;
   k_subtree<K, Leaf><<<(unsigned)(L / T0), subtree_threads(T0), 0, st>>>(
       leaf, layers, L, 0, T0, rt, top ? hop : RootHop{nullptr, nullptr, 0});

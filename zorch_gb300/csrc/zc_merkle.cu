@@ -143,15 +143,15 @@ __global__ void __launch_bounds__(kMaxT) k_tree_batch(const __grid_constant__ Tr
 }
 
 // One CTA per tree: level `top` (<= 256 nodes, already stored) to the root,
-// each level compressed by half-warps (64 halves: the first level of up to 128
-// parents takes up to two rounds, every later level one).
+// each level compressed in one round (subtree_level: quarter-warps for the
+// levels wider than 32 parents, half-warps above).
 template <class K>
-__global__ void __launch_bounds__(8 * kSubT) k_tree_top(const __grid_constant__ TreeBatch B,
+__global__ void __launch_bounds__(4 * kSubT) k_tree_top(const __grid_constant__ TreeBatch B,
                                                        const P2Params* rt) {
   using F = typename K::F;
-  constexpr int S = 2 * kSubT;  // slot stride: up to 256 nodes
+  constexpr int S = 2 * kSubT;  // up to 256 nodes
   __shared__ P2Params s_rt;
-  __shared__ uint32_t sm[2][8 * S];
+  __shared__ __align__(16) uint32_t sm[2][8 * S];  // [node][word] digest slots
   KIn<K>::make(rt, &s_rt);
   const P2Params* hp = KIn<K>::half(rt, &s_rt);
   const int j = find_tree(B.tree_prefix, B.njobs, (int64_t)blockIdx.x);
@@ -159,14 +159,14 @@ __global__ void __launch_bounds__(8 * kSubT) k_tree_top(const __grid_constant__ 
   uint32_t* lay = J.layers + ((int64_t)blockIdx.x - B.tree_prefix[j]) * J.lstride;
   int lvl = J.top;
   int width = (int)(J.L >> lvl);
-  const uint32_t* src = lay + 8 * level_offset(J.L, lvl);
-  for (int i = threadIdx.x; i < width * 8; i += blockDim.x) sm[0][(i & 7) * S + (i >> 3)] = src[i];
+  const uint4* src = reinterpret_cast<const uint4*>(lay + 8 * level_offset(J.L, lvl));
+  for (int i = threadIdx.x; i < width * 2; i += blockDim.x) reinterpret_cast<uint4*>(sm[0])[i] = src[i];
   int cur = 0;
   while (width > 1) {
     __syncthreads();
     width >>= 1;
     lvl++;
-    subtree_level<F>(sm[cur], sm[cur ^ 1], S, lay + 8 * level_offset(J.L, lvl), width, hp);
+    subtree_level<F>(sm[cur], sm[cur ^ 1], lay + 8 * level_offset(J.L, lvl), width, hp);
     cur ^= 1;
   }
 }
@@ -223,7 +223,7 @@ zc_status tree_batch_wave(const zc_merkle_job* jobs, int n, unsigned long long* 
     ZC_TRY(launch_check());
   }
   if (trees > 0x7fffffff) return ZC_BAD_SHAPE;
-  k_tree_top<K><<<(unsigned)trees, 8 * kSubT, 0, st>>>(B, rt);
+  k_tree_top<K><<<(unsigned)trees, 4 * kSubT, 0, st>>>(B, rt);
   return launch_check();
 }
 
@@ -457,6 +457,19 @@ zc_status zc_fill_u32(uint32_t* out, int64_t n, uint32_t value, void* stream) {
   if (blocks > 152 * 16) blocks = 152 * 16;
   k_fill_u32<<<(unsigned)blocks, 256, 0, (cudaStream_t)stream>>>(out, n, value);
   return launch_check();
+}
+
+zc_status zc_copy_rows(void* dst, int64_t dst_pitch, const void* src, int64_t src_pitch,
+                       int64_t row_bytes, int64_t rows, void* stream) {
+  if (rows < 0 || row_bytes < 0 || dst_pitch < row_bytes || src_pitch < row_bytes) {
+    set_error("copy_rows: pitches must be >= the row size, sizes >= 0");
+    return ZC_BAD_ARG;
+  }
+  if (rows == 0 || row_bytes == 0) return ZC_OK;
+  if (!dst || !src) return ZC_BAD_ARG;
+  ZC_CUDA(cudaMemcpy2DAsync(dst, (size_t)dst_pitch, src, (size_t)src_pitch, (size_t)row_bytes,
+                            (size_t)rows, cudaMemcpyDeviceToDevice, (cudaStream_t)stream));
+  return ZC_OK;
 }
 
 zc_status zc_fill_uniform(zc_field field, uint32_t* out, int64_t n, uint64_t seed, void* stream) {

@@ -76,6 +76,13 @@ __device__ __forceinline__ int pad(int i) { return i + (i >> 5); }
 __device__ __forceinline__ int brev(int i, int bits) {
   return bits ? (int)(__brev((unsigned)i) >> (32 - bits)) : 0;
 }
+// brev(j, R) for a j known at compile time once a member loop is unrolled.
+template <int R>
+__host__ __device__ constexpr int brev_r(int j) {
+  int r = 0;
+  for (int b = 0; b < R; b++) r |= ((j >> b) & 1) << (R - 1 - b);
+  return r;
+}
 __host__ __device__ __forceinline__ int padded(int m) { return m + (m >> 5); }
 // Row stride of a tile of rows of m words: padded, then odd, so that threads
 // of a warp reading the same position of consecutive rows hit distinct banks.
@@ -169,6 +176,13 @@ __device__ __forceinline__ void dif_pass(uint32_t* a, int log_rows, int logm, in
 // Largest radix-2^R register pass by default (radix-2^5 passes spill under
 // the 64-register cap the two-CTA occupancy needs).
 constexpr int kMaxRadixLog = 4;
+// The wide four-step variant (k_lde_pass1/2 with MR = 5): radix-2^5 register
+// passes -- two passes for a 2^10 row instead of three, so one shared-memory
+// round trip and one barrier fewer per four-step pass -- need 128 registers,
+// hence one 512-thread CTA per SM, fed by 2^15-word (128 KB) tiles so that
+// enough loads stay in flight. Used for large transforms (lde_launch).
+constexpr int kWideRadixLog = 5;
+constexpr int kWideTileLog = 15;
 
 // max_r (2..4) bounds the passes' radix: ceil(logm / max_r) balanced passes.
 template <class F>
@@ -373,9 +387,12 @@ __device__ __forceinline__ void p1_pass(uint32_t* work, int rs, int log_ti, int 
       for (int j = 0; j < G; j++) v[j] = ar[pad(j << lS)];
     }
     dif_group<F, R>(v, tw, off, lS, sh0);
-    if (last) {  // lS == 0: members are the positions base + j
+    if (last) {  // lS == 0: members are the positions base + j, base = blk 2^R, so
+                 // brev(base + j) = brev(base) + brev_R(j) 2^(log_k2 - R)
+      uint32_t* zp = zd + d + ((uint32_t)brev(base, log_k2) << log_k1);
+      const int so = log_k1 + log_k2 - R;
 #pragma unroll
-      for (int j = 0; j < G; j++) zd[d + ((uint32_t)brev(base + j, log_k2) << log_k1)] = v[j];
+      for (int j = 0; j < G; j++) zp[(uint32_t)brev_r<R>(j) << so] = v[j];
     } else {
 #pragma unroll
       for (int j = 0; j < G; j++) ar[pad(j << lS)] = v[j];
@@ -384,8 +401,9 @@ __device__ __forceinline__ void p1_pass(uint32_t* work, int rs, int log_ti, int 
 }
 
 // Pass-1 item with fused load and store. Layout: work[TI][rs] | tw[k2/2] |
-// gi[TI] | Gt[S] (S = the first pass's member stride).
-template <class F>
+// gi[TI] | Gt[S] (S = the first pass's member stride). MR: the largest radix
+// compiled in (max_r <= MR).
+template <class F, int MR = kMaxRadixLog>
 __device__ void lde_pass1_fused(const uint32_t* x, uint32_t* z, int log_k1, int log_k2, int log_b,
                                 int log_ti, uint32_t h, int s, int tile, int64_t c, uint32_t* sm,
                                 int max_r) {
@@ -413,6 +431,7 @@ __device__ void lde_pass1_fused(const uint32_t* x, uint32_t* z, int log_k1, int 
     const int R = pass_radix(h0, passes, q);
     const bool first = q == 0, last = q == passes - 1;
     switch (R) {
+      case 5: if constexpr (MR >= 5) p1_pass<F, 5>(work, rs, log_ti, log_k1, log_k2, h0, first, last, xs, gi, Gt, GS, tw, zd); break;
       case 4: p1_pass<F, 4>(work, rs, log_ti, log_k1, log_k2, h0, first, last, xs, gi, Gt, GS, tw, zd); break;
       case 3: p1_pass<F, 3>(work, rs, log_ti, log_k1, log_k2, h0, first, last, xs, gi, Gt, GS, tw, zd); break;
       case 2: p1_pass<F, 2>(work, rs, log_ti, log_k1, log_k2, h0, first, last, xs, gi, Gt, GS, tw, zd); break;
@@ -459,7 +478,7 @@ __device__ __forceinline__ void p2_first(uint32_t* work, int rs, int log_b, int 
           if (brev_out)
             oc[((int64_t)brev(s, log_b) << log_k) + ((int64_t)brev((int)t, log_k2) << log_k1) + j] = v[j];
           else
-            oc[((int64_t)t << log_b) + s + ((int64_t)brev(j, log_k1) << (log_k2 + log_b))] = v[j];
+            oc[((int64_t)t << log_b) + s + ((int64_t)brev_r<R>(j) << (log_k2 + log_b))] = v[j];  // R == log_k1
         }
       } else {
         uint32_t* ar = work + ((dt << log_b) + s) * rs + pad(off);
@@ -498,16 +517,18 @@ __device__ __forceinline__ void p2_last(uint32_t* work, int rs, int log_b, int l
 #pragma unroll
       for (int j = 0; j < G; j++) orow[j] = v[j];
     } else {
-      uint32_t* ob = oc + ((int64_t)t << log_b) + s;
+      // base = g 2^R: brev(base + j) = brev(base) + brev_R(j) 2^(log_k1 - R)
       const int sh = log_k2 + log_b;
+      uint32_t* ob = oc + ((int64_t)t << log_b) + s + ((int64_t)brev(base, log_k1) << sh);
+      const int so = log_k1 - R + sh;
 #pragma unroll
-      for (int j = 0; j < G; j++) ob[(int64_t)brev(base + j, log_k1) << sh] = v[j];
+      for (int j = 0; j < G; j++) ob[(uint32_t)brev_r<R>(j) << so] = v[j];  // < n <= 2^30
     }
   }
 }
 
 // Pass-2 item with fused load and store. Layout: work[b*TT][rs] | tw[k1/2].
-template <class F>
+template <class F, int MR = kMaxRadixLog>
 __device__ void lde_pass2_fused(const uint32_t* z, uint32_t* out, int log_k1, int log_k2,
                                 int log_b, int log_tt, int tile, int64_t c, uint32_t* sm,
                                 int brev_out, int max_r) {
@@ -529,6 +550,7 @@ __device__ void lde_pass2_fused(const uint32_t* z, uint32_t* out, int log_k1, in
     const bool first = q == 0, last = q == passes - 1;
     if (first) {
       switch (R) {
+        case 5: if constexpr (MR >= 5) p2_first<F, 5>(work, rs, log_b, log_tt, log_k1, log_k, t2_0, zc_, tw, last, oc, log_k2, brev_out); break;
         case 4: p2_first<F, 4>(work, rs, log_b, log_tt, log_k1, log_k, t2_0, zc_, tw, last, oc, log_k2, brev_out); break;
         case 3: p2_first<F, 3>(work, rs, log_b, log_tt, log_k1, log_k, t2_0, zc_, tw, last, oc, log_k2, brev_out); break;
         case 2: p2_first<F, 2>(work, rs, log_b, log_tt, log_k1, log_k, t2_0, zc_, tw, last, oc, log_k2, brev_out); break;
@@ -536,6 +558,7 @@ __device__ void lde_pass2_fused(const uint32_t* z, uint32_t* out, int log_k1, in
       }
     } else if (last) {
       switch (R) {
+        case 5: if constexpr (MR >= 5) p2_last<F, 5>(work, rs, log_b, log_tt, log_k1, log_k2, log_k, t2_0, h0, tw, oc, brev_out); break;
         case 4: p2_last<F, 4>(work, rs, log_b, log_tt, log_k1, log_k2, log_k, t2_0, h0, tw, oc, brev_out); break;
         case 3: p2_last<F, 3>(work, rs, log_b, log_tt, log_k1, log_k2, log_k, t2_0, h0, tw, oc, brev_out); break;
         case 2: p2_last<F, 2>(work, rs, log_b, log_tt, log_k1, log_k2, log_k, t2_0, h0, tw, oc, brev_out); break;
@@ -543,6 +566,7 @@ __device__ void lde_pass2_fused(const uint32_t* z, uint32_t* out, int log_k1, in
       }
     } else {
       switch (R) {
+        case 5: if constexpr (MR >= 5) dif_pass<F, 5>(work, log_rows, log_k1, rs, tw, h0); break;
         case 4: dif_pass<F, 4>(work, log_rows, log_k1, rs, tw, h0); break;
         case 3: dif_pass<F, 3>(work, log_rows, log_k1, rs, tw, h0); break;
         case 2: dif_pass<F, 2>(work, log_rows, log_k1, rs, tw, h0); break;
@@ -554,14 +578,14 @@ __device__ void lde_pass2_fused(const uint32_t* z, uint32_t* out, int log_k1, in
   }
 }
 
-template <class F>
-__global__ void __launch_bounds__(kThreads, 2) k_lde_pass1(const uint32_t* x, uint32_t* z, int log_k1,
+template <class F, int MR = kMaxRadixLog>
+__global__ void __launch_bounds__(kThreads, MR > 4 ? 1 : 2) k_lde_pass1(const uint32_t* x, uint32_t* z, int log_k1,
                                                         int log_k2, int log_b, int log_ti,
                                                         uint32_t h) {
   extern __shared__ uint32_t sm[];
 #if ZC_LDE_FUSED
-  lde_pass1_fused<F>(x, z, log_k1, log_k2, log_b, log_ti, h, blockIdx.x, blockIdx.y, blockIdx.z,
-                     sm, kMaxRadixLog);
+  lde_pass1_fused<F, MR>(x, z, log_k1, log_k2, log_b, log_ti, h, blockIdx.x, blockIdx.y,
+                         blockIdx.z, sm, MR);
 #else
   lde_pass1_body<F>(x, z, log_k1, log_k2, log_b, log_ti, h, blockIdx.x, blockIdx.y, blockIdx.z,
                     sm);
@@ -647,14 +671,14 @@ __device__ void lde_pass2_body(const uint32_t* z, uint32_t* out, int log_k1, int
   }
 }
 
-template <class F>
-__global__ void __launch_bounds__(kThreads, 2) k_lde_pass2(const uint32_t* z, uint32_t* out,
+template <class F, int MR = kMaxRadixLog>
+__global__ void __launch_bounds__(kThreads, MR > 4 ? 1 : 2) k_lde_pass2(const uint32_t* z, uint32_t* out,
                                                         int log_k1, int log_k2, int log_b,
                                                         int log_tt, int brev_out) {
   extern __shared__ uint32_t sm[];
 #if ZC_LDE_FUSED
-  lde_pass2_fused<F>(z, out, log_k1, log_k2, log_b, log_tt, blockIdx.x, blockIdx.y, sm, brev_out,
-                     kMaxRadixLog);
+  lde_pass2_fused<F, MR>(z, out, log_k1, log_k2, log_b, log_tt, blockIdx.x, blockIdx.y, sm,
+                         brev_out, MR);
 #else
   lde_pass2_body<F>(z, out, log_k1, log_k2, log_b, log_tt, blockIdx.x, blockIdx.y, sm, brev_out);
 #endif
@@ -697,10 +721,43 @@ inline LdePlan plan_lde(int log_k, int log_b, int tile_log = 0, int max_r = kMax
   return p;
 }
 
+// Whether a four-step LDE of `batch` columns of 2^log_n outputs takes the
+// wide variant: at least two of its 2^15-word tiles per SM, so that one
+// resident CTA per SM still fills the GPU (2^20 x 64 at blowup 4: 2.10 ms
+// against 2.23 ms for the radix-2^4 form on the GB300).
+inline bool lde_wide(int64_t batch, int log_n) {
+#if ZC_LDE_FUSED
+  static const int sms = [] {
+    int dev = 0, n = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess ||
+        cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
+      n = 152;
+    return n;
+  }();
+  const int64_t tiles = log_n >= kWideTileLog ? batch << (log_n - kWideTileLog) : 0;
+  return tiles >= 2 * (int64_t)sms;
+#else
+  (void)batch;
+  (void)log_n;
+  return false;
+#endif
+}
+
+template <class F, int MR>
+zc_status lde_four_step(const uint32_t* x, int64_t batch, int log_k, int log_b, uint32_t h,
+                        uint32_t* out, void* ws, size_t ws_bytes, cudaStream_t st, int brev_out,
+                        const LdePlan& p);
+
 template <class F>
 zc_status lde_launch(const uint32_t* x, int64_t batch, int log_k, int log_b, uint32_t h,
                      uint32_t* out, void* ws, size_t ws_bytes, cudaStream_t st,
                      int brev_out = 0) {
+  if (!plan_lde(log_k, log_b).small && lde_wide(batch, log_k + log_b)) {
+    const LdePlan pw = plan_lde(log_k, log_b, kWideTileLog, kWideRadixLog);
+    if (pw.smem1 <= 227 * 1024 && pw.smem2 <= 227 * 1024)
+      return lde_four_step<F, kWideRadixLog>(x, batch, log_k, log_b, h, out, ws, ws_bytes, st,
+                                             brev_out, pw);
+  }
   const LdePlan p = plan_lde(log_k, log_b);
   const int log_n = log_k + log_b;
   const size_t smem_cap = 227 * 1024;
@@ -720,6 +777,16 @@ zc_status lde_launch(const uint32_t* x, int64_t batch, int log_k, int log_b, uin
     }
     return ZC_OK;
   }
+  return lde_four_step<F, kMaxRadixLog>(x, batch, log_k, log_b, h, out, ws, ws_bytes, st,
+                                        brev_out, p);
+}
+
+// The two four-step passes over column chunks that fit the workspace.
+template <class F, int MR>
+zc_status lde_four_step(const uint32_t* x, int64_t batch, int log_k, int log_b, uint32_t h,
+                        uint32_t* out, void* ws, size_t ws_bytes, cudaStream_t st, int brev_out,
+                        const LdePlan& p) {
+  const int log_n = log_k + log_b;
   const size_t col_bytes = (size_t)4 << log_n;
   if (!ws || ws_bytes < col_bytes) {
     set_error("rs_encode workspace smaller than one column's LDE (4 * 2^(log_k+log_b) bytes)");
@@ -729,20 +796,20 @@ zc_status lde_launch(const uint32_t* x, int64_t batch, int log_k, int log_b, uin
   int64_t chunk = (int64_t)(ws_bytes / col_bytes);
   if (chunk > 65535) chunk = 65535;
   if (chunk > batch) chunk = batch;
-  ZC_CUDA(cudaFuncSetAttribute(k_lde_pass1<F>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+  ZC_CUDA(cudaFuncSetAttribute(k_lde_pass1<F, MR>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                (int)p.smem1));
-  ZC_CUDA(cudaFuncSetAttribute(k_lde_pass2<F>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+  ZC_CUDA(cudaFuncSetAttribute(k_lde_pass2<F, MR>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                (int)p.smem2));
   uint32_t* z = (uint32_t*)ws;
   for (int64_t c0 = 0; c0 < batch; c0 += chunk) {
     const int64_t cols = batch - c0 < chunk ? batch - c0 : chunk;
     dim3 g1(1u << log_b, 1u << (p.log_k1 - p.log_ti), (unsigned)cols);
-    k_lde_pass1<F><<<g1, kThreads, p.smem1, st>>>(x + (c0 << log_k), z, p.log_k1, p.log_k2,
-                                                  log_b, p.log_ti, h);
+    k_lde_pass1<F, MR><<<g1, kThreads, p.smem1, st>>>(x + (c0 << log_k), z, p.log_k1, p.log_k2,
+                                                      log_b, p.log_ti, h);
     ZC_TRY(launch_check());
     dim3 g2(1u << (p.log_k2 - p.log_tt), (unsigned)cols);
-    k_lde_pass2<F><<<g2, kThreads, p.smem2, st>>>(z, out + (c0 << log_n), p.log_k1, p.log_k2,
-                                                  log_b, p.log_tt, brev_out);
+    k_lde_pass2<F, MR><<<g2, kThreads, p.smem2, st>>>(z, out + (c0 << log_n), p.log_k1,
+                                                      p.log_k2, log_b, p.log_tt, brev_out);
     ZC_TRY(launch_check());
   }
   return ZC_OK;

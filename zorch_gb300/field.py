@@ -154,6 +154,28 @@ def full_u32(shape, value: int = 0, device="cuda") -> torch.Tensor:
     return t
 
 
+def copy_rows(dst: torch.Tensor, src: torch.Tensor) -> torch.Tensor:
+    """dst[i] = src[i] for 2D device tensors whose rows are contiguous (inner
+    stride 1) but may sit at any row pitch -- e.g. every tree's root row out
+    of a stack of digest layers -- as one 2D copy-engine transfer on the
+    current stream (zc_copy_rows), not a framework gather kernel."""
+    if src.dim() != 2 or dst.shape != src.shape or dst.dtype != src.dtype:
+        raise ValueError(f"copy_rows: 2D tensors of one shape and dtype, got "
+                         f"{tuple(dst.shape)} {dst.dtype} and {tuple(src.shape)} {src.dtype}")
+    rows, cols = src.shape
+    if rows == 0 or cols == 0:
+        return dst
+    if (cols > 1 and (src.stride(1) != 1 or dst.stride(1) != 1)) or not (src.is_cuda and dst.is_cuda):
+        raise ValueError("copy_rows: rows must be contiguous device memory")
+    es = src.element_size()
+    row = cols * es  # a single row's pitch is free (its stride may be anything)
+    dp = dst.stride(0) * es if rows > 1 else row
+    sp = src.stride(0) * es if rows > 1 else row
+    _lib.check(_lib.lib().zc_copy_rows(dst.data_ptr(), dp, src.data_ptr(), sp, row, rows,
+                                       stream_handle()), "copy_rows")
+    return dst
+
+
 def parts_to_pinned(parts: list[torch.Tensor]) -> torch.Tensor:
     """Concatenate device tensors into one page-locked host buffer with one
     asynchronous device->host copy per part on the current stream (copy
