@@ -1108,26 +1108,33 @@ def main():
                 "peak_source": peak_src, "binding_unit": binding, "ms": ms_, "perms": perms_,
                 "perm_rate": perms_ / (ms_ / 1e3), "inst_per_perm": inst_per_perm}
 
-    def ntt_roof(bytes_, ms_, kernel):
+    # Thread instructions per output word of the LDE passes (ncu, 2^17 x 64
+    # blowup-4 capture) against the butterflies' own: log2(k)/2 = 8.5 radix-2
+    # butterflies per output word at ~11 field instructions each.
+    lde_radix4 = {"binding_unit": "integer issue (issue active 59-62 %, FMA-heavy pipe 64-69 % "
+                                  "in the ncu capture), not HBM",
+                  "inst_per_output_word": 175.0, "butterfly_floor_per_output_word": 93.5,
+                  "issue_frac": 93.5 / 175.0,
+                  "issue_source": "profiles/k_lde_four_step_trace_2p17x64_blowup4.md"}
+    lde_wide = {"binding_unit": "integer issue at one 512-thread CTA per SM (issue active "
+                                "46-54 % in the ncu capture), not HBM",
+                "inst_per_output_word": 136.7, "butterfly_floor_per_output_word": 93.5,
+                "issue_frac": 93.5 / 136.7,
+                "issue_source": "profiles/k_lde_wide_trace_2p17x64_blowup4.md"}
+
+    def ntt_roof(bytes_, ms_, kernel, issue):
         ach = bytes_ / (ms_ / 1e3) / 1e9
         return {"bound": "hbm", "kernel": kernel, "achieved": ach, "peak": hbm_peak,
                 "unit": "GB/s", "frac": ach / hbm_peak, "ms": ms_,
-                "peak_source": "MEASURED_PEAKS.json hbm_gbs (of measured)",
-                "binding_unit": "integer issue (issue active 59-62 %, FMA-heavy pipe 64-69 % in "
-                                "the ncu capture), not HBM",
-                # thread instructions per output word (ncu, 2^17 x 64 blowup-4 capture)
-                # against the butterflies' own: log2(k)/2 radix-2 butterflies per
-                # output word at ~11 field instructions each
-                "inst_per_output_word": 175.0, "butterfly_floor_per_output_word": 93.5,
-                "issue_frac": 93.5 / 175.0,
-                "issue_source": "profiles/k_lde_four_step_trace_2p17x64_blowup4.md"}
+                "peak_source": "MEASURED_PEAKS.json hbm_gbs (of measured)", **issue}
 
     trace_roof = hash_roof(perms, hash_ms, "Poseidon2 Merkle hashing of the 2^20 x 64 trace "
                            "commit (k_leaf leaves + levels + fused top)",
                            traffic_per_word * info["leaves"] * args.cols)
     trace_roof["traffic_note"] = "bytes per launch, scaled from the 2^19 x 64 ncu capture"
     trace_ntt = ntt_roof(info["ntt_bytes"], ntt_ms, "coset LDE of the 2^20 x 64 trace "
-                                                    "(k_lde_pass1 + pass2)")
+                                                    "(k_lde_pass1 + pass2, radix-2^5 variant)",
+                         lde_wide)
     if served_roof is not None:
         roofline = hash_roof(served_roof["perms"], served_roof["hash_ms"],
                              "Poseidon2 pair-leaf Merkle hashing of the served stream "
@@ -1137,7 +1144,8 @@ def main():
                                     "each codeword word once (trace capture: 1.00x the "
                                     "algorithmic bytes)")
         roofline_ntt = ntt_roof(served_roof["lde_bytes"], served_roof["lde_ms"],
-                                "coset LDE of the served stream (k_lde_batch phases)")
+                                "coset LDE of the served stream (k_lde_batch phases)",
+                                lde_radix4)
     else:
         roofline, roofline_ntt = trace_roof, trace_ntt
     out = {

@@ -122,6 +122,11 @@ def pass2(z, out, c, tile, lk1, lk2, lb, ltt, max_r, brev_out, writes):
     oc = c << ln
     wk = root(lk)
     ps = passes(lk1, max_r)
+    if len(ps) > 1 and lk1 - ps[0][1] < 5:  # the smaller radix first (lde_pass2_fused)
+        r0 = lk1 // len(ps)
+        rest = passes(lk1 - r0, max_r)
+        assert len(rest) == len(ps) - 1
+        ps = [(lk1 - 1, r0)] + [(h0, r) for h0, r in rest]
 
     def put(pos, val):
         out[pos] = val

@@ -546,7 +546,11 @@ __device__ void lde_pass2_fused(const uint32_t* z, uint32_t* out, int log_k1, in
   const int passes = pass_count(log_k1, max_r);
   int h0 = log_k1 - 1;
   for (int q = 0; q < passes; q++) {
-    const int R = pass_radix(h0, passes, q);
+    int R = pass_radix(h0, passes, q);
+    // the first pass maps a warp onto 2^(log_k1 - R) consecutive offsets of a
+    // row: keep that at >= 32 (conflict-free shared-memory writes) by taking
+    // the smaller radix first (a 2^9 row: 4 + 5, not 5 + 4)
+    if (q == 0 && passes > 1 && log_k1 - R < 5) R = log_k1 / passes;
     const bool first = q == 0, last = q == passes - 1;
     if (first) {
       switch (R) {
