@@ -179,10 +179,17 @@ constexpr int kMaxRadixLog = 4;
 // The wide four-step variant (k_lde_pass1/2 with MR = 5): radix-2^5 register
 // passes -- two passes for a 2^10 row instead of three, so one shared-memory
 // round trip and one barrier fewer per four-step pass -- need 128 registers,
-// hence one 512-thread CTA per SM, fed by 2^15-word (128 KB) tiles so that
-// enough loads stay in flight. Used for large transforms (lde_launch).
+// hence 512 threads per SM: two 256-thread CTAs on 2^14-word tiles (one CTA's
+// loads overlap the other's arithmetic), or one 512-thread CTA on 2^15-word
+// tiles. Used for large transforms (lde_launch).
 constexpr int kWideRadixLog = 5;
-constexpr int kWideTileLog = 15;
+#ifndef ZC_LDE_WIDE_THREADS
+#define ZC_LDE_WIDE_THREADS 256
+#endif
+static_assert(ZC_LDE_WIDE_THREADS == 256 || ZC_LDE_WIDE_THREADS == 512,
+              "wide LDE CTAs of 256 or 512 threads");
+constexpr int kWideThreads = ZC_LDE_WIDE_THREADS;
+constexpr int kWideTileLog = kWideThreads == 256 ? 14 : 15;
 
 // max_r (2..4) bounds the passes' radix: ceil(logm / max_r) balanced passes.
 template <class F>
@@ -206,6 +213,16 @@ __device__ void smem_ntt_dif(uint32_t* a, int log_rows, int logm, int rs, const 
 
 constexpr int kThreads = 512;
 [[maybe_unused]] constexpr int kLogThreads = 9;
+// Threads and resident CTAs per SM of the four-step passes with largest radix
+// 2^MR: the wide build's 128 registers allow 512 threads per SM.
+template <int MR>
+constexpr int lde_threads() {
+  return MR > 4 ? kWideThreads : kThreads;
+}
+template <int MR>
+constexpr int lde_min_blocks() {
+  return MR > 4 ? 65536 / (128 * kWideThreads) : 2;
+}
 
 // Asynchronous 4-byte global -> shared copies (cp.async): a tile's loads are
 // all in flight at once, overlapping the twiddle-table set-up, instead of one
@@ -583,7 +600,7 @@ __device__ void lde_pass2_fused(const uint32_t* z, uint32_t* out, int log_k1, in
 }
 
 template <class F, int MR = kMaxRadixLog>
-__global__ void __launch_bounds__(kThreads, MR > 4 ? 1 : 2) k_lde_pass1(const uint32_t* x, uint32_t* z, int log_k1,
+__global__ void __launch_bounds__(lde_threads<MR>(), lde_min_blocks<MR>()) k_lde_pass1(const uint32_t* x, uint32_t* z, int log_k1,
                                                         int log_k2, int log_b, int log_ti,
                                                         uint32_t h) {
   extern __shared__ uint32_t sm[];
@@ -676,7 +693,7 @@ __device__ void lde_pass2_body(const uint32_t* z, uint32_t* out, int log_k1, int
 }
 
 template <class F, int MR = kMaxRadixLog>
-__global__ void __launch_bounds__(kThreads, MR > 4 ? 1 : 2) k_lde_pass2(const uint32_t* z, uint32_t* out,
+__global__ void __launch_bounds__(lde_threads<MR>(), lde_min_blocks<MR>()) k_lde_pass2(const uint32_t* z, uint32_t* out,
                                                         int log_k1, int log_k2, int log_b,
                                                         int log_tt, int brev_out) {
   extern __shared__ uint32_t sm[];
@@ -726,9 +743,9 @@ inline LdePlan plan_lde(int log_k, int log_b, int tile_log = 0, int max_r = kMax
 }
 
 // Whether a four-step LDE of `batch` columns of 2^log_n outputs takes the
-// wide variant: at least two of its 2^15-word tiles per SM, so that one
-// resident CTA per SM still fills the GPU (2^20 x 64 at blowup 4: 2.10 ms
-// against 2.23 ms for the radix-2^4 form on the GB300).
+// wide variant: at least two of its tiles per SM (2^20 x 64 at blowup 4 with
+// one 512-thread CTA per SM: 2.10 ms against 2.23 ms for the radix-2^4 form
+// on the GB300).
 inline bool lde_wide(int64_t batch, int log_n) {
 #if ZC_LDE_FUSED
   static const int sms = [] {
@@ -808,12 +825,13 @@ zc_status lde_four_step(const uint32_t* x, int64_t batch, int log_k, int log_b, 
   for (int64_t c0 = 0; c0 < batch; c0 += chunk) {
     const int64_t cols = batch - c0 < chunk ? batch - c0 : chunk;
     dim3 g1(1u << log_b, 1u << (p.log_k1 - p.log_ti), (unsigned)cols);
-    k_lde_pass1<F, MR><<<g1, kThreads, p.smem1, st>>>(x + (c0 << log_k), z, p.log_k1, p.log_k2,
-                                                      log_b, p.log_ti, h);
+    k_lde_pass1<F, MR><<<g1, lde_threads<MR>(), p.smem1, st>>>(x + (c0 << log_k), z, p.log_k1,
+                                                               p.log_k2, log_b, p.log_ti, h);
     ZC_TRY(launch_check());
     dim3 g2(1u << (p.log_k2 - p.log_tt), (unsigned)cols);
-    k_lde_pass2<F, MR><<<g2, kThreads, p.smem2, st>>>(z, out + (c0 << log_n), p.log_k1,
-                                                      p.log_k2, log_b, p.log_tt, brev_out);
+    k_lde_pass2<F, MR><<<g2, lde_threads<MR>(), p.smem2, st>>>(z, out + (c0 << log_n), p.log_k1,
+                                                               p.log_k2, log_b, p.log_tt,
+                                                               brev_out);
     ZC_TRY(launch_check());
   }
   return ZC_OK;
