@@ -1116,8 +1116,8 @@ def main():
                   "inst_per_output_word": 175.0, "butterfly_floor_per_output_word": 93.5,
                   "issue_frac": 93.5 / 175.0,
                   "issue_source": "profiles/k_lde_four_step_trace_2p17x64_blowup4.md"}
-    lde_wide = {"binding_unit": "integer issue at one 512-thread CTA per SM (issue active "
-                                "46-54 % in the ncu capture), not HBM",
+    lde_wide = {"binding_unit": "integer issue at 512 threads per SM (128 registers per "
+                                "thread; issue active 49-55 % in the ncu capture), not HBM",
                 "inst_per_output_word": 136.7, "butterfly_floor_per_output_word": 93.5,
                 "issue_frac": 93.5 / 136.7,
                 "issue_source": "profiles/k_lde_wide_trace_2p17x64_blowup4.md"}
