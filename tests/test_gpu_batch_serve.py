@@ -117,6 +117,37 @@ def test_autotuner_choice_keeps_bytes(tmp_path):
         assert torch.equal(x.layers.flat, y.layers.flat)
 
 
+def test_large_jobs_on_single_matrix_kernels_keep_bytes():
+    """Jobs of at least direct_min_words codeword words run on the single-matrix
+    kernels inside a batch (eager and graphed): the codewords and digest
+    layers equal those of the work-list kernels, natural and bit-reversed."""
+    from zorch_gb300.batch import BatchCommitter, GraphedBatch, MatrixJob
+
+    def fill(w, log_h, seed):
+        from zorch_gb300.field import ptr, stream_handle, to_mont
+
+        x = torch.empty((w, 1 << log_h), dtype=torch.int32, device="cuda")
+        _lib.check(_lib.lib().zc_fill_uniform(0, ptr(x), x.numel(), seed, stream_handle()), "fill")
+        return to_mont(BABYBEAR, x)
+
+    # (width, log2 height, log2 blowup): the first and third reach 2^22 codeword words
+    shapes = [(8, 20, 1), (3, 12, 2), (2, 19, 3), (1, 16, 1)]
+    mats = [(fill(w, lh, 40 + i), lb) for i, (w, lh, lb) in enumerate(shapes)]
+    for br in (False, True):
+        jobs = [MatrixJob(x, lb, bit_reversed=br) for x, lb in mats]
+        want = BatchCommitter(direct_min_words=0).commit(jobs)
+        got = BatchCommitter(direct_min_words=1 << 22).commit(jobs)
+        for a, b in zip(got, want):
+            assert torch.equal(a.codeword, b.codeword)
+            assert torch.equal(a.layers.flat, b.layers.flat)
+    g = GraphedBatch(BatchCommitter(direct_min_words=1 << 22), [(x.shape[0], x.shape[1], lb)
+                                                                for x, lb in mats])
+    want = BatchCommitter(direct_min_words=0).commit([MatrixJob(x, lb) for x, lb in mats])
+    for a, b in zip(g.replay([x for x, _ in mats]), want):
+        assert torch.equal(a.codeword, b.codeword)
+        assert torch.equal(a.layers.flat, b.layers.flat)
+
+
 @pytest.mark.parametrize("tile,radix,top", [(13, 2, 1), (15, 3, 4), (14, 4, 8), (0, 2, 6)])
 def test_tuning_choices_keep_bytes(tile, radix, top):
     """Every tile, radix and tree-top depth the tuner may pick gives the same

@@ -118,10 +118,15 @@ def test_config4_uneven_batch_bytes(orc):
         _lib.check(_lib.lib().zc_fill_uniform(0, ptr(xx), xx.numel(), 900 + i, stream_handle()),
                    "fill")
         canon.append(xx)
-    bc = BatchCommitter()
-    batched = bc.commit([MatrixJob(to_mont(BABYBEAR, x), lb) for x, (_, _, lb) in
-                         zip(canon, shapes)])
+    # every job on the work-list kernels (direct_min_words=0), then the default
+    # routing (the largest jobs on the single-matrix kernels): same roots
+    bc = BatchCommitter(direct_min_words=0)
+    jobs = [MatrixJob(to_mont(BABYBEAR, x), lb) for x, (_, _, lb) in zip(canon, shapes)]
+    batched = bc.commit(jobs)
     roots = [to_host(b.root) for b in batched]
+    routed = BatchCommitter().commit(jobs)
+    assert all(np.array_equal(to_host(r.root), root) for r, root in zip(routed, roots))
+    del routed, jobs
     tree = MerkleTree(bc.perm, column_major=True)
     for b in batched[:6]:  # per-matrix commit == batched, layer for layer
         _, layers = tree.commit(b.codeword)

@@ -149,6 +149,22 @@ def test_batch_committer_choice_prefers_overrides():
     assert bc._choice(20, 8) == {"tile": 0, "radix": 4, "top": 0}
 
 
+def test_batch_committer_routes_large_jobs_to_single_matrix_kernels():
+    """Jobs whose codeword reaches direct_min_words words take the single-matrix
+    kernels, in job order; the rest stay on the work lists; 0 turns it off."""
+    import torch
+
+    from zorch_gb300.batch import BatchCommitter, MatrixJob
+
+    bc = BatchCommitter.__new__(BatchCommitter)
+    bc.direct_min_words = 1 << 22
+    jobs = [MatrixJob(torch.empty((w, 1 << lh), dtype=torch.int32), lb)
+            for w, lh, lb in [(8, 20, 1), (3, 12, 2), (2, 19, 3), (1, 16, 1), (64, 15, 1)]]
+    assert bc._split(jobs) == ([0, 2, 4], [1, 3])
+    bc.direct_min_words = 0
+    assert bc._split(jobs) == ([], [0, 1, 2, 3, 4])
+
+
 def test_xla_ffi_shim_is_header_gated(tmp_path, monkeypatch):
     """libzc_xla.so is built only where xla/ffi/api/ffi.h is found; the
     committed handlers name the four custom-call targets."""

@@ -148,18 +148,19 @@ class Autotuner:
         best, best_ms = (0, 0), float("inf")
         for tl in _TILE_CANDIDATES:
             for rx in _RADIX_CANDIDATES:
-                bc = BatchCommitter(perm, f, tuner=None, tile_override=tl, radix_override=rx)
+                bc = BatchCommitter(perm, f, tuner=None, tile_override=tl, radix_override=rx,
+                                    direct_min_words=0)
                 try:
                     ms = self._time(lambda: bc.encode([job]), reps)
                 except (NotImplementedError, ValueError):
                     continue
                 if ms < best_ms:
                     best, best_ms = (tl, rx), ms
-        bc = BatchCommitter(perm, f, tuner=None)
+        bc = BatchCommitter(perm, f, tuner=None, direct_min_words=0)
         cw = bc.encode([job])
         top, top_ms = 0, float("inf")
         for tp in _TOP_CANDIDATES:
-            bt = BatchCommitter(bc.perm, f, tuner=None, top_override=tp)
+            bt = BatchCommitter(bc.perm, f, tuner=None, top_override=tp, direct_min_words=0)
             ms = self._time(lambda: bt.merkle(cw), reps)
             if ms < top_ms:
                 top, top_ms = tp, ms
@@ -169,9 +170,23 @@ class Autotuner:
 
 
 class BatchCommitter:
+    """Many matrices per commit: the LDEs of all jobs in two work-list
+    launches, all their trees in one work-list launch per level. A job whose
+    codeword has at least `direct_min_words` words (2^24 by default) fills the
+    GPU on its own, gains nothing from sharing launches and runs on the
+    single-matrix kernels instead (zc_rs_encode, zc_merkle_commit: the radix-2^5
+    LDE build, the fused subtree tops), in job order on the same stream; every
+    byte is the same either way (config 4's 48 matrices: 1.02x the plain path
+    routed, 0.98x all on work lists). The per-column pair-leaf trees of
+    pair_trees stay on the tree-family work list at every size: one
+    single-tree commit per column measured slower on the served stream and
+    filled the launch queue, so the server thread blocked behind a large
+    request (p50 26 ms -> 987 ms)."""
+
     def __init__(self, perm: Poseidon2 | None = None, field=BABYBEAR, generator: int | None = None,
                  tuner: Autotuner | None = None, tile_override: int = 0,
-                 radix_override: int = 0, top_override: int = 0) -> None:
+                 radix_override: int = 0, top_override: int = 0,
+                 direct_min_words: int = 1 << 24) -> None:
         self.field = field_of(field)
         self.perm = perm if perm is not None else Poseidon2.builtin(self.field)
         self.generator = generator or 0
@@ -179,6 +194,10 @@ class BatchCommitter:
         self.tile_override = tile_override
         self.radix_override = radix_override
         self.top_override = top_override
+        self.direct_min_words = direct_min_words
+
+    def _direct(self, width: int, n: int) -> bool:
+        return self.direct_min_words > 0 and width * n >= self.direct_min_words
 
     def _choice(self, log_n: int, width: int) -> dict:
         c = self.tuner.choice(log_n, width) if self.tuner else {"tile": 0, "radix": 0, "top": 0}
@@ -196,6 +215,26 @@ class BatchCommitter:
                                  c["tile"], int(j.bit_reversed), c["radix"])
         return arr
 
+    def _split(self, jobs: list[MatrixJob]) -> tuple[list[int], list[int]]:
+        direct = [i for i, j in enumerate(jobs) if self._direct(j.width, j.height << j.log_blowup)]
+        ds = set(direct)
+        return direct, [i for i in range(len(jobs)) if i not in ds]
+
+    def encode_workspace_bytes(self, jobs: list[MatrixJob], outs: list[torch.Tensor]) -> int:
+        """Workspace bytes encode() needs for these jobs (the work-list jobs'
+        and each single-matrix job's, one after another on one buffer)."""
+        L = _lib.lib()
+        direct, batched = self._split(jobs)
+        need = 0
+        if batched:
+            arr = self._lde_jobs([jobs[i] for i in batched], [outs[i] for i in batched])
+            need = L.zc_rs_encode_batch_workspace_bytes(arr, len(batched))
+        for i in direct:
+            j = jobs[i]
+            need = max(need, L.zc_rs_encode_workspace_bytes(j.width, j.height.bit_length() - 1,
+                                                            j.log_blowup))
+        return need
+
     def encode(self, jobs: list[MatrixJob], outs: list[torch.Tensor] | None = None,
                workspace: torch.Tensor | None = None) -> list[torch.Tensor]:
         for j in jobs:
@@ -205,14 +244,23 @@ class BatchCommitter:
         if outs is None:
             outs = [torch.empty((j.width, j.height << j.log_blowup), dtype=torch.int32,
                                 device=j.columns.device) for j in jobs]
-        arr = self._lde_jobs(jobs, outs)
         L = _lib.lib()
-        need = L.zc_rs_encode_batch_workspace_bytes(arr, len(jobs))
+        need = self.encode_workspace_bytes(jobs, outs)
         if workspace is None or workspace.numel() * 4 < need:
             workspace = torch.empty((need + 3) // 4, dtype=torch.int32, device=jobs[0].columns.device)
-        _lib.check(L.zc_rs_encode_batch(self.field.id, arr, len(jobs), self.generator,
-                                        ptr(workspace), workspace.numel() * 4, stream_handle()),
-                   "rs_encode_batch")
+        direct, batched = self._split(jobs)
+        for i in direct:
+            j, o = jobs[i], outs[i]
+            fn = L.zc_rs_encode_bitrev if j.bit_reversed else L.zc_rs_encode
+            _lib.check(fn(self.field.id, ptr(j.columns), j.width, j.height.bit_length() - 1,
+                          j.log_blowup, self.field.mont(j.shift) if j.shift else 0,
+                          self.generator, ptr(o), ptr(workspace), workspace.numel() * 4,
+                          stream_handle()), "rs_encode")
+        if batched:
+            arr = self._lde_jobs([jobs[i] for i in batched], [outs[i] for i in batched])
+            _lib.check(L.zc_rs_encode_batch(self.field.id, arr, len(batched), self.generator,
+                                            ptr(workspace), workspace.numel() * 4,
+                                            stream_handle()), "rs_encode_batch")
         return outs
 
     # -- Merkle ----------------------------------------------------------------
@@ -221,16 +269,27 @@ class BatchCommitter:
         if flats is None:
             flats = [torch.empty((2 * cw.shape[1] - 1, 8), dtype=torch.int32, device=cw.device)
                      for cw in codewords]
-        arr = (_lib.MerkleJob * len(codewords))()
+        L = _lib.lib()
+        batched = []
         for i, (cw, fl) in enumerate(zip(codewords, flats)):
             w, n = cw.shape
-            top = self._choice(n.bit_length() - 1, w)["top"]
-            arr[i] = _lib.MerkleJob(_lib.Leaves(ptr(cw), n, w, 1, n), ptr(fl), top)
-        if counters is None:
-            counters = torch.empty(64, dtype=torch.int32, device=codewords[0].device)
-        _lib.check(_lib.lib().zc_merkle_commit_batch(self.perm.handle, arr, len(codewords),
-                                                     ptr(counters), counters.numel() * 4,
-                                                     stream_handle()), "merkle_commit_batch")
+            if self._direct(w, n):
+                _lib.check(L.zc_merkle_commit(self.perm.handle, _lib.Leaves(ptr(cw), n, w, 1, n),
+                                              ptr(fl), stream_handle()), "merkle_commit")
+            else:
+                batched.append(i)
+        if batched:
+            arr = (_lib.MerkleJob * len(batched))()
+            for a, i in enumerate(batched):
+                cw, fl = codewords[i], flats[i]
+                w, n = cw.shape
+                top = self._choice(n.bit_length() - 1, w)["top"]
+                arr[a] = _lib.MerkleJob(_lib.Leaves(ptr(cw), n, w, 1, n), ptr(fl), top)
+            if counters is None:
+                counters = torch.empty(64, dtype=torch.int32, device=codewords[0].device)
+            _lib.check(L.zc_merkle_commit_batch(self.perm.handle, arr, len(batched), ptr(counters),
+                                                counters.numel() * 4, stream_handle()),
+                       "merkle_commit_batch")
         return [DigestLayers(fl, cw.shape[1]) for fl, cw in zip(flats, codewords)]
 
     def commit(self, jobs: list[MatrixJob]) -> list[CommittedMatrix]:
@@ -312,9 +371,8 @@ class GraphedBatch:
                      for w, h, lb in shapes]
         self.flats = [torch.empty((2 * (h << lb) - 1, 8), dtype=torch.int32, device=device)
                       for w, h, lb in shapes]
-        arr = committer._lde_jobs(self.jobs, self.outs)
-        need = _lib.lib().zc_rs_encode_batch_workspace_bytes(arr, len(self.jobs))
-        self.ws = torch.empty((need + 3) // 4, dtype=torch.int32, device=device)
+        need = committer.encode_workspace_bytes(self.jobs, self.outs)
+        self.ws = torch.empty(max(1, (need + 3) // 4), dtype=torch.int32, device=device)
         self.ctr = torch.empty(64, dtype=torch.int32, device=device)
         # warm up once outside capture (sets kernel attributes), then capture
         self._run()
