@@ -391,7 +391,6 @@ def served_hash_roofline(reqs, server, mode):
     Returns (lde_ms, hash_ms, permutations, lde_bytes)."""
     import torch
 
-    from zorch_gb300 import _lib
     from zorch_gb300.batch import MatrixJob
     from zorch_gb300.field import BABYBEAR, to_mont
     from zorch_gb300.serve import FRI_LAYER_CAP
@@ -405,8 +404,7 @@ def served_hash_roofline(reqs, server, mode):
         w, n = r.width, 1 << r.log_n
         job = MatrixJob(x, r.log_blowup, 31)
         cw = torch.empty((w, n), dtype=torch.int32, device=x.device)
-        arr = bc._lde_jobs([job], [cw])
-        ws = torch.empty((_lib.lib().zc_rs_encode_batch_workspace_bytes(arr, 1) + 3) // 4 + 64,
+        ws = torch.empty((bc.encode_workspace_bytes([job], [cw]) + 3) // 4 + 64,
                          dtype=torch.int32, device=x.device)
         ws = ws[(-ws.data_ptr() % 256) // 4:]  # 256-byte aligned view
         if mode == "fri":
@@ -1108,14 +1106,10 @@ def main():
                 "peak_source": peak_src, "binding_unit": binding, "ms": ms_, "perms": perms_,
                 "perm_rate": perms_ / (ms_ / 1e3), "inst_per_perm": inst_per_perm}
 
-    # Thread instructions per output word of the LDE passes (ncu, 2^17 x 64
-    # blowup-4 capture) against the butterflies' own: log2(k)/2 = 8.5 radix-2
-    # butterflies per output word at ~11 field instructions each.
-    lde_radix4 = {"binding_unit": "integer issue (issue active 59-62 %, FMA-heavy pipe 64-69 % "
-                                  "in the ncu capture), not HBM",
-                  "inst_per_output_word": 175.0, "butterfly_floor_per_output_word": 93.5,
-                  "issue_frac": 93.5 / 175.0,
-                  "issue_source": "profiles/k_lde_four_step_trace_2p17x64_blowup4.md"}
+    # Thread instructions per output word of the radix-2^5 LDE passes (ncu,
+    # 2^17 x 64 blowup-4 capture; 175 for the radix-2^4 build) against the
+    # butterflies' own: log2(k)/2 = 8.5 radix-2 butterflies per output word at
+    # ~11 field instructions each.
     lde_wide = {"binding_unit": "integer issue at 512 threads per SM (128 registers per "
                                 "thread; issue active 49-55 % in the ncu capture), not HBM",
                 "inst_per_output_word": 136.7, "butterfly_floor_per_output_word": 93.5,
@@ -1144,8 +1138,10 @@ def main():
                                     "each codeword word once (trace capture: 1.00x the "
                                     "algorithmic bytes)")
         roofline_ntt = ntt_roof(served_roof["lde_bytes"], served_roof["lde_ms"],
-                                "coset LDE of the served stream (k_lde_batch phases)",
-                                lde_radix4)
+                                "coset LDE of the served stream (the largest requests on the "
+                                "radix-2^5 single-matrix passes, which carry most of its "
+                                "outputs; the rest on the batched radix-2^4 phases)",
+                                lde_wide)
     else:
         roofline, roofline_ntt = trace_roof, trace_ntt
     out = {
