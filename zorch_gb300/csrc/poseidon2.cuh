@@ -220,9 +220,8 @@ ZC_HD void p2_compress(const uint32_t* l, const uint32_t* r, uint32_t* out,
 //  - external layer: y_j = s_b + x_j + 2 x_{j+1} is M4 = circ(2,3,1,1) on the
 //    4-word block b (s_b = block sum, j + 1 mod 4), then y += the sum of y over
 //    the lane class (xor 4, xor 8);
-//  - partial round: every lane keeps word 0 and runs its S-box; the sum of
-//    words 1..15 for the next round is reduced while this round's S-box runs
-//    (it is 15 sum + sum_{l>=1} d_l x_l), so the chain is the S-box and two adds.
+//  - partial round: the sum of lanes 1..15 is reduced while lane 0 runs its
+//    S-box, and lane 0's new word is broadcast and added afterwards.
 // Constants come from a P2Params in shared memory. Every lane of the warp must
 // make the call (full-warp shuffles), active half or not.
 constexpr unsigned kFullMask = 0xffffffffu;
@@ -265,29 +264,17 @@ __device__ __forceinline__ uint32_t half_permute_a(uint32_t x, const P2Params* p
     x = half_ext_linear<F>(ark_sbox_a<F, ALPHA>(x, c, alpha));
     c = c_next;
   }
-  // Partial rounds. Every lane keeps word 0 (w0) and runs its S-box, so no
-  // broadcast sits on the chain; and the sum of words 1..15 entering round
-  // r+1 is 15 sum_r + sum_{l>=1} d_l x_l (x_l of round r), whose reduction
-  // runs beside round r's S-box. The chain per round is then the S-box and
-  // two adds (w0' = sum + d_0 s0, with d_0 = -2 taken on the adder).
-  uint32_t w0 = __shfl_sync(kFullMask, x, threadIdx.x & 16);
-  uint32_t rest = half_sum16<F>(l == 0 ? 0u : x);  // words 1..15
-  const uint32_t d0 = p->diag[0], c15 = to_mont<F>(15u);
-  const bool d0_neg2 = d0 == mneg<F>(to_mont<F>(2u));
 #pragma unroll 1
   for (int r = 0; r < rp; r++) {
     const uint32_t c_next = r + 1 < rp ? p->int_rc[r + 1] : p->ext_term[0][l];
-    const uint32_t s0 = ark_sbox_a<F, ALPHA>(w0, c, alpha);
-    const uint32_t dx = mmul<F>(dg, x);                    // lanes 1..15 use it
-    const uint32_t dsum = half_sum16<F>(l == 0 ? 0u : dx);  // sum_{l>=1} d_l x_l
-    uint32_t sum = madd<F>(rest, s0);
+    const uint32_t s0 = ark_sbox_a<F, ALPHA>(x, c, alpha);  // lane 0's is used
+    const uint32_t rest = half_sum16<F>(l == 0 ? 0u : x);   // lanes 1..15
+    const uint32_t dx = mmul<F>(dg, l == 0 ? s0 : x);
+    uint32_t sum = madd<F>(rest, __shfl_sync(kFullMask, s0, threadIdx.x & 16));
     if (!jone) sum = mmul<F>(sum, js);
     x = madd<F>(sum, dx);
-    w0 = d0_neg2 ? msub<F>(sum, madd<F>(s0, s0)) : madd<F>(sum, mmul<F>(d0, s0));
-    rest = madd<F>(mmul<F>(sum, c15), dsum);
     c = c_next;
   }
-  if (l == 0) x = w0;
   if (rp == 0) c = p->ext_term[0][l];
 #pragma unroll 1
   for (int r = 0; r < rfh; r++) {

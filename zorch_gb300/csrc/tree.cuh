@@ -229,8 +229,9 @@ struct FoldLeaf {
 };
 
 // Nodes per tree-top CTA of the batched commit (k_tree_top) at its first
-// level; its threads: 4 per node, so each level above is one round of
-// quarter-warp permutations.
+// level; its threads: 4 per node, so every level above is one round
+// (subtree_level: quarter-warps while a level has more than 32 parents,
+// half-warps above).
 constexpr int kSubT = 128;
 // Largest number of nodes per fused-subtree CTA (k_subtree) at its first
 // level; its threads: 4 per node (a quarter-warp permutation per parent), at
@@ -240,10 +241,10 @@ constexpr int kSubCap = 256;
 // The tree driver's shape: levels with more than `levelwise_min` nodes run one
 // thread per node; the top runs as fused subtrees of `subtree_t` first-level
 // nodes per CTA. Defaults 2^14 and 128 (the 2^22 FRI commit phase, graphed:
-// 6.01 ms against 6.08 at 2^13, 6.12 at 2^15, 6.18 with 256-node subtrees);
-// the environment variables
-// ZC_LEVELWISE_MIN_LOG (8..20) and ZC_SUBTREE_T (a power of two in 2..256)
-// override them for tuning (read once; no byte of any result depends on them).
+// 6.01 ms against 6.08 at 2^13, 6.12 at 2^15, 6.18 with 256-node subtrees).
+// The environment variables ZC_LEVELWISE_MIN_LOG (8..20) and ZC_SUBTREE_T (a
+// power of two in 2..256) override them for tuning (read once; no byte of any
+// result depends on them).
 struct TreeShape {
   int64_t levelwise_min;
   int subtree_t;
@@ -320,8 +321,8 @@ __device__ __forceinline__ void subtree_level(const uint32_t* src, uint32_t* dst
 }
 
 // One subtree of T first-level nodes per CTA (blockDim = subtree_threads(T)):
-// the first level is T leaf digests (one thread each; for NodeLeaf,
-// quarter-warps compressing stored children), then every level up to the
+// the first level is T leaf digests (one thread each; for NodeLeaf, quarter-
+// or half-warps compressing stored children), then every level up to the
 // subtree root is compressed out of ping-pong shared-memory slots
 // (subtree_level), each level written to `layers`.
 template <class K, class Leaf>
