@@ -372,7 +372,8 @@ __global__ void __launch_bounds__(1024) k_subtree(Leaf leaf, uint32_t* layers, i
 // the unbounded build gave the level form 32; the 2^22 x 64 trace hash went
 // 9.18 -> 9.00 ms); no bound for run-time parameter sets, whose constants come
 // from shared memory and which would spill under it. The batched tree kernel
-// keeps the compiler's choice: bounding it measured slower.
+// keeps the compiler's choice: bounding it to five or six resident CTAs
+// measured slower on the served stream (1.136 / 1.153 against 1.163 G elem/s).
 template <class K>
 struct HashOcc {
   static constexpr int v = 1;
