@@ -78,18 +78,40 @@ struct HostPerm {
 // Every lane of the (single) warp holds the same Duplex state and runs the same
 // control flow; a permutation runs on each half-warp (both compute the same
 // result) and is gathered back into every lane's copy.
+template <class HP>
+__device__ __forceinline__ void half_apply(uint32_t* s, const HP& perm) {
+  const int lane = threadIdx.x & 31;
+  uint32_t x = 0;
+#pragma unroll
+  for (int j = 0; j < 16; j++) x = (lane & 15) == j ? s[j] : x;
+  x = perm.half(x);
+#pragma unroll
+  for (int j = 0; j < 16; j++) s[j] = __shfl_sync(kFullMask, x, (lane & 16) | j);
+}
+
 template <class F>
 struct HalfPerm {
   const P2Params* p;  // shared memory
-  __device__ void operator()(uint32_t* s) const {
-    const int lane = threadIdx.x & 31;
-    uint32_t x = 0;
+  __device__ uint32_t half(uint32_t x) const { return p2_permute_half<F>(x, p); }
+  __device__ void operator()(uint32_t* s) const { half_apply(s, *this); }
+};
+
+// The built-in BabyBear-16 instance (half_permute_bb16): the constants of this
+// lane's word are loaded into registers once, when the transcript kernel
+// starts.
+struct HalfPermBb16 {
+  uint32_t ei[4], et[4], dg;
+  __device__ HalfPermBb16() {
+    const int l = threadIdx.x & 15;
 #pragma unroll
-    for (int j = 0; j < 16; j++) x = (lane & 15) == j ? s[j] : x;
-    x = p2_permute_half<F>(x, p);
-#pragma unroll
-    for (int j = 0; j < 16; j++) s[j] = __shfl_sync(kFullMask, x, (lane & 16) | j);
+    for (int r = 0; r < 4; r++) {
+      ei[r] = c_bb16_ext_init[r * 16 + l];
+      et[r] = c_bb16_ext_term[r * 16 + l];
+    }
+    dg = c_bb16_diag[l];
   }
+  __device__ uint32_t half(uint32_t x) const { return half_permute_bb16(x, ei, et, dg); }
+  __device__ void operator()(uint32_t* s) const { half_apply(s, *this); }
 };
 
 // duplex_observe on the device (same result): full rate blocks are absorbed
@@ -99,8 +121,8 @@ struct HalfPerm {
 // (a final fold layer, a sponge chain of hundreds of blocks) costs one
 // half-warp permutation per block and no per-word state shuffling. The
 // pending prefix and the tail take the generic path.
-template <class F>
-__device__ void duplex_observe(Duplex& t, const uint32_t* v, int64_t m, const HalfPerm<F>& perm) {
+template <class HP>
+__device__ void half_observe(Duplex& t, const uint32_t* v, int64_t m, const HP& perm) {
   if (m <= 0) return;
   int pos = t.in_pos & 7;
   int64_t i = 0;
@@ -122,7 +144,7 @@ __device__ void duplex_observe(Duplex& t, const uint32_t* v, int64_t m, const Ha
       const uint32_t cur = nxt;
       if (m - i >= 16 && l < 8) nxt = v[i + 8 + l];  // issued before the permutation
       if (l < 8) x = cur;
-      x = p2_permute_half<F>(x, perm.p);
+      x = perm.half(x);
     }
 #pragma unroll
     for (int j = 0; j < 16; j++) t.sponge[j] = __shfl_sync(kFullMask, x, (lane & 16) | j);
@@ -139,6 +161,14 @@ __device__ void duplex_observe(Duplex& t, const uint32_t* v, int64_t m, const Ha
     for (int j = 0; j < 8; j++) t.out_buf[j] = 0;
     t.out_pos = 0;
   }
+}
+template <class F>
+__device__ void duplex_observe(Duplex& t, const uint32_t* v, int64_t m, const HalfPerm<F>& perm) {
+  half_observe(t, v, m, perm);
+}
+__device__ inline void duplex_observe(Duplex& t, const uint32_t* v, int64_t m,
+                                      const HalfPermBb16& perm) {
+  half_observe(t, v, m, perm);
 }
 
 }  // namespace zc

@@ -389,6 +389,32 @@ __device__ __forceinline__ void p2_permute_quarter(uint32_t (&x)[4], const P2Par
   }
 }
 
+// The built-in BabyBear-16 instance on a half-warp, for permutations that run
+// alone (the transcript's one-warp chains): the same rounds as half_permute_a,
+// unrolled, with this lane's external-round constants and diagonal entry
+// passed in registers (ei, et, dg: loaded once per kernel) and the
+// partial-round constants read as constant-bank operands, so no round loads
+// a constant or runs loop control.
+static_assert(ZC_BB16_ROUNDS_F_HALF == 4, "built-in instance: 4 + 4 full rounds");
+__device__ __forceinline__ uint32_t half_permute_bb16(uint32_t x, const uint32_t (&ei)[4],
+                                                      const uint32_t (&et)[4], uint32_t dg) {
+  using F = BabyBear;
+  const int l = threadIdx.x & 15;
+  x = half_ext_linear<F>(x);
+#pragma unroll
+  for (int r = 0; r < 4; r++) x = half_ext_linear<F>(ark_sbox_a<F, 7>(x, ei[r], 7));
+#pragma unroll
+  for (int r = 0; r < ZC_BB16_ROUNDS_P; r++) {
+    const uint32_t s0 = ark_sbox_a<F, 7>(x, c_bb16_int_rc[r], 7);  // lane 0's is used
+    const uint32_t rest = half_sum16<F>(l == 0 ? 0u : x);           // lanes 1..15
+    const uint32_t dx = mmul<F>(dg, l == 0 ? s0 : x);
+    x = madd<F>(madd<F>(rest, __shfl_sync(kFullMask, s0, threadIdx.x & 16)), dx);
+  }
+#pragma unroll
+  for (int r = 0; r < 4; r++) x = half_ext_linear<F>(ark_sbox_a<F, 7>(x, et[r], 7));
+  return x;
+}
+
 // Stage run-time params into shared memory (whole block participates).
 __device__ __forceinline__ void stage_params(P2Params* dst, const P2Params* src) {
   const uint32_t* s = reinterpret_cast<const uint32_t*>(src);

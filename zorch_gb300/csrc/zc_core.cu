@@ -7,6 +7,8 @@
 #include <atomic>
 #include <mutex>
 
+#include <type_traits>
+
 #include "duplex.cuh"
 #include "internal.cuh"
 
@@ -49,6 +51,21 @@ zc_status ensure_init() {
   return ZC_OK;
 }
 
+// Calls fn(perm) with the transcript's half-warp permutation: the unrolled
+// built-in form for the built-in instance, the run-time form (constants
+// staged to shared memory) otherwise.
+template <class K, class Fn>
+__device__ __forceinline__ void with_half_perm(const P2Params* rt, P2Params* s_rt, Fn&& fn) {
+  if constexpr (std::is_same<K, Bb16Builtin>::value) {
+    const HalfPermBb16 perm;
+    fn(perm);
+  } else {
+    KIn<K>::make(rt, s_rt);
+    const HalfPerm<typename K::F> perm{KIn<K>::half(rt, s_rt)};
+    fn(perm);
+  }
+}
+
 // One warp; lane 0 writes the results.
 template <class K>
 __global__ void __launch_bounds__(32) k_duplex_step(const P2Params* rt, uint32_t* state,
@@ -56,21 +73,21 @@ __global__ void __launch_bounds__(32) k_duplex_step(const P2Params* rt, uint32_t
                                                     uint32_t* out, int32_t* positions,
                                                     int64_t block_len) {
   __shared__ P2Params s_rt;
-  KIn<K>::make(rt, &s_rt);
-  const HalfPerm<typename K::F> perm{KIn<K>::half(rt, &s_rt)};
-  Duplex t;
-  memcpy(&t, state, sizeof(Duplex));
-  duplex_observe(t, values, m, perm);
-  for (int i = 0; i < n; i++) {
-    uint32_t w;
-    duplex_sample(t, 1, &w, perm);
-    if (threadIdx.x == 0) {
-      if (out) out[i] = w;
-      if (positions) positions[i] = (int32_t)(w % (uint32_t)block_len);
+  with_half_perm<K>(rt, &s_rt, [&](const auto& perm) {
+    Duplex t;
+    memcpy(&t, state, sizeof(Duplex));
+    duplex_observe(t, values, m, perm);
+    for (int i = 0; i < n; i++) {
+      uint32_t w;
+      duplex_sample(t, 1, &w, perm);
+      if (threadIdx.x == 0) {
+        if (out) out[i] = w;
+        if (positions) positions[i] = (int32_t)(w % (uint32_t)block_len);
+      }
     }
-  }
-  __syncwarp();
-  if (threadIdx.x == 0) memcpy(state, &t, sizeof(Duplex));
+    __syncwarp();
+    if (threadIdx.x == 0) memcpy(state, &t, sizeof(Duplex));
+  });
 }
 
 template <class K>
@@ -80,32 +97,32 @@ __global__ void __launch_bounds__(32) k_duplex_hop(
     uint32_t* in_buf_o, uint32_t* out_buf_o, uint32_t* sponge_o, uint32_t* in_pos_o,
     uint32_t* out_pos_o, uint32_t* chal) {
   __shared__ P2Params s_rt;
-  KIn<K>::make(rt, &s_rt);
-  const HalfPerm<typename K::F> perm{KIn<K>::half(rt, &s_rt)};
-  Duplex t;
-  for (int j = 0; j < 8; j++) {
-    t.in_buf[j] = in_buf[j];
-    t.out_buf[j] = out_buf[j];
-  }
-  for (int j = 0; j < 16; j++) t.sponge[j] = sponge[j];
-  t.in_pos = (int32_t)in_pos[0];
-  t.out_pos = (int32_t)out_pos[0];
-  duplex_observe(t, values, m, perm);
-  for (int i = 0; i < n; i++) {
-    uint32_t w;
-    duplex_sample(t, 1, &w, perm);
-    if (threadIdx.x == 0) chal[i] = w;
-  }
-  // inputs may alias outputs: every lane has read them by now
-  __syncwarp();
-  if (threadIdx.x != 0) return;
-  for (int j = 0; j < 8; j++) {
-    in_buf_o[j] = t.in_buf[j];
-    out_buf_o[j] = t.out_buf[j];
-  }
-  for (int j = 0; j < 16; j++) sponge_o[j] = t.sponge[j];
-  in_pos_o[0] = (uint32_t)t.in_pos;
-  out_pos_o[0] = (uint32_t)t.out_pos;
+  with_half_perm<K>(rt, &s_rt, [&](const auto& perm) {
+    Duplex t;
+    for (int j = 0; j < 8; j++) {
+      t.in_buf[j] = in_buf[j];
+      t.out_buf[j] = out_buf[j];
+    }
+    for (int j = 0; j < 16; j++) t.sponge[j] = sponge[j];
+    t.in_pos = (int32_t)in_pos[0];
+    t.out_pos = (int32_t)out_pos[0];
+    duplex_observe(t, values, m, perm);
+    for (int i = 0; i < n; i++) {
+      uint32_t w;
+      duplex_sample(t, 1, &w, perm);
+      if (threadIdx.x == 0) chal[i] = w;
+    }
+    // inputs may alias outputs: every lane has read them by now
+    __syncwarp();
+    if (threadIdx.x != 0) return;
+    for (int j = 0; j < 8; j++) {
+      in_buf_o[j] = t.in_buf[j];
+      out_buf_o[j] = t.out_buf[j];
+    }
+    for (int j = 0; j < 16; j++) sponge_o[j] = t.sponge[j];
+    in_pos_o[0] = (uint32_t)t.in_pos;
+    out_pos_o[0] = (uint32_t)t.out_pos;
+  });
 }
 
 template <class F>
