@@ -275,6 +275,23 @@ template <class F>
 __device__ __forceinline__ uint32_t half_perm(uint32_t x, const P2Params* hp) {
   return p2_permute_half<F>(x, hp);
 }
+// The same for the provider K: the built-in instance runs unrolled
+// (half_permute_bb16), its lane constants read from the staged copy.
+template <class K>
+__device__ __forceinline__ uint32_t half_perm_k(uint32_t x, const P2Params* hp) {
+  if constexpr (std::is_same<K, Bb16Builtin>::value) {
+    const int l = threadIdx.x & 15;
+    uint32_t ei[4], et[4];
+#pragma unroll
+    for (int r = 0; r < 4; r++) {
+      ei[r] = hp->ext_init[r][l];
+      et[r] = hp->ext_term[r][l];
+    }
+    return half_permute_bb16(x, ei, et, hp->diag[l]);
+  } else {
+    return p2_permute_half<typename K::F>(x, hp);
+  }
+}
 
 // One level of a subtree: parent i (< width) = compress(children 2i, 2i+1)
 // read from the digest slots `src` ([node][8 words], 16-byte aligned),
@@ -287,9 +304,10 @@ __device__ __forceinline__ uint32_t half_perm(uint32_t x, const P2Params* hp) {
 // counts when the level is a latency chain. Parents are taken round-robin by
 // quarter (half) g = g, g + Q, ...; a warp with no parent in a round skips it
 // (a warp-uniform branch: the shuffles need every lane of a running warp).
-template <class F>
+template <class K>
 __device__ __forceinline__ void subtree_level(const uint32_t* src, uint32_t* dst, uint32_t* lay,
                                               int width, const P2Params* hp) {
+  using F = typename K::F;
   const int t = threadIdx.x;
   if (width > (int)(blockDim.x >> 4)) {  // quarter-warps: lane q holds words 4q .. 4q+3
     const int q = t & 3, Q = blockDim.x >> 2;
@@ -313,7 +331,7 @@ __device__ __forceinline__ void subtree_level(const uint32_t* src, uint32_t* dst
   if (2 * (t >> 5) >= width) return;
   const bool on = node < width;
   uint32_t x = on ? src[16 * node + l] : 0u;
-  x = half_perm<F>(x, hp);
+  x = half_perm_k<K>(x, hp);
   if (on && l < 8) {
     lay[8 * node + l] = x;
     dst[8 * node + l] = x;
@@ -338,7 +356,7 @@ __global__ void __launch_bounds__(1024) k_subtree(Leaf leaf, uint32_t* layers, i
   const int64_t base = (int64_t)blockIdx.x * T;
   uint32_t* lay0 = layers + 8 * (level_offset(L, l0) + base);
   if constexpr (std::is_same<Leaf, NodeLeaf>::value) {
-    subtree_level<F>(leaf.in + 16 * base, sm[0], lay0, T, hp);
+    subtree_level<K>(leaf.in + 16 * base, sm[0], lay0, T, hp);
   } else {
     if (t < T) {
       uint32_t d[8];
@@ -352,7 +370,7 @@ __global__ void __launch_bounds__(1024) k_subtree(Leaf leaf, uint32_t* layers, i
     __syncthreads();
     width >>= 1;
     lvl++;
-    subtree_level<F>(sm[cur], sm[cur ^ 1],
+    subtree_level<K>(sm[cur], sm[cur ^ 1],
                      layers + 8 * (level_offset(L, lvl) + (int64_t)blockIdx.x * width), width, hp);
     cur ^= 1;
   }

@@ -148,7 +148,6 @@ __global__ void __launch_bounds__(kMaxT) k_tree_batch(const __grid_constant__ Tr
 template <class K>
 __global__ void __launch_bounds__(4 * kSubT) k_tree_top(const __grid_constant__ TreeBatch B,
                                                        const P2Params* rt) {
-  using F = typename K::F;
   constexpr int S = 2 * kSubT;  // up to 256 nodes
   __shared__ P2Params s_rt;
   __shared__ __align__(16) uint32_t sm[2][8 * S];  // [node][word] digest slots
@@ -166,7 +165,7 @@ __global__ void __launch_bounds__(4 * kSubT) k_tree_top(const __grid_constant__ 
     __syncthreads();
     width >>= 1;
     lvl++;
-    subtree_level<F>(sm[cur], sm[cur ^ 1], lay + 8 * level_offset(J.L, lvl), width, hp);
+    subtree_level<K>(sm[cur], sm[cur ^ 1], lay + 8 * level_offset(J.L, lvl), width, hp);
     cur ^= 1;
   }
 }
