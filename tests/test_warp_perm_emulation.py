@@ -1,12 +1,17 @@
-"""CPU emulation of the quarter-warp Poseidon2 permutation
-(p2_permute_quarter in zorch_gb300/csrc/poseidon2.cuh): lane q of a quarter
+"""CPU emulation of the quarter- and half-warp Poseidon2 permutations
+(p2_permute_quarter, p2_permute_half / half_permute_bb16 in
+zorch_gb300/csrc/poseidon2.cuh). Quarter: lane q of a quarter
 holds the M4 block q (state words 4q .. 4q+3); the external layer is the block
 matrix on each lane's own words plus the sums over the four blocks (the two
 xor-shuffle levels); in the partial rounds every lane keeps word 0, runs its
 S-box redundantly and forms the sum of words 1..15 from its local words and
-the same two shuffle levels. Restated with exact integers, lane by lane, and
-compared with the oracle's permutation for the built-in BabyBear-16 instance
-and the reference's KoalaBear-16 golden instance."""
+the same two shuffle levels. Half: lane l holds word l; the external layer is
+y_l = s_b + x_l + 2 x_(l+1 in its block) (the block sum s_b by two xor
+shuffles) plus the sum over the lane class l mod 4 (xor 4, xor 8); the partial
+round sums lanes 1..15 while lane 0 runs its S-box. Restated with exact
+integers, lane by lane, and compared with the oracle's permutation for the
+built-in BabyBear-16 instance and the reference's KoalaBear-16 golden
+instance."""
 
 from __future__ import annotations
 
@@ -57,8 +62,32 @@ def quarter_permute(state, ei, et, ir, dg, alpha, j, p):
     return [lanes[q][k] for q in range(4) for k in range(4)]
 
 
+def _half_ext(x, p):
+    y = []
+    for l in range(16):
+        b = l & ~3
+        s_b = sum(x[b:b + 4]) % p
+        y.append((s_b + x[l] + 2 * x[b | ((l + 1) & 3)]) % p)
+    c = [sum(y[(l & 3) + 4 * i] for i in range(4)) % p for l in range(16)]
+    return [(y[l] + c[l]) % p for l in range(16)]
+
+
+def half_permute(state, ei, et, ir, dg, alpha, j, p):
+    x = _half_ext([int(v) for v in state], p)
+    for r in range(len(ei)):
+        x = _half_ext([pow((x[l] + int(ei[r][l])) % p, alpha, p) for l in range(16)], p)
+    for r in range(len(ir)):
+        s0 = pow((x[0] + int(ir[r])) % p, alpha, p)  # lane 0's S-box
+        rest = sum(x[1:]) % p                        # lanes 1..15 (four xor levels)
+        total = (rest + s0) * j % p                  # s0 broadcast from lane 0
+        x = [(total + int(dg[l]) * (s0 if l == 0 else x[l])) % p for l in range(16)]
+    for r in range(len(et)):
+        x = _half_ext([pow((x[l] + int(et[r][l])) % p, alpha, p) for l in range(16)], p)
+    return x
+
+
 @pytest.mark.parametrize("which", ["babybear16", "koalabear16"])
-def test_quarter_layout_equals_the_oracle_permutation(orc, which):
+def test_warp_layouts_equal_the_oracle_permutation(orc, which):
     if which == "babybear16":
         p2, p, j = orc.Poseidon2.babybear16(), orc.P_BABYBEAR, 1
         field = 0
@@ -71,5 +100,5 @@ def test_quarter_layout_equals_the_oracle_permutation(orc, which):
     for _ in range(4):
         x = rng.integers(0, p, size=16, dtype=np.uint64).astype(np.uint32)
         want = orc.from_mont(field, p2.permute(orc.to_mont(field, x)))
-        got = quarter_permute(x, ei, et, ir, dg, p2.alpha, j, p)
-        assert [int(v) for v in want] == got
+        assert quarter_permute(x, ei, et, ir, dg, p2.alpha, j, p) == [int(v) for v in want]
+        assert half_permute(x, ei, et, ir, dg, p2.alpha, j, p) == [int(v) for v in want]
